@@ -1,0 +1,42 @@
+// Symbolic analysis of the normal matrix A A^T.
+// The first two functions and SymbolicFactorization mirror the reference's
+// src/ipm/symbolic.hpp:20-63 and give bit-identical results: exact minimum
+// degree with lowest-index tie-break, and the elimination tree + strictly lower
+// CSR pattern of P (A A^T) P^T. fill_reducing_ordering is the fast ordering used
+// by the solver itself.
+#pragma once
+
+#include <vector>
+
+#include "core/sparse_matrix.hpp"
+
+namespace sankhya {
+namespace ipm {
+
+struct SymbolicFactorization {
+    std::vector<Index> P;       // P[k] = original row eliminated k-th
+    std::vector<Index> P_inv;   // P_inv[original] = k
+    std::vector<Index> parent;  // elimination tree of the permuted matrix, -1 = root
+    core::CSRMatrix L_pattern;  // strictly lower pattern of L, CSR, dummy values 1.0
+};
+
+std::vector<Index> compute_amd_ordering(const core::CSRMatrix& A);
+
+void compute_symbolic_factorization(const core::CSRMatrix& A, const std::vector<Index>& P,
+                                    SymbolicFactorization& out);
+
+// Approximate minimum degree (quotient graph, element absorption, approximate
+// external degrees) on the graph of A A^T; P[k] = original row eliminated k-th.
+std::vector<Index> fill_reducing_ordering(const core::CSRMatrix& A);
+
+// Lower adjacency of A A^T in CSR with rows / columns in the given order:
+// row k lists j < k (increasing) such that rows P[k], P[j] of A share a column.
+void permuted_lower_pattern(const core::CSRMatrix& A, const std::vector<Index>& P_inv,
+                            std::vector<Index>& rowptr, std::vector<Index>& colidx);
+
+// Elimination tree of a symmetric pattern given by its strict lower rows (Liu).
+std::vector<Index> elimination_tree(Index m, const std::vector<Index>& rowptr,
+                                    const std::vector<Index>& colidx);
+
+}  // namespace ipm
+}  // namespace sankhya

@@ -1,0 +1,167 @@
+/*
+ * sk_ipm.h -- C ABI of the GB300 device Mehrotra interior-point LP engine.
+ *
+ * Plain pointers and sizes only (int32 indices, FP64 values). No exception
+ * crosses this boundary: every function returns an SK_* status code. Each entry
+ * point names the reference interface it replaces (paths inside the reference
+ * project). Device pointers are marked d_*; everything else is host memory.
+ */
+#ifndef SK_IPM_H
+#define SK_IPM_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes (0 = ok). */
+#define SK_OK 0
+#define SK_ERR_INVALID 1       /* bad argument / inconsistent sizes */
+#define SK_ERR_CUDA 2          /* CUDA runtime error (std::runtime_error in the reference, src/ipm/mehrotra_device.cu:26-43) */
+#define SK_ERR_NUMERICAL 3     /* factorisation failed for every regularisation (src/cuda/kkt.cu:600-602, 862-864) */
+#define SK_ERR_NO_DEVICE 4     /* no CUDA device visible */
+#define SK_ERR_ALLOC 5         /* device allocation failed (std::bad_alloc in src/gpu/vram_arena.cu:58-60) */
+#define SK_ERR_INTERNAL 6
+#define SK_ERR_TOO_LARGE 7     /* request exceeds a stated maximum size */
+
+/* Solver status, numbered as the reference's simplex::SimplexStatus (src/simplex/primal.hpp:26-31). */
+#define SK_STATUS_OPTIMAL 0
+#define SK_STATUS_INFEASIBLE 1
+#define SK_STATUS_UNBOUNDED 2
+#define SK_STATUS_ITERATION_LIMIT 3
+
+/* Precision of the normal-equation factorisation. */
+#define SK_PREC_FP64 0         /* plain FP64 factor (reference arithmetic) */
+#define SK_PREC_MIXED 1        /* FP32 factor + FP64 residuals / refinement, FP64 switch near convergence */
+
+/* Starting point. */
+#define SK_START_UNIT 0        /* x = s = 1, y = 0 (src/ipm/mehrotra_device.cu:93-102) */
+#define SK_START_MEHROTRA 1    /* Mehrotra's standard heuristic start */
+#define SK_START_USER 2        /* x, y, s given in sk_solver_set_start (scaled space of the caller's LP) */
+
+/* Stopping rule. */
+#define SK_CRIT_RELATIVE 0     /* rel_pinf, rel_dinf, rel_gap <= tol on the unscaled LP */
+#define SK_CRIT_REFERENCE 1    /* ||rp||_2, ||rd||_2, mu < 1e-6 on the scaled LP (src/ipm/mehrotra_device.cu:746-748) */
+
+/* Fill-reducing ordering of A A^T. */
+#define SK_ORDER_AUTO 0        /* approximate minimum degree, or one dense front when A A^T is dense */
+#define SK_ORDER_REFERENCE 1   /* exact minimum degree, lowest index wins ties (src/ipm/symbolic.cpp:11-98) */
+#define SK_ORDER_NATURAL 2
+
+typedef struct sk_options {
+    int precision;        /* SK_PREC_* (default SK_PREC_MIXED) */
+    int start;            /* SK_START_* (default SK_START_UNIT) */
+    int criteria;         /* SK_CRIT_* (default SK_CRIT_RELATIVE) */
+    double tol;           /* default 1e-8 */
+    int max_iter;         /* default 200 (src/ipm/mehrotra_device.cu:703) */
+    int ordering;         /* SK_ORDER_* (default SK_ORDER_AUTO) */
+    int verbose;          /* 0 = silent; >0 prints per-iteration lines on stderr */
+    double mu_switch;     /* mixed precision: switch the factor to FP64 once mu < mu_switch (default 1e-6) */
+    int ruiz_passes;      /* default 10 (src/ipm/mehrotra_device.cu:293) */
+} sk_options;
+
+typedef struct sk_info {
+    int status;               /* SK_STATUS_* */
+    int iterations;
+    double objective;         /* c^T x, unscaled */
+    double primal_residual;   /* reference quantities: scaled ||Ax-b||_2 */
+    double dual_residual;     /* scaled ||A^T y + s - c||_2 */
+    double duality_gap;       /* scaled mu = x^T s / n */
+    double rel_pinf, rel_dinf, rel_gap;  /* unscaled relative measures */
+    int precision_path;       /* 0 FP64 throughout, 1 FP32 throughout, 2 FP32 then FP64 */
+    int switch_iteration;     /* first FP64 iteration in mixed mode, -1 if none */
+    int factorizations;
+    int solves;
+    int refine_steps;
+    int learned_start;        /* 1 if a user / learned start was accepted */
+    double setup_ms;          /* host analysis + upload */
+    double solve_ms;          /* IPM iterations */
+    long long nnz_factor;     /* stored factor entries */
+    int num_supernodes;
+    int dense_front;          /* 1 if A A^T was treated as one dense front */
+} sk_info;
+
+/* Fills the defaults listed above. */
+void sk_options_default(sk_options* opt);
+
+/* One-shot solve of min c^T x, Ax = b, x >= 0 from host CSC arrays (rows sorted or
+ * not, no duplicates). x (n), y (m), s (n) receive the unscaled primal / dual /
+ * reduced-cost solution; any may be NULL. info may be NULL.
+ * Replaces: sankhya::ipm::MehrotraSolver(const core::Model&) + solve()
+ *           (src/ipm/mehrotra.hpp:21-31, src/ipm/mehrotra_device.cu:1049-1059). */
+int sk_ipm_solve_csc(int m, int n, const int* col_ptrs, const int* row_idx, const double* vals,
+                     const double* b, const double* c, const sk_options* opt,
+                     double* x, double* y, double* s, sk_info* info);
+
+/* Persistent solver over a batch of independent LPs (num_lps >= 1), all resident in
+ * device memory after creation. The batch is solved as one block-diagonal problem
+ * with per-LP step lengths, merit and convergence.
+ * Replaces: MehrotraSolver::Impl::Impl (src/ipm/mehrotra_device.cu:276-465) for
+ *           each LP; the reference has no batch entry point. */
+typedef struct sk_solver sk_solver;
+int sk_solver_create(int num_lps, const int* m, const int* n, const int* const* col_ptrs,
+                     const int* const* row_idx, const double* const* vals, const double* const* b,
+                     const double* const* c, const sk_options* opt, sk_solver** out);
+/* Optional starting point for LP `lp` (unscaled x, y, s); used when opt.start == SK_START_USER. */
+int sk_solver_set_start(sk_solver* h, int lp, const double* x, const double* y, const double* s);
+/* Runs the IPM from the start point on the resident data (Impl::solve, :695-1047). */
+int sk_solver_run(sk_solver* h);
+int sk_solver_result(sk_solver* h, int lp, double* x, double* y, double* s, sk_info* info);
+void sk_solver_destroy(sk_solver* h);
+
+/* ---- KKT normal-equation engine (device pointers) ----
+ * Replaces: gpu::GPUKKTCholeskySolver (src/cuda/kkt.cuh:28-71). A is CSR (m x n).
+ * P: elimination order (P[k] = original row), NULL = choose per opt.ordering. */
+typedef struct sk_kkt sk_kkt;
+int sk_kkt_create(int m, int n, const int* row_ptrs, const int* col_idx, const double* vals,
+                  const int* P, int precision, sk_kkt** out);                /* kkt.cuh:38-43 */
+int sk_kkt_factorize_device(sk_kkt* k, const double* d_theta);              /* kkt.cuh:67 */
+/* Solves M0 dy = rhs in place (M0 = A diag(theta) A^T); returns SK_OK when
+ * ||rhs - M0 dy||_inf <= tol * max(1, ||rhs||_inf), SK_ERR_NUMERICAL otherwise. */
+int sk_kkt_solve_device(sk_kkt* k, double* d_rhs, double tol);              /* kkt.cuh:68 */
+int sk_kkt_factorize(sk_kkt* k, const double* theta);                       /* kkt.cuh:53 */
+int sk_kkt_solve(sk_kkt* k, double* rhs, double tol);                        /* kkt.cuh:61 */
+/* Copies the factor of D (P M0 P^T) D + delta I as a dense lower-triangular m x m
+ * row-major matrix in the elimination order, plus D (m), for inspection. */
+int sk_kkt_get_factor(sk_kkt* k, double* L_dense, double* D);
+void sk_kkt_destroy(sk_kkt* k);
+
+/* ---- Symbolic analysis (host) ----
+ * Replaces: ipm::compute_amd_ordering (src/ipm/symbolic.hpp:50) -- exact minimum
+ * degree with lowest-index tie-break, bit-exact with the reference. */
+int sk_compute_amd_ordering(int m, int n, const int* row_ptrs, const int* col_idx, int* P);
+/* Replaces: ipm::compute_symbolic_factorization (src/ipm/symbolic.hpp:59-63):
+ * P_inv, elimination tree parent (-1 = root) and strictly lower L pattern in CSR
+ * (L_row_ptrs: m+1, L_cols: capacity cap). Returns nnz(L) >= 0, -1 if cap is too small. */
+int sk_compute_symbolic(int m, int n, const int* row_ptrs, const int* col_idx, const int* P,
+                        int* P_inv, int* parent, int* L_row_ptrs, int* L_cols, int cap);
+/* Fill-reducing approximate minimum degree order of A A^T used by the solver (no
+ * reference counterpart beyond compute_amd_ordering's role). */
+int sk_fill_ordering(int m, int n, const int* row_ptrs, const int* col_idx, int* P);
+
+/* ---- Device kernels exposed for parity tests (device pointers, stream may be NULL) ---- */
+/* y = alpha * A x + beta * y for CSR A (rows x ?). Replaces cusparseSpMV CSR FP64
+ * (src/ipm/mehrotra_device.cu:512,603,635,936). */
+int sk_spmv_csr(int rows, const int* d_row_ptrs, const int* d_col_idx, const double* d_vals,
+                const double* d_x, double alpha, double beta, double* d_y, void* stream);
+
+/* ---- Model input ----
+ * Replaces: parsers::read_mps (src/parsers/mps_reader.hpp:20) and the seeded
+ * generators (no reference counterpart). An sk_lp owns CSC arrays + b + c. */
+typedef struct sk_lp sk_lp;
+int sk_lp_read_mps(const char* path, sk_lp** out);
+int sk_lp_generate(int family, int instance, sk_lp** out);
+int sk_lp_random(int m, int n, double density, unsigned long long seed, sk_lp** out);
+int sk_lp_dims(const sk_lp* lp, int* m, int* n, int* nnz);
+/* Pointers into the LP's own storage (valid until sk_lp_free). lb / ub may be NULL. */
+int sk_lp_arrays(const sk_lp* lp, const int** col_ptrs, const int** row_idx, const double** vals,
+                 const double** b, const double** c);
+int sk_lp_bounds(const sk_lp* lp, const double** lb, const double** ub);
+void sk_lp_free(sk_lp* lp);
+
+/* Last error message of the calling thread ("" if none). */
+const char* sk_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

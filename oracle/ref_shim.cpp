@@ -1,0 +1,104 @@
+// C entry points over the reference's own CPU code, compiled from the reference
+// sources where they lie (see Makefile target `ref`). TEST INFRASTRUCTURE ONLY:
+// the reference is used here as a checker (symbolic analysis, simplex objective,
+// certificate) and as the timed CPU baseline; nothing in the product links it.
+#include <cstring>
+#include <vector>
+
+#include "core/problem.hpp"
+#include "core/sparse_matrix.hpp"
+#include "ipm/symbolic.hpp"
+#include "numerics/sparse_lu.hpp"
+#include "simplex/phase1.hpp"
+#include "verifier/certificate.hpp"
+
+using namespace sankhya;
+
+static core::CSRMatrix csr_of(int m, int n, const int* rp, const int* ci) {
+    core::CSRMatrix A;
+    A.rows = m;
+    A.cols = n;
+    A.row_ptrs.assign(rp, rp + m + 1);
+    A.col_indices.assign(ci, ci + rp[m]);
+    A.values.assign(static_cast<size_t>(rp[m]), 1.0);
+    return A;
+}
+
+static core::Model model_of(int m, int n, const int* cp, const int* ri, const double* va,
+                            const double* b, const double* c) {
+    core::Model model;
+    for (int j = 0; j < n; ++j) model.add_variable(c[j]);
+    std::vector<std::vector<Index>> rc(static_cast<size_t>(m));
+    std::vector<std::vector<Float>> rv(static_cast<size_t>(m));
+    for (int j = 0; j < n; ++j)
+        for (int k = cp[j]; k < cp[j + 1]; ++k) {
+            rc[static_cast<size_t>(ri[k])].push_back(j);
+            rv[static_cast<size_t>(ri[k])].push_back(va[k]);
+        }
+    for (int i = 0; i < m; ++i) model.add_constraint(rc[static_cast<size_t>(i)], rv[static_cast<size_t>(i)], b[i]);
+    model.finalize();
+    return model;
+}
+
+extern "C" {
+
+int ref_min_degree(int m, int n, const int* rp, const int* ci, int* P) {
+    try {
+        auto p = ipm::compute_amd_ordering(csr_of(m, n, rp, ci));
+        std::memcpy(P, p.data(), sizeof(int) * static_cast<size_t>(m));
+        return 0;
+    } catch (...) {
+        return -1;
+    }
+}
+
+int ref_symbolic(int m, int n, const int* rp, const int* ci, const int* P, int* P_inv, int* parent,
+                 int* L_rp, int* L_ci, int cap) {
+    try {
+        ipm::SymbolicFactorization sym;
+        std::vector<Index> pv(P, P + m);
+        ipm::compute_symbolic_factorization(csr_of(m, n, rp, ci), pv, sym);
+        const int nnz = sym.L_pattern.row_ptrs[static_cast<size_t>(m)];
+        if (nnz > cap) return -1;
+        std::memcpy(P_inv, sym.P_inv.data(), sizeof(int) * static_cast<size_t>(m));
+        std::memcpy(parent, sym.parent.data(), sizeof(int) * static_cast<size_t>(m));
+        std::memcpy(L_rp, sym.L_pattern.row_ptrs.data(), sizeof(int) * static_cast<size_t>(m + 1));
+        std::memcpy(L_ci, sym.L_pattern.col_indices.data(), sizeof(int) * static_cast<size_t>(nnz));
+        return nnz;
+    } catch (...) {
+        return -2;
+    }
+}
+
+// Phase-I + primal simplex with the reference's sparse LU; returns the
+// SimplexStatus as int (0 Optimal), objective and x.
+int ref_simplex_solve(int m, int n, const int* cp, const int* ri, const double* va, const double* b,
+                      const double* c, double* x_out, double* obj) {
+    try {
+        core::Model model = model_of(m, n, cp, ri, va, b, c);
+        simplex::Basis basis;
+        std::vector<Float> x;
+        numerics::SparseLUFactorization lu;
+        auto st = simplex::solve_with_phase1(model, basis, x, lu);
+        double o = 0.0;
+        for (size_t j = 0; j < x.size(); ++j) o += x[j] * model.obj[j];
+        if (obj) *obj = o;
+        if (x_out && x.size() == static_cast<size_t>(n)) std::memcpy(x_out, x.data(), sizeof(double) * static_cast<size_t>(n));
+        return static_cast<int>(st);
+    } catch (...) {
+        return -1;
+    }
+}
+
+int ref_verify_optimal(int m, int n, const int* cp, const int* ri, const double* va, const double* b,
+                       const double* c, const double* x, const double* pi) {
+    try {
+        core::Model model = model_of(m, n, cp, ri, va, b, c);
+        std::vector<Float> xv(x, x + n), pv(pi, pi + m);
+        return verifier::verify_optimal(model, xv, pv) ? 1 : 0;
+    } catch (...) {
+        return -1;
+    }
+}
+
+}  // extern "C"

@@ -1,0 +1,215 @@
+// Host-side C ABI entry points: model input (generators, MPS), symbolic
+// analysis, options and error reporting. See include/sankhya/sk_ipm.h.
+#include <cstring>
+#include <exception>
+#include <new>
+#include <string>
+
+#include "api/sk_error.hpp"
+#include "core/problem.hpp"
+#include "gen/lpgen.hpp"
+#include "ipm/symbolic.hpp"
+#include "parsers/mps_reader.hpp"
+#include "sankhya/sk_ipm.h"
+
+struct sk_lp {
+    sankhya::core::Model model;
+};
+
+namespace sankhya {
+namespace api {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+void clear_error() { g_last_error.clear(); }
+
+int status_of_current_exception() {
+    try {
+        throw;
+    } catch (const sk_exception& e) {
+        set_error(e.what());
+        return e.code;
+    } catch (const std::bad_alloc& e) {
+        set_error(std::string("allocation failed: ") + e.what());
+        return SK_ERR_ALLOC;
+    } catch (const std::invalid_argument& e) {
+        set_error(e.what());
+        return SK_ERR_INVALID;
+    } catch (const std::out_of_range& e) {
+        set_error(e.what());
+        return SK_ERR_INVALID;
+    } catch (const std::exception& e) {
+        set_error(e.what());
+        return SK_ERR_INTERNAL;
+    } catch (...) {
+        set_error("unknown exception");
+        return SK_ERR_INTERNAL;
+    }
+}
+
+core::CSRMatrix pattern_csr(int m, int n, const int* row_ptrs, const int* col_idx) {
+    if (m < 0 || n < 0 || !row_ptrs || (row_ptrs[m] > 0 && !col_idx))
+        throw std::invalid_argument("invalid CSR pattern");
+    core::CSRMatrix A;
+    A.rows = m;
+    A.cols = n;
+    A.row_ptrs.assign(row_ptrs, row_ptrs + m + 1);
+    A.col_indices.assign(col_idx, col_idx + row_ptrs[m]);
+    for (Index i = 0; i < m; ++i)
+        if (A.row_ptrs[i + 1] < A.row_ptrs[i]) throw std::invalid_argument("CSR row_ptrs not monotone");
+    for (Index c : A.col_indices)
+        if (c < 0 || c >= n) throw std::invalid_argument("CSR column index out of range");
+    A.values.assign(A.col_indices.size(), 1.0);
+    return A;
+}
+
+}  // namespace api
+}  // namespace sankhya
+
+using namespace sankhya;
+
+extern "C" {
+
+const char* sk_last_error(void) { return api::g_last_error.c_str(); }
+
+void sk_options_default(sk_options* opt) {
+    if (!opt) return;
+    opt->precision = SK_PREC_MIXED;
+    opt->start = SK_START_UNIT;
+    opt->criteria = SK_CRIT_RELATIVE;
+    opt->tol = 1e-8;
+    opt->max_iter = 200;
+    opt->ordering = SK_ORDER_AUTO;
+    opt->verbose = 0;
+    opt->mu_switch = 1e-6;
+    opt->ruiz_passes = 10;
+}
+
+int sk_lp_generate(int family, int instance, sk_lp** out) {
+    api::clear_error();
+    if (!out) return SK_ERR_INVALID;
+    try {
+        auto g = gen::family_lp(family, instance);
+        auto* lp = new sk_lp;
+        lp->model = core::Model::from_csc(g.m, g.n, g.col_ptrs.data(), g.row_idx.data(), g.vals.data(),
+                                          g.b.data(), g.c.data());
+        *out = lp;
+        return SK_OK;
+    } catch (...) {
+        return api::status_of_current_exception();
+    }
+}
+
+int sk_lp_random(int m, int n, double density, unsigned long long seed, sk_lp** out) {
+    api::clear_error();
+    if (!out) return SK_ERR_INVALID;
+    try {
+        auto g = gen::random_sparse_lp(m, n, density, seed);
+        auto* lp = new sk_lp;
+        lp->model = core::Model::from_csc(g.m, g.n, g.col_ptrs.data(), g.row_idx.data(), g.vals.data(),
+                                          g.b.data(), g.c.data());
+        *out = lp;
+        return SK_OK;
+    } catch (...) {
+        return api::status_of_current_exception();
+    }
+}
+
+int sk_lp_read_mps(const char* path, sk_lp** out) {
+    api::clear_error();
+    if (!path || !out) return SK_ERR_INVALID;
+    try {
+        auto* lp = new sk_lp;
+        try {
+            lp->model = parsers::read_mps(path);
+        } catch (const std::runtime_error& e) {
+            delete lp;
+            api::set_error(e.what());
+            return SK_ERR_INVALID;
+        }
+        *out = lp;
+        return SK_OK;
+    } catch (...) {
+        return api::status_of_current_exception();
+    }
+}
+
+int sk_lp_dims(const sk_lp* lp, int* m, int* n, int* nnz) {
+    if (!lp) return SK_ERR_INVALID;
+    if (m) *m = lp->model.A.rows;
+    if (n) *n = lp->model.A.cols;
+    if (nnz) *nnz = lp->model.A.nnz();
+    return SK_OK;
+}
+
+int sk_lp_arrays(const sk_lp* lp, const int** col_ptrs, const int** row_idx, const double** vals,
+                 const double** b, const double** c) {
+    if (!lp) return SK_ERR_INVALID;
+    if (col_ptrs) *col_ptrs = lp->model.A.col_ptrs.data();
+    if (row_idx) *row_idx = lp->model.A.row_indices.data();
+    if (vals) *vals = lp->model.A.values.data();
+    if (b) *b = lp->model.rhs.data();
+    if (c) *c = lp->model.obj.data();
+    return SK_OK;
+}
+
+int sk_lp_bounds(const sk_lp* lp, const double** lb, const double** ub) {
+    if (!lp) return SK_ERR_INVALID;
+    if (lb) *lb = lp->model.lb.data();
+    if (ub) *ub = lp->model.ub.data();
+    return SK_OK;
+}
+
+void sk_lp_free(sk_lp* lp) { delete lp; }
+
+int sk_compute_amd_ordering(int m, int n, const int* row_ptrs, const int* col_idx, int* P) {
+    api::clear_error();
+    if (!P) return SK_ERR_INVALID;
+    try {
+        auto p = ipm::compute_amd_ordering(api::pattern_csr(m, n, row_ptrs, col_idx));
+        std::memcpy(P, p.data(), sizeof(int) * static_cast<size_t>(m));
+        return SK_OK;
+    } catch (...) {
+        return api::status_of_current_exception();
+    }
+}
+
+int sk_fill_ordering(int m, int n, const int* row_ptrs, const int* col_idx, int* P) {
+    api::clear_error();
+    if (!P) return SK_ERR_INVALID;
+    try {
+        auto p = ipm::fill_reducing_ordering(api::pattern_csr(m, n, row_ptrs, col_idx));
+        std::memcpy(P, p.data(), sizeof(int) * static_cast<size_t>(m));
+        return SK_OK;
+    } catch (...) {
+        return api::status_of_current_exception();
+    }
+}
+
+int sk_compute_symbolic(int m, int n, const int* row_ptrs, const int* col_idx, const int* P, int* P_inv,
+                        int* parent, int* L_row_ptrs, int* L_cols, int cap) {
+    api::clear_error();
+    if (!P || !P_inv || !parent || !L_row_ptrs || (cap > 0 && !L_cols)) return -SK_ERR_INVALID;
+    try {
+        std::vector<Index> pv(P, P + m);
+        std::vector<char> seen(static_cast<size_t>(m), 0);
+        for (Index v : pv) {
+            if (v < 0 || v >= m || seen[v]) throw std::invalid_argument("P is not a permutation");
+            seen[v] = 1;
+        }
+        ipm::SymbolicFactorization sym;
+        ipm::compute_symbolic_factorization(api::pattern_csr(m, n, row_ptrs, col_idx), pv, sym);
+        const int nnz = sym.L_pattern.row_ptrs[static_cast<size_t>(m)];
+        if (nnz > cap) return -1;
+        std::memcpy(P_inv, sym.P_inv.data(), sizeof(int) * static_cast<size_t>(m));
+        std::memcpy(parent, sym.parent.data(), sizeof(int) * static_cast<size_t>(m));
+        std::memcpy(L_row_ptrs, sym.L_pattern.row_ptrs.data(), sizeof(int) * static_cast<size_t>(m + 1));
+        if (nnz > 0) std::memcpy(L_cols, sym.L_pattern.col_indices.data(), sizeof(int) * static_cast<size_t>(nnz));
+        return nnz;
+    } catch (...) {
+        return -api::status_of_current_exception();
+    }
+}
+
+}  // extern "C"

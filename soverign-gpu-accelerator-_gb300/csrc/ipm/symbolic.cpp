@@ -1,0 +1,271 @@
+// Symbolic analysis: exact minimum degree (reference ordering), elimination
+// tree, L pattern, and the approximate minimum degree ordering of the solver.
+#include "ipm/symbolic.hpp"
+
+#include <algorithm>
+#include <numeric>
+#include <stdexcept>
+
+namespace sankhya {
+namespace ipm {
+
+namespace {
+
+// Rows of each column of CSR A (transpose of the pattern).
+void column_rows(const core::CSRMatrix& A, std::vector<Index>& cptr, std::vector<Index>& crow) {
+    cptr.assign(static_cast<size_t>(A.cols) + 1, 0);
+    const Index nz = A.row_ptrs[static_cast<size_t>(A.rows)];
+    for (Index k = 0; k < nz; ++k) cptr[static_cast<size_t>(A.col_indices[k]) + 1]++;
+    for (Index j = 0; j < A.cols; ++j) cptr[j + 1] += cptr[j];
+    crow.resize(static_cast<size_t>(nz));
+    std::vector<Index> next(cptr.begin(), cptr.end() - 1);
+    for (Index i = 0; i < A.rows; ++i)
+        for (Index k = A.row_ptrs[i]; k < A.row_ptrs[i + 1]; ++k) crow[next[A.col_indices[k]]++] = i;
+}
+
+// Sorted, duplicate-free adjacency of A A^T without self loops.
+std::vector<std::vector<Index>> aat_graph(const core::CSRMatrix& A) {
+    std::vector<Index> cptr, crow;
+    column_rows(A, cptr, crow);
+    std::vector<std::vector<Index>> adj(static_cast<size_t>(A.rows));
+    std::vector<Index> mark(static_cast<size_t>(A.rows), -1);
+    for (Index i = 0; i < A.rows; ++i) {
+        auto& ai = adj[static_cast<size_t>(i)];
+        mark[i] = i;
+        for (Index k = A.row_ptrs[i]; k < A.row_ptrs[i + 1]; ++k) {
+            const Index j = A.col_indices[k];
+            for (Index q = cptr[j]; q < cptr[j + 1]; ++q) {
+                const Index r = crow[q];
+                if (mark[r] != i) { mark[r] = i; ai.push_back(r); }
+            }
+        }
+        std::sort(ai.begin(), ai.end());
+    }
+    return adj;
+}
+
+}  // namespace
+
+std::vector<Index> compute_amd_ordering(const core::CSRMatrix& A) {
+    const Index m = A.rows;
+    auto adj = aat_graph(A);
+    std::vector<char> done(static_cast<size_t>(m), 0);
+    std::vector<Index> P;
+    P.reserve(static_cast<size_t>(m));
+    std::vector<Index> merged;
+    for (Index step = 0; step < m; ++step) {
+        Index u = -1;
+        size_t best = static_cast<size_t>(m) + 1;
+        for (Index i = 0; i < m; ++i)  // lowest index wins ties
+            if (!done[i] && adj[i].size() < best) { best = adj[i].size(); u = i; }
+        if (u < 0) throw std::runtime_error("compute_amd_ordering: Disconnected graph or invalid state");
+        done[u] = 1;
+        P.push_back(u);
+        const std::vector<Index> nb = adj[u];
+        for (Index v : nb) {
+            // adj[v] <- (adj[v] \ {u}) U (nb \ {v})
+            auto& av = adj[v];
+            merged.clear();
+            merged.reserve(av.size() + nb.size());
+            std::set_union(av.begin(), av.end(), nb.begin(), nb.end(), std::back_inserter(merged));
+            merged.erase(std::remove_if(merged.begin(), merged.end(), [&](Index w) { return w == u || w == v; }),
+                         merged.end());
+            av.swap(merged);
+        }
+    }
+    return P;
+}
+
+void permuted_lower_pattern(const core::CSRMatrix& A, const std::vector<Index>& P_inv,
+                            std::vector<Index>& rowptr, std::vector<Index>& colidx) {
+    const Index m = A.rows;
+    std::vector<Index> cptr, crow;
+    column_rows(A, cptr, crow);
+    std::vector<Index> P(static_cast<size_t>(m));
+    for (Index i = 0; i < m; ++i) P[P_inv[i]] = i;
+    rowptr.assign(static_cast<size_t>(m) + 1, 0);
+    colidx.clear();
+    std::vector<Index> mark(static_cast<size_t>(m), -1);
+    std::vector<Index> row;
+    for (Index k = 0; k < m; ++k) {
+        const Index i = P[k];
+        mark[i] = k;
+        row.clear();
+        for (Index q = A.row_ptrs[i]; q < A.row_ptrs[i + 1]; ++q) {
+            const Index j = A.col_indices[q];
+            for (Index t = cptr[j]; t < cptr[j + 1]; ++t) {
+                const Index r = crow[t];
+                if (mark[r] != k) {
+                    mark[r] = k;
+                    const Index pr = P_inv[r];
+                    if (pr < k) row.push_back(pr);
+                }
+            }
+        }
+        std::sort(row.begin(), row.end());
+        colidx.insert(colidx.end(), row.begin(), row.end());
+        rowptr[k + 1] = static_cast<Index>(colidx.size());
+    }
+}
+
+std::vector<Index> elimination_tree(Index m, const std::vector<Index>& rowptr,
+                                    const std::vector<Index>& colidx) {
+    std::vector<Index> parent(static_cast<size_t>(m), -1), anc(static_cast<size_t>(m), -1);
+    for (Index i = 0; i < m; ++i) {
+        for (Index q = rowptr[i]; q < rowptr[i + 1]; ++q) {
+            Index j = colidx[q];
+            while (j != -1 && j < i) {  // climb with path compression towards i
+                const Index next = anc[j];
+                anc[j] = i;
+                if (next == -1) { parent[j] = i; break; }
+                j = next;
+            }
+        }
+    }
+    return parent;
+}
+
+void compute_symbolic_factorization(const core::CSRMatrix& A, const std::vector<Index>& P,
+                                    SymbolicFactorization& out) {
+    const Index m = A.rows;
+    if (static_cast<Index>(P.size()) != m) throw std::invalid_argument("compute_symbolic_factorization: |P| != m");
+    out.P = P;
+    out.P_inv.assign(static_cast<size_t>(m), 0);
+    for (Index k = 0; k < m; ++k) out.P_inv[P[k]] = k;
+    std::vector<Index> rp, ci;
+    permuted_lower_pattern(A, out.P_inv, rp, ci);
+    out.parent = elimination_tree(m, rp, ci);
+    // Row i of L = union of etree paths from each j in row i of M up to i
+    // (row-subtree traversal), listed in increasing column order.
+    out.L_pattern.rows = m;
+    out.L_pattern.cols = m;
+    out.L_pattern.row_ptrs.assign(static_cast<size_t>(m) + 1, 0);
+    out.L_pattern.col_indices.clear();
+    std::vector<Index> mark(static_cast<size_t>(m), -1), row;
+    for (Index i = 0; i < m; ++i) {
+        mark[i] = i;
+        row.clear();
+        for (Index q = rp[i]; q < rp[i + 1]; ++q) {
+            for (Index j = ci[q]; j != -1 && mark[j] != i; j = out.parent[j]) {
+                mark[j] = i;
+                row.push_back(j);
+            }
+        }
+        std::sort(row.begin(), row.end());
+        out.L_pattern.col_indices.insert(out.L_pattern.col_indices.end(), row.begin(), row.end());
+        out.L_pattern.row_ptrs[i + 1] = static_cast<Index>(out.L_pattern.col_indices.size());
+    }
+    out.L_pattern.values.assign(out.L_pattern.col_indices.size(), 1.0);
+}
+
+// ---------------------------------------------------------------------------
+// Approximate minimum degree on the quotient graph (Amestoy, Davis & Duff 1996):
+// eliminated pivots become elements (cliques); each variable keeps its adjacent
+// elements E_i and remaining variable neighbours A_i; the external degree of a
+// variable touched by pivot p is bounded by
+//   min(n_live - 1, d_old + |L_p \ i|, |A_i \ i| + |L_p \ i| + sum_{e in E_i, e != p} |L_e \ L_p|).
+// Elements whose members all lie in L_p are absorbed (aggressive absorption).
+// Ties go to the most recently inserted variable of the minimum-degree bucket.
+std::vector<Index> fill_reducing_ordering(const core::CSRMatrix& A) {
+    const Index m = A.rows;
+    std::vector<Index> order;
+    order.reserve(static_cast<size_t>(m));
+    if (m == 0) return order;
+    auto Av = aat_graph(A);                        // variable neighbours
+    std::vector<std::vector<Index>> Ev(static_cast<size_t>(m));   // adjacent elements
+    std::vector<std::vector<Index>> Le(static_cast<size_t>(m));   // element members (live variables)
+    std::vector<char> eliminated(static_cast<size_t>(m), 0), dead_elem(static_cast<size_t>(m), 0);
+    std::vector<Index> deg(static_cast<size_t>(m));
+    for (Index i = 0; i < m; ++i) deg[i] = static_cast<Index>(Av[i].size());
+    // Degree buckets as ordered sets of (degree, index) via a simple bucket array
+    // of doubly linked lists; the minimum-degree search scans upward from the last
+    // known minimum.
+    std::vector<Index> head(static_cast<size_t>(m) + 1, -1), nxt(static_cast<size_t>(m), -1),
+        prv(static_cast<size_t>(m), -1);
+    auto insert = [&](Index i) {
+        const Index d = deg[i];
+        nxt[i] = head[d];
+        prv[i] = -1;
+        if (head[d] != -1) prv[head[d]] = i;
+        head[d] = i;
+    };
+    auto remove = [&](Index i) {
+        const Index d = deg[i];
+        if (prv[i] != -1) nxt[prv[i]] = nxt[i]; else head[d] = nxt[i];
+        if (nxt[i] != -1) prv[nxt[i]] = prv[i];
+    };
+    for (Index i = m - 1; i >= 0; --i) insert(i);
+    std::vector<Index> w(static_cast<size_t>(m), -1);   // |L_e \ L_p| scratch, -1 = unset
+    std::vector<Index> inLp(static_cast<size_t>(m), -1);
+    std::vector<Index> touched;
+    Index mindeg = 0;
+    Index live = m;
+    for (Index k = 0; k < m; ++k) {
+        while (mindeg <= m && head[mindeg] == -1) ++mindeg;
+        const Index p = head[mindeg];   // most recently inserted of the minimum bucket
+        remove(p);
+        eliminated[p] = 1;
+        order.push_back(p);
+        --live;
+        // L_p = A_p U (U_{e in E_p} L_e) \ {p}
+        auto& Lp = Le[p];
+        Lp.clear();
+        inLp[p] = p;
+        for (Index v : Av[p]) if (!eliminated[v] && inLp[v] != p) { inLp[v] = p; Lp.push_back(v); }
+        for (Index e : Ev[p]) {
+            if (dead_elem[e]) continue;
+            for (Index v : Le[e]) if (!eliminated[v] && inLp[v] != p) { inLp[v] = p; Lp.push_back(v); }
+            dead_elem[e] = 1;               // absorbed into p
+            Le[e].clear();
+            Le[e].shrink_to_fit();
+        }
+        Av[p].clear(); Av[p].shrink_to_fit();
+        Ev[p].clear(); Ev[p].shrink_to_fit();
+        const Index lp_size = static_cast<Index>(Lp.size());
+        // Update E_i, prune A_i, compute |L_e \ L_p|.
+        touched.clear();
+        for (Index i : Lp) {
+            auto& Ei = Ev[i];
+            size_t o = 0;
+            for (Index e : Ei) if (!dead_elem[e] && e != p) Ei[o++] = e;
+            Ei.resize(o);
+            for (Index e : Ei) {
+                if (w[e] < 0) { w[e] = static_cast<Index>(Le[e].size()); touched.push_back(e); }
+                w[e] -= 1;
+            }
+            Ei.push_back(p);
+            auto& Ai = Av[i];
+            size_t t = 0;
+            for (Index v : Ai) if (!eliminated[v] && inLp[v] != p) Ai[t++] = v;
+            Ai.resize(t);
+        }
+        // Aggressive absorption of elements entirely inside L_p.
+        for (Index e : touched)
+            if (w[e] == 0) { dead_elem[e] = 1; Le[e].clear(); }
+        for (Index i : Lp) {
+            Index ext = 0;
+            Index d = static_cast<Index>(Av[i].size()) + (lp_size - 1);
+            auto& Ei = Ev[i];
+            size_t o = 0;
+            for (Index e : Ei) {
+                if (dead_elem[e]) continue;
+                Ei[o++] = e;
+                if (e != p) ext += w[e];
+            }
+            Ei.resize(o);
+            d += ext;
+            const Index bound = std::min<Index>(live - 1, deg[i] + lp_size - 1);
+            if (d > bound) d = bound;
+            if (d < 0) d = 0;
+            remove(i);
+            deg[i] = d;
+            insert(i);
+            if (d < mindeg) mindeg = d;
+        }
+        for (Index e : touched) w[e] = -1;
+    }
+    return order;
+}
+
+}  // namespace ipm
+}  // namespace sankhya

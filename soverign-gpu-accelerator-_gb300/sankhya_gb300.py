@@ -1,0 +1,199 @@
+"""ctypes binding of libsankhya_gb300.so (the C ABI in include/sankhya/sk_ipm.h).
+
+The engine itself is C++ / CUDA; this module only marshals numpy arrays across
+the C ABI. There is no Python fallback: if the library is missing, loading fails.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libsankhya_gb300.so")
+
+SK_OK = 0
+SK_ERR_NUMERICAL = 3
+SK_ERR_TOO_LARGE = 7
+STATUS = {0: "Optimal", 1: "Infeasible", 2: "Unbounded", 3: "IterationLimit"}
+PREC_FP64, PREC_MIXED = 0, 1
+START_UNIT, START_MEHROTRA, START_USER = 0, 1, 2
+CRIT_RELATIVE, CRIT_REFERENCE = 0, 1
+ORDER_AUTO, ORDER_REFERENCE, ORDER_NATURAL = 0, 1, 2
+
+_i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+
+
+class Options(C.Structure):
+    _fields_ = [("precision", C.c_int), ("start", C.c_int), ("criteria", C.c_int), ("tol", C.c_double),
+                ("max_iter", C.c_int), ("ordering", C.c_int), ("verbose", C.c_int),
+                ("mu_switch", C.c_double), ("ruiz_passes", C.c_int)]
+
+
+class Info(C.Structure):
+    _fields_ = [("status", C.c_int), ("iterations", C.c_int), ("objective", C.c_double),
+                ("primal_residual", C.c_double), ("dual_residual", C.c_double), ("duality_gap", C.c_double),
+                ("rel_pinf", C.c_double), ("rel_dinf", C.c_double), ("rel_gap", C.c_double),
+                ("precision_path", C.c_int), ("switch_iteration", C.c_int), ("factorizations", C.c_int),
+                ("solves", C.c_int), ("refine_steps", C.c_int), ("learned_start", C.c_int),
+                ("setup_ms", C.c_double), ("solve_ms", C.c_double), ("nnz_factor", C.c_longlong),
+                ("num_supernodes", C.c_int), ("dense_front", C.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_lib = None
+
+
+def lib():
+    """Loads the engine library (raises OSError if it has not been built)."""
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(LIB_PATH)
+        _declare(_lib)
+    return _lib
+
+
+def _declare(L):
+    vp = C.c_void_p
+    L.sk_last_error.restype = C.c_char_p
+    L.sk_options_default.argtypes = [C.POINTER(Options)]
+    L.sk_lp_generate.argtypes = [C.c_int, C.c_int, C.POINTER(vp)]
+    L.sk_lp_random.argtypes = [C.c_int, C.c_int, C.c_double, C.c_ulonglong, C.POINTER(vp)]
+    L.sk_lp_read_mps.argtypes = [C.c_char_p, C.POINTER(vp)]
+    L.sk_lp_dims.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    L.sk_lp_arrays.argtypes = [vp] + [C.POINTER(vp)] * 5
+    L.sk_lp_bounds.argtypes = [vp, C.POINTER(vp), C.POINTER(vp)]
+    L.sk_lp_free.argtypes = [vp]
+    L.sk_compute_amd_ordering.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _i32p]
+    L.sk_fill_ordering.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _i32p]
+    L.sk_compute_symbolic.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _i32p, _i32p, _i32p, _i32p, _i32p, C.c_int]
+    if hasattr(L, "sk_ipm_solve_csc"):
+        L.sk_ipm_solve_csc.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p, _f64p, _f64p, C.POINTER(Options),
+                                       vp, vp, vp, C.POINTER(Info)]
+        L.sk_solver_create.argtypes = [C.c_int, vp, vp, vp, vp, vp, vp, vp, C.POINTER(Options), C.POINTER(vp)]
+        L.sk_solver_set_start.argtypes = [vp, C.c_int, vp, vp, vp]
+        L.sk_solver_run.argtypes = [vp]
+        L.sk_solver_result.argtypes = [vp, C.c_int, vp, vp, vp, C.POINTER(Info)]
+        L.sk_solver_destroy.argtypes = [vp]
+        L.sk_kkt_create.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p, vp, C.c_int, C.POINTER(vp)]
+        L.sk_kkt_factorize_device.argtypes = [vp, vp]
+        L.sk_kkt_solve_device.argtypes = [vp, vp, C.c_double]
+        L.sk_kkt_factorize.argtypes = [vp, _f64p]
+        L.sk_kkt_solve.argtypes = [vp, _f64p, C.c_double]
+        L.sk_kkt_get_factor.argtypes = [vp, _f64p, _f64p]
+        L.sk_kkt_destroy.argtypes = [vp]
+        L.sk_spmv_csr.argtypes = [C.c_int, vp, vp, vp, vp, C.c_double, C.c_double, vp, vp]
+
+
+def last_error():
+    return lib().sk_last_error().decode()
+
+
+def check(rc, what):
+    if rc != SK_OK:
+        raise RuntimeError("%s failed (code %d): %s" % (what, rc, last_error()))
+
+
+def options(**kw):
+    o = Options()
+    lib().sk_options_default(C.byref(o))
+    for k, v in kw.items():
+        if not hasattr(o, k):
+            raise KeyError(k)
+        setattr(o, k, v)
+    return o
+
+
+class LP:
+    """An LP in standard form min c^T x, Ax = b, x >= 0 with A in CSC (numpy arrays)."""
+
+    def __init__(self, m, n, col_ptrs, row_idx, vals, b, c, name="lp"):
+        self.m, self.n = int(m), int(n)
+        self.col_ptrs = np.ascontiguousarray(col_ptrs, dtype=np.int32)
+        self.row_idx = np.ascontiguousarray(row_idx, dtype=np.int32)
+        self.vals = np.ascontiguousarray(vals, dtype=np.float64)
+        self.b = np.ascontiguousarray(b, dtype=np.float64)
+        self.c = np.ascontiguousarray(c, dtype=np.float64)
+        self.name = name
+
+    @property
+    def nnz(self):
+        return int(self.col_ptrs[-1])
+
+    def csr(self):
+        """(row_ptrs, col_idx, vals) of A in CSR with increasing columns per row."""
+        m = self.m
+        counts = np.bincount(self.row_idx, minlength=m)
+        rp = np.zeros(m + 1, dtype=np.int32)
+        np.cumsum(counts, out=rp[1:])
+        cols = np.repeat(np.arange(self.n, dtype=np.int32), np.diff(self.col_ptrs))
+        order = np.lexsort((cols, self.row_idx))
+        return rp, np.ascontiguousarray(cols[order]), np.ascontiguousarray(self.vals[order])
+
+    def nbytes(self):
+        return self.col_ptrs.nbytes + self.row_idx.nbytes + self.vals.nbytes + self.b.nbytes + self.c.nbytes
+
+
+def _lp_from_handle(h, name):
+    L = lib()
+    m, n, nz = C.c_int(), C.c_int(), C.c_int()
+    L.sk_lp_dims(h, C.byref(m), C.byref(n), C.byref(nz))
+    ptrs = [C.c_void_p() for _ in range(5)]
+    L.sk_lp_arrays(h, *[C.byref(p) for p in ptrs])
+
+    def arr(p, count, ctype, dtype):
+        if count == 0:
+            return np.zeros(0, dtype=dtype)
+        return np.ctypeslib.as_array(C.cast(p, C.POINTER(ctype)), shape=(count,)).astype(dtype, copy=True)
+
+    lp = LP(m.value, n.value, arr(ptrs[0], n.value + 1, C.c_int, np.int32),
+            arr(ptrs[1], nz.value, C.c_int, np.int32), arr(ptrs[2], nz.value, C.c_double, np.float64),
+            arr(ptrs[3], m.value, C.c_double, np.float64), arr(ptrs[4], n.value, C.c_double, np.float64), name)
+    L.sk_lp_free(h)
+    return lp
+
+
+def generate(family, instance=0):
+    """Seeded LP of family 0..3 (see csrc/gen/lpgen.hpp)."""
+    h = C.c_void_p()
+    check(lib().sk_lp_generate(family, instance, C.byref(h)), "sk_lp_generate")
+    return _lp_from_handle(h, "family%d/%d" % (family, instance))
+
+
+def random_lp(m, n, density, seed):
+    h = C.c_void_p()
+    check(lib().sk_lp_random(m, n, density, seed, C.byref(h)), "sk_lp_random")
+    return _lp_from_handle(h, "random%dx%d" % (m, n))
+
+
+def read_mps(path):
+    h = C.c_void_p()
+    check(lib().sk_lp_read_mps(path.encode(), C.byref(h)), "sk_lp_read_mps")
+    return _lp_from_handle(h, os.path.basename(path))
+
+
+def amd_ordering(m, n, rp, ci):
+    P = np.zeros(m, dtype=np.int32)
+    check(lib().sk_compute_amd_ordering(m, n, rp, ci, P), "sk_compute_amd_ordering")
+    return P
+
+
+def fill_ordering(m, n, rp, ci):
+    P = np.zeros(m, dtype=np.int32)
+    check(lib().sk_fill_ordering(m, n, rp, ci, P), "sk_fill_ordering")
+    return P
+
+
+def symbolic(m, n, rp, ci, P, cap=None):
+    cap = cap if cap is not None else max(1, m * (m - 1) // 2)
+    P = np.ascontiguousarray(P, dtype=np.int32)
+    Pinv = np.zeros(m, dtype=np.int32)
+    parent = np.zeros(m, dtype=np.int32)
+    Lrp = np.zeros(m + 1, dtype=np.int32)
+    Lci = np.zeros(cap, dtype=np.int32)
+    nnz = lib().sk_compute_symbolic(m, n, rp, ci, P, Pinv, parent, Lrp, Lci, cap)
+    if nnz < 0:
+        raise RuntimeError("sk_compute_symbolic failed (%d): %s" % (nnz, last_error()))
+    return Pinv, parent, Lrp, Lci[:nnz].copy()
