@@ -1,0 +1,298 @@
+"""Benchmark of the device Mehrotra IPM on the block-angular LP (family 1:
+40 blocks of 500x1200 + 2000 linking rows, m=22000, n=48000, 288k nnz).
+
+A step is one complete solve to 1e-8 relative primal / dual infeasibility and
+duality gap, mixed precision (FP32 fronts, FP64 residuals and refinement, FP64
+switch near convergence). value = LPs/s with the LP resident in device memory
+(CUDA events around sk_solver_run on the solver stream); e2e = LPs/s through the
+one-shot C ABI call sk_ipm_solve_csc from host arrays (analysis, upload, solve
+and download inside the timed region).
+
+--impl reference times the CPU restatement of the reference algorithm (oracle/,
+plain C, FP64, dense Cholesky) on all host cores over a bounded sample of the
+same LP family (see cpu_sample()).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "soverign-gpu-accelerator-_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+METRIC = "time-to-1e-8 gap & LPs/sec: mixed+learned vs plain FP64 IPM, same GB300"
+WORKLOAD = "block-angular LP, 40 blocks of 500x1200 + 2000 linking rows (m=22000, n=48000, 6 nnz/col), seed 0xC1"
+FULL_NNZ = 288000
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+def ensure_built():
+    import sankhya_gb300 as sk
+    if not os.path.exists(sk.LIB_PATH):
+        import __graft_entry__ as g
+        g.build()
+    return sk
+
+
+def cpu_sample(sk):
+    """Bounded CPU sample of the workload: one block of the same family
+    (500x1200 block + 50 linking rows, m=550, n=1200, 7200 nnz = 1/40 of the full
+    LP's nonzeros). CPU LPs/s on the full LP is reported as the sample rate x
+    7200/288000 (linear in nnz, which favours the CPU: its dense factorisation
+    grows as m^3)."""
+    return sk.block_angular(0xC1, 1, 500, 1200, 50, 5)
+
+
+class Clocks:
+    def __init__(self):
+        self.p = None
+        self.path = os.path.join(ROOT, "gpurun_out", "bench_clocks.csv") if os.path.isdir(
+            os.path.join(ROOT, "gpurun_out")) else "/tmp/bench_clocks.csv"
+
+    def start(self):
+        try:
+            self.f = open(self.path, "w")
+            self.p = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if not self.p:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.p.terminate()
+        self.p.wait()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        dev = os.environ.get("LOCAL_RANK", "0")
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, parts[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
+        return rank, world, dist
+    return rank, world, None
+
+
+def barrier_max(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_ours(args):
+    rank, world, dist = dist_setup(args)
+    sk = ensure_built()
+    import numpy as np
+    import torch
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    os.environ.setdefault("CUDA_VISIBLE_DEVICES", os.environ.get("CUDA_VISIBLE_DEVICES", ""))
+    lp = sk.generate(1, 0)
+    solver = sk.Solver([lp], precision=sk.PREC_MIXED)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")   # 256 MB > 129 MB L2
+    for _ in range(args.warmup):
+        solver.run()
+    info0, *_ = solver.result(0, want_vectors=False)
+    if info0["status"] != 0:
+        raise SystemExit("warm-up solve did not converge: %s" % info0)
+    clocks = Clocks()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    dev_ms = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        solver.run()
+        info, *_ = solver.result(0, want_vectors=False)
+        assert info["status"] == 0, info
+        dev_ms.append(info["device_ms"])
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    total_ms = barrier_max(dist, sum(dev_ms))
+    value = world * args.steps / (total_ms / 1000.0)
+    # kernel-class breakdown (instrumented replay of one factorisation + solve at the final iterate)
+    prof = solver.profile(fp32=True)
+    solver.close()
+    # plain FP64 solve of the same LP for the comparison the metric names
+    fp64 = sk.Solver([lp], precision=sk.PREC_FP64)
+    fp64.run()
+    info64, *_ = fp64.result(0, want_vectors=False)
+    fp64.run()
+    info64b, *_ = fp64.result(0, want_vectors=False)
+    prof64 = fp64.profile(fp32=False)
+    fp64.close()
+    # end to end through the C ABI (host arrays in, host solution out)
+    e2e_t = []
+    for _ in range(max(1, args.steps)):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        infoe, x, y, s = sk.solve(lp, precision=sk.PREC_MIXED)
+        e2e_t.append(time.perf_counter() - t)
+        assert infoe["status"] == 0
+    e2e_total = barrier_max(dist, sum(e2e_t))
+    e2e_value = world * len(e2e_t) / e2e_total
+    h2d = lp.nbytes()
+    d2h = (2 * lp.n + lp.m) * 8
+    hbm, bf16, src = peaks()
+    upd = prof["update"]
+    achieved_tflops = prof["update_flops"] / (upd["ms"] / 1000.0) / 1e12 if upd["ms"] > 0 else 0.0
+    roof = {"kernel": "k_update<float> (FP32 frontal trailing update, SIMT)", "bound": "tensor",
+            "achieved": achieved_tflops, "peak": bf16, "unit": "TFLOP/s", "frac": achieved_tflops / bf16,
+            "peak_source": "%s bf16 dense tensor peak (MEASURED_PEAKS.json bf16_tflops)" % src,
+            "traffic": None, "launches": upd["launches"], "ms_total": upd["ms"],
+            "note": "timed by an event-instrumented replay of one factorisation at the final iterate"}
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(sk, cores=1)
+    line = {"metric": METRIC, "value": value, "unit": "LPs/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32",
+            "data": "synthetic, seeded generator (family 1)",
+            "config": {"workload": WORKLOAD, "precision": "mixed (FP32 fronts, FP64 residuals/refinement)",
+                       "tolerance": "rel pinf, dinf, gap <= 1e-8", "l2": "256 MB buffer written between steps",
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "iterations": info["iterations"], "precision_path": info["precision_path"],
+                       "switch_iteration": info["switch_iteration"], "factorizations": info["factorizations"],
+                       "solves": info["solves"], "nnz_factor": info["nnz_factor"],
+                       "supernodes": info["num_supernodes"], "flops_per_factorization": info["flops_factor"]},
+            "plain_fp64": {"ms_per_solve": info64b["device_ms"], "iterations": info64b["iterations"],
+                           "lps_per_s": 1000.0 / info64b["device_ms"] if info64b["device_ms"] > 0 else None,
+                           "speedup_mixed_vs_fp64": info64b["device_ms"] / (total_ms / args.steps)},
+            "kernel_breakdown_ms": {"mixed": {k: v for k, v in prof.items() if isinstance(v, dict)},
+                                    "fp64": {k: v for k, v in prof64.items() if isinstance(v, dict)}},
+            "wall_s_timed_region": wall,
+            "gpu_launches": None,
+            "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
+            "e2e": {"value": e2e_value, "unit": "LPs/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "ms_per_step": 1000.0 * e2e_total / len(e2e_t)}}
+    if rank == 0:
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+def _cpu_worker(args):
+    import sk_oracle as so
+    import sankhya_gb300 as sk
+    lp = cpu_sample(sk)
+    t = time.perf_counter()
+    r, *_ = so.ipm_solve(lp)
+    return time.perf_counter() - t, r["status"], r["objective"]
+
+
+def cpu_baseline(sk, cores=1, rounds=12):
+    """Oracle port (FP64 CPU restatement of the reference algorithm) on the
+    bounded sample; `cores` processes each solve their own copy."""
+    import multiprocessing as mp
+    import sk_oracle as so
+    so.oracle()
+    lp = cpu_sample(sk)
+    t0 = time.perf_counter()
+    if cores == 1:
+        res = [_cpu_worker(None) for _ in range(rounds)]
+    else:
+        ctx = mp.get_context("spawn")
+        with ctx.Pool(cores) as pool:
+            res = pool.map(_cpu_worker, range(cores * rounds))
+    wall = time.perf_counter() - t0
+    n = len(res)
+    assert all(r[1] == 0 for r in res), res[:2]
+    sample_rate = n / wall
+    return {"value": sample_rate * lp.nnz / FULL_NNZ, "unit": "LPs/s", "cores": cores, "kind": "port",
+            "sample": "%d solves of the one-block member of the family (m=%d, n=%d, nnz=%d) on %d core(s), "
+                      "%.1f s; full-LP rate = sample rate x %d/%d nnz" % (n, lp.m, lp.n, lp.nnz, cores, wall,
+                                                                       lp.nnz, FULL_NNZ),
+            "sample_lps_per_s": sample_rate}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    sk = ensure_built()
+    import sk_oracle as so
+    so.oracle()
+    cores = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_baseline(sk, cores=cores, rounds=1)
+    vals = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        vals.append(cpu_baseline(sk, cores=cores, rounds=1))
+    wall = time.perf_counter() - t0
+    v = statistics.mean(x["value"] for x in vals)
+    line = {"metric": METRIC, "impl": "reference", "value": v, "unit": "LPs/s", "n_gpus": 0, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 * wall / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic, seeded generator (family 1)",
+            "config": {"workload": WORKLOAD, "implementation": "CPU restatement of the reference's Mehrotra IPM "
+                       "(oracle/sk_oracle.c, dense FP64 Cholesky); the reference's own CPU code cannot be built "
+                       "on the GPU host (its sources are not there)"},
+            "cpu_baseline": {"value": v, "unit": "LPs/s", "cores": cores, "kind": "port", "sample": vals[0]["sample"]},
+            "e2e": {"value": v, "unit": "LPs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -78,6 +78,8 @@ typedef struct sk_info {
     long long nnz_factor;     /* stored factor entries */
     int num_supernodes;
     int dense_front;          /* 1 if A A^T was treated as one dense front */
+    double device_ms;         /* last sk_solver_run measured with CUDA events on the solver stream */
+    double flops_factor;      /* algorithmic flops of one factorisation: sum_j c_j^2 over factor columns */
 } sk_info;
 
 /* Fills the defaults listed above. */
@@ -107,6 +109,15 @@ int sk_solver_set_start(sk_solver* h, int lp, const double* x, const double* y, 
 int sk_solver_run(sk_solver* h);
 int sk_solver_result(sk_solver* h, int lp, double* x, double* y, double* s, sk_info* info);
 void sk_solver_destroy(sk_solver* h);
+/* Kernel-class breakdown of one factorisation + one solve at the current iterate,
+ * replayed without graphs with CUDA events around every launch (diagnostics;
+ * not part of a solve). out[2*c] = total ms, out[2*c+1] = launches, for classes
+ * c = 0 assembly, 1 potrf, 2 trsm, 3 update, 4 extend-add, 5 forward solve,
+ * 6 backward solve; out[14] = algorithmic flops of the update launches, out[15] =
+ * bytes the update launches must move at least (each input tile read once, each
+ * output tile read and written once). fp32 selects the FP32 front path. Returns
+ * the number of values written (16). No reference counterpart. */
+int sk_solver_profile(sk_solver* h, int fp32, double* out, int cap);
 
 /* ---- KKT normal-equation engine (device pointers) ----
  * Replaces: gpu::GPUKKTCholeskySolver (src/cuda/kkt.cuh:28-71). A is CSR (m x n).
@@ -151,6 +162,10 @@ typedef struct sk_lp sk_lp;
 int sk_lp_read_mps(const char* path, sk_lp** out);
 int sk_lp_generate(int family, int instance, sk_lp** out);
 int sk_lp_random(int m, int n, double density, unsigned long long seed, sk_lp** out);
+/* Block-angular member of family 1 with a chosen shape (family 1 itself is
+ * blocks=40, block_rows=500, block_cols=1200, link_rows=2000, nnz_per_col=5). */
+int sk_lp_block_angular(unsigned long long seed, int blocks, int block_rows, int block_cols, int link_rows,
+                        int nnz_per_col, sk_lp** out);
 int sk_lp_dims(const sk_lp* lp, int* m, int* n, int* nnz);
 /* Pointers into the LP's own storage (valid until sk_lp_free). lb / ub may be NULL. */
 int sk_lp_arrays(const sk_lp* lp, const int** col_ptrs, const int** row_idx, const double** vals,

@@ -1,0 +1,356 @@
+// Device-side C ABI entry points (include/sankhya/sk_ipm.h): one-shot and
+// persistent IPM solves, the KKT engine and the SpMV kernel.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "api/sk_error.hpp"
+#include "cuda/device_ipm.hpp"
+#include "cuda/kkt_engine.hpp"
+#include "ipm/front_plan.hpp"
+#include "sankhya/sk_ipm.h"
+
+using namespace sankhya;
+
+struct sk_solver {
+    std::unique_ptr<dev::DeviceIPM> ipm;
+};
+
+struct sk_kkt {
+    int m = 0, n = 0, precision = 0;
+    cudaStream_t st = nullptr;
+    dev::Arena arena;
+    dev::Slot<int> a_rp, a_ci, t_rp, t_ci, row_lp, col_lp;
+    dev::Slot<double> a_v, t_v, theta, out, r, corr, bak, tmp, scratch, hostio;
+    dev::DeviceLP lp;
+    std::unique_ptr<dev::KktEngine> eng;
+    bool factored = false;
+    ~sk_kkt() {
+        eng.reset();
+        if (st) cudaStreamDestroy(st);
+    }
+};
+
+namespace {
+
+sk_options opts_or_default(const sk_options* o) {
+    sk_options d;
+    sk_options_default(&d);
+    return o ? *o : d;
+}
+
+void check_options(const sk_options& o) {
+    if (o.precision != SK_PREC_FP64 && o.precision != SK_PREC_MIXED) throw std::invalid_argument("bad precision");
+    if (o.start < SK_START_UNIT || o.start > SK_START_USER) throw std::invalid_argument("bad start");
+    if (o.criteria != SK_CRIT_RELATIVE && o.criteria != SK_CRIT_REFERENCE) throw std::invalid_argument("bad criteria");
+    if (!(o.tol > 0.0) || o.max_iter < 0 || o.ruiz_passes < 0) throw std::invalid_argument("bad tolerance / limits");
+    if (o.ordering < SK_ORDER_AUTO || o.ordering > SK_ORDER_NATURAL) throw std::invalid_argument("bad ordering");
+}
+
+void check_csc(int m, int n, const int* cp, const int* ri, const double* v, const double* b, const double* c) {
+    if (m <= 0 || n <= 0 || !cp || !b || !c) throw std::invalid_argument("invalid LP arrays");
+    if (cp[0] != 0) throw std::invalid_argument("col_ptrs[0] != 0");
+    for (int j = 0; j < n; ++j) if (cp[j + 1] < cp[j]) throw std::invalid_argument("col_ptrs not monotone");
+    if (cp[n] > 0 && (!ri || !v)) throw std::invalid_argument("invalid LP arrays");
+}
+
+}  // namespace
+
+extern "C" {
+
+int sk_ipm_solve_csc(int m, int n, const int* col_ptrs, const int* row_idx, const double* vals, const double* b,
+                     const double* c, const sk_options* opt, double* x, double* y, double* s, sk_info* info) {
+    api::clear_error();
+    try {
+        const sk_options o = opts_or_default(opt);
+        check_options(o);
+        check_csc(m, n, col_ptrs, row_idx, vals, b, c);
+        ipm::LpView v;
+        v.m = m; v.n = n; v.col_ptrs = col_ptrs; v.row_idx = row_idx; v.vals = vals;
+        dev::DeviceIPM solver({v}, {b}, {c}, o);
+        solver.run();
+        solver.result(0, x, y, s, info);
+        return SK_OK;
+    } catch (...) {
+        return api::status_of_current_exception();
+    }
+}
+
+int sk_solver_create(int num_lps, const int* m, const int* n, const int* const* col_ptrs, const int* const* row_idx,
+                     const double* const* vals, const double* const* b, const double* const* c, const sk_options* opt,
+                     sk_solver** out) {
+    api::clear_error();
+    if (!out || num_lps <= 0 || !m || !n || !col_ptrs || !row_idx || !vals || !b || !c) return SK_ERR_INVALID;
+    try {
+        const sk_options o = opts_or_default(opt);
+        check_options(o);
+        std::vector<ipm::LpView> views(num_lps);
+        std::vector<const double*> bv(num_lps), cv(num_lps);
+        for (int k = 0; k < num_lps; ++k) {
+            check_csc(m[k], n[k], col_ptrs[k], row_idx[k], vals[k], b[k], c[k]);
+            views[k].m = m[k]; views[k].n = n[k];
+            views[k].col_ptrs = col_ptrs[k]; views[k].row_idx = row_idx[k]; views[k].vals = vals[k];
+            bv[k] = b[k];
+            cv[k] = c[k];
+        }
+        auto* h = new sk_solver;
+        try {
+            h->ipm.reset(new dev::DeviceIPM(views, bv, cv, o));
+        } catch (...) {
+            delete h;
+            throw;
+        }
+        *out = h;
+        return SK_OK;
+    } catch (...) {
+        return api::status_of_current_exception();
+    }
+}
+
+int sk_solver_set_start(sk_solver* h, int lp, const double* x, const double* y, const double* s) {
+    api::clear_error();
+    if (!h) return SK_ERR_INVALID;
+    try {
+        h->ipm->set_start(lp, x, y, s);
+        return SK_OK;
+    } catch (...) {
+        return api::status_of_current_exception();
+    }
+}
+
+int sk_solver_run(sk_solver* h) {
+    api::clear_error();
+    if (!h) return SK_ERR_INVALID;
+    try {
+        h->ipm->run();
+        return SK_OK;
+    } catch (...) {
+        return api::status_of_current_exception();
+    }
+}
+
+int sk_solver_result(sk_solver* h, int lp, double* x, double* y, double* s, sk_info* info) {
+    api::clear_error();
+    if (!h) return SK_ERR_INVALID;
+    try {
+        h->ipm->result(lp, x, y, s, info);
+        return SK_OK;
+    } catch (...) {
+        return api::status_of_current_exception();
+    }
+}
+
+void sk_solver_destroy(sk_solver* h) { delete h; }
+
+int sk_solver_profile(sk_solver* h, int fp32, double* out, int cap) {
+    api::clear_error();
+    if (!h || !out || cap < 16) return -SK_ERR_INVALID;
+    try {
+        h->ipm->profile(fp32 != 0, out);
+        return 16;
+    } catch (...) {
+        return -api::status_of_current_exception();
+    }
+}
+
+int sk_kkt_create(int m, int n, const int* row_ptrs, const int* col_idx, const double* vals, const int* P,
+                  int precision, sk_kkt** out) {
+    api::clear_error();
+    if (!out || m <= 0 || n <= 0 || !row_ptrs || !col_idx || !vals) return SK_ERR_INVALID;
+    if (precision != SK_PREC_FP64 && precision != SK_PREC_MIXED) return SK_ERR_INVALID;
+    try {
+        core::CSRMatrix A = api::pattern_csr(m, n, row_ptrs, col_idx);
+        A.values.assign(vals, vals + row_ptrs[m]);
+        int ndev = 0;
+        if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+            throw api::sk_exception(SK_ERR_NO_DEVICE, "no CUDA device visible");
+        std::unique_ptr<sk_kkt> k(new sk_kkt);
+        k->m = m;
+        k->n = n;
+        k->precision = precision;
+        SK_CUDA(cudaStreamCreateWithFlags(&k->st, cudaStreamNonBlocking));
+        // CSC of A
+        const int nz = row_ptrs[m];
+        std::vector<int> cp(n + 1, 0), ri(nz);
+        std::vector<double> cv(nz);
+        for (int q = 0; q < nz; ++q) cp[col_idx[q] + 1]++;
+        for (int j = 0; j < n; ++j) cp[j + 1] += cp[j];
+        std::vector<int> nx(cp.begin(), cp.end() - 1);
+        for (int i = 0; i < m; ++i)
+            for (int q = row_ptrs[i]; q < row_ptrs[i + 1]; ++q) {
+                const int d = nx[col_idx[q]]++;
+                ri[d] = i;
+                cv[d] = vals[q];
+            }
+        ipm::LpView v;
+        v.m = m; v.n = n; v.col_ptrs = cp.data(); v.row_idx = ri.data(); v.vals = cv.data();
+        ipm::FrontPlan plan;
+        std::vector<Index> pv;
+        if (P) pv.assign(P, P + m);
+        ipm::build_front_plan({v}, A, SK_ORDER_AUTO, plan, P ? &pv : nullptr);
+        dev::Arena& ar = k->arena;
+        dev::reserve(ar, k->a_rp, m + 1); dev::reserve(ar, k->a_ci, nz); dev::reserve(ar, k->a_v, nz);
+        dev::reserve(ar, k->t_rp, n + 1); dev::reserve(ar, k->t_ci, nz); dev::reserve(ar, k->t_v, nz);
+        dev::reserve(ar, k->row_lp, m); dev::reserve(ar, k->col_lp, n);
+        for (auto* s : {&k->out, &k->r, &k->corr, &k->bak, &k->tmp, &k->hostio}) dev::reserve(ar, *s, m);
+        dev::reserve(ar, k->theta, n);
+        dev::reserve(ar, k->scratch, 64);
+        ar.commit();
+        for (auto* s : {&k->a_rp, &k->a_ci, &k->t_rp, &k->t_ci, &k->row_lp, &k->col_lp}) dev::bind(ar, *s);
+        for (auto* s : {&k->a_v, &k->t_v, &k->out, &k->r, &k->corr, &k->bak, &k->tmp, &k->hostio, &k->theta,
+                        &k->scratch})
+            dev::bind(ar, *s);
+        dev::upload(k->a_rp, A.row_ptrs, k->st); dev::upload(k->a_ci, A.col_indices, k->st);
+        dev::upload(k->a_v, A.values, k->st); dev::upload(k->t_rp, cp, k->st); dev::upload(k->t_ci, ri, k->st);
+        dev::upload(k->t_v, cv, k->st);
+        SK_CUDA(cudaMemsetAsync(k->row_lp.ptr, 0, sizeof(int) * m, k->st));
+        SK_CUDA(cudaMemsetAsync(k->col_lp.ptr, 0, sizeof(int) * n, k->st));
+        auto& lp = k->lp;
+        lp.nlp = 1; lp.M = m; lp.N = n; lp.nnz = nz;
+        lp.a_rp = k->a_rp.ptr; lp.a_ci = k->a_ci.ptr; lp.a_v = k->a_v.ptr;
+        lp.t_rp = k->t_rp.ptr; lp.t_ci = k->t_ci.ptr; lp.t_v = k->t_v.ptr;
+        lp.row_lp = k->row_lp.ptr; lp.col_lp = k->col_lp.ptr;
+        k->eng.reset(new dev::KktEngine(plan, k->lp, k->st));
+        SK_CUDA(cudaStreamSynchronize(k->st));
+        *out = k.release();
+        return SK_OK;
+    } catch (...) {
+        return api::status_of_current_exception();
+    }
+}
+
+int sk_kkt_factorize_device(sk_kkt* k, const double* d_theta) {
+    api::clear_error();
+    if (!k || !d_theta) return SK_ERR_INVALID;
+    try {
+        SK_CUDA(cudaMemcpyAsync(k->theta.ptr, d_theta, sizeof(double) * k->n, cudaMemcpyDeviceToDevice, k->st));
+        const bool fp32 = k->precision == SK_PREC_MIXED;
+        double delta = fp32 ? 1e-7 : 1e-9;
+        for (int retry = 0; retry < 5; ++retry, delta *= 10.0) {
+            if (k->eng->factor(k->theta.ptr, delta, fp32)) {
+                k->factored = true;
+                return SK_OK;
+            }
+        }
+        k->factored = false;
+        api::set_error("factorisation failed: matrix is not positive definite for any regularisation");
+        return SK_ERR_NUMERICAL;
+    } catch (...) {
+        return api::status_of_current_exception();
+    }
+}
+
+int sk_kkt_solve_device(sk_kkt* k, double* d_rhs, double tol) {
+    api::clear_error();
+    if (!k || !d_rhs) return SK_ERR_INVALID;
+    if (!k->factored) { api::set_error("solve before a successful factorisation"); return SK_ERR_INVALID; }
+    try {
+        const int m = k->m;
+        cudaStream_t st = k->st;
+        auto& E = *k->eng;
+        const double rn_rhs = dev::absmax_device(m, d_rhs, k->scratch.ptr, st);
+        const double t = tol * std::max(1.0, rn_rhs);
+        E.apply_inverse(d_rhs, k->out.ptr);
+        auto resid = [&]() {
+            E.apply_normal(k->theta.ptr, k->out.ptr, k->tmp.ptr);
+            dev::vec_diff(m, d_rhs, k->tmp.ptr, k->r.ptr, st);
+            return dev::absmax_device(m, k->r.ptr, k->scratch.ptr, st);
+        };
+        double rn = resid();
+        const int max_ir = k->precision == SK_PREC_MIXED ? 30 : 10;
+        for (int it = 0; it < max_ir && rn > t; ++it) {
+            SK_CUDA(cudaMemcpyAsync(k->bak.ptr, k->out.ptr, sizeof(double) * m, cudaMemcpyDeviceToDevice, st));
+            E.apply_inverse(k->r.ptr, k->corr.ptr);
+            dev::vec_add(m, k->corr.ptr, k->out.ptr, st);
+            const double rn2 = resid();
+            if (rn2 >= rn) {
+                SK_CUDA(cudaMemcpyAsync(k->out.ptr, k->bak.ptr, sizeof(double) * m, cudaMemcpyDeviceToDevice, st));
+                break;
+            }
+            rn = rn2;
+        }
+        SK_CUDA(cudaMemcpyAsync(d_rhs, k->out.ptr, sizeof(double) * m, cudaMemcpyDeviceToDevice, st));
+        SK_CUDA(cudaStreamSynchronize(st));
+        return rn <= t ? SK_OK : SK_ERR_NUMERICAL;
+    } catch (...) {
+        return api::status_of_current_exception();
+    }
+}
+
+int sk_kkt_factorize(sk_kkt* k, const double* theta) {
+    api::clear_error();
+    if (!k || !theta) return SK_ERR_INVALID;
+    try {
+        dev::Arena tmp;
+        dev::Slot<double> th;
+        dev::reserve(tmp, th, k->n);
+        tmp.commit();
+        dev::bind(tmp, th);
+        SK_CUDA(cudaMemcpyAsync(th.ptr, theta, sizeof(double) * k->n, cudaMemcpyHostToDevice, k->st));
+        SK_CUDA(cudaStreamSynchronize(k->st));
+        return sk_kkt_factorize_device(k, th.ptr);
+    } catch (...) {
+        return api::status_of_current_exception();
+    }
+}
+
+int sk_kkt_solve(sk_kkt* k, double* rhs, double tol) {
+    api::clear_error();
+    if (!k || !rhs) return SK_ERR_INVALID;
+    try {
+        SK_CUDA(cudaMemcpyAsync(k->hostio.ptr, rhs, sizeof(double) * k->m, cudaMemcpyHostToDevice, k->st));
+        SK_CUDA(cudaStreamSynchronize(k->st));
+        const int rc = sk_kkt_solve_device(k, k->hostio.ptr, tol);
+        if (rc != SK_OK && rc != SK_ERR_NUMERICAL) return rc;
+        SK_CUDA(cudaMemcpyAsync(rhs, k->hostio.ptr, sizeof(double) * k->m, cudaMemcpyDeviceToHost, k->st));
+        SK_CUDA(cudaStreamSynchronize(k->st));
+        return rc;
+    } catch (...) {
+        return api::status_of_current_exception();
+    }
+}
+
+int sk_kkt_get_factor(sk_kkt* k, double* L_dense, double* D) {
+    api::clear_error();
+    if (!k || !L_dense) return SK_ERR_INVALID;
+    if (!k->factored) return SK_ERR_INVALID;
+    try {
+        const auto& p = k->eng->plan();
+        std::vector<double> F = k->eng->fronts_host();
+        const int m = k->m;
+        std::memset(L_dense, 0, sizeof(double) * static_cast<size_t>(m) * m);
+        for (int s = 0; s < p.ns; ++s) {
+            const int N = p.sn_nrows[s], K = p.sn_ncols[s], f = p.sn_first[s];
+            const int* R = p.rows.data() + p.sn_rows_off[s];
+            for (int c = 0; c < K; ++c)
+                for (int r = c; r < N; ++r)
+                    L_dense[static_cast<size_t>(R[r]) * m + (f + c)] = F[p.sn_F_off[s] + r + static_cast<int64_t>(c) * N];
+        }
+        if (D) {
+            SK_CUDA(cudaMemcpyAsync(D, k->eng->diag_D(), sizeof(double) * m, cudaMemcpyDeviceToHost, k->st));
+            SK_CUDA(cudaStreamSynchronize(k->st));
+        }
+        return SK_OK;
+    } catch (...) {
+        return api::status_of_current_exception();
+    }
+}
+
+void sk_kkt_destroy(sk_kkt* k) { delete k; }
+
+int sk_spmv_csr(int rows, const int* d_row_ptrs, const int* d_col_idx, const double* d_vals, const double* d_x,
+                double alpha, double beta, double* d_y, void* stream) {
+    api::clear_error();
+    if (rows < 0 || (rows > 0 && (!d_row_ptrs || !d_col_idx || !d_vals || !d_x || !d_y))) return SK_ERR_INVALID;
+    try {
+        dev::spmv_csr(rows, d_row_ptrs, d_col_idx, d_vals, d_x, alpha, beta, d_y, static_cast<cudaStream_t>(stream));
+        return SK_OK;
+    } catch (...) {
+        return api::status_of_current_exception();
+    }
+}
+
+}  // extern "C"

@@ -116,6 +116,24 @@ int sk_lp_random(int m, int n, double density, unsigned long long seed, sk_lp** 
     }
 }
 
+int sk_lp_block_angular(unsigned long long seed, int blocks, int block_rows, int block_cols, int link_rows,
+                        int nnz_per_col, sk_lp** out) {
+    api::clear_error();
+    if (!out || blocks <= 0 || block_rows <= 0 || block_cols <= 0 || link_rows < 0 || nnz_per_col <= 0 ||
+        nnz_per_col > block_rows)
+        return SK_ERR_INVALID;
+    try {
+        auto g = gen::block_angular_lp(seed, blocks, block_rows, block_cols, link_rows, nnz_per_col);
+        auto* lp = new sk_lp;
+        lp->model = core::Model::from_csc(g.m, g.n, g.col_ptrs.data(), g.row_idx.data(), g.vals.data(),
+                                          g.b.data(), g.c.data());
+        *out = lp;
+        return SK_OK;
+    } catch (...) {
+        return api::status_of_current_exception();
+    }
+}
+
 int sk_lp_read_mps(const char* path, sk_lp** out) {
     api::clear_error();
     if (!path || !out) return SK_ERR_INVALID;

@@ -1,0 +1,948 @@
+// Device Mehrotra predictor-corrector IPM (batch of LPs, lock-step iterations
+// with per-LP masks). Follows the reference's MehrotraSolver::Impl
+// (src/ipm/mehrotra_device.cu:276-1047):
+//   * 10-pass inline Ruiz scaling (:289-323), unit start x = s = 1, y = 0 (:93-102)
+//   * predictor: r_xs = -x s, v = -Theta rd - r_xs/s, rkkt = -rp + A v (:783-786)
+//   * ds = -rd - A^T dy, dx = -Theta ds + r_xs/s (:799-802, :128-133)
+//   * direction check e1, e2, e3 <= 1e-8 (:494-587)
+//   * sigma = min(1, (mu_aff/mu)^3), corrector r_xs = -x s + sigma mu - dx_aff ds_aff (:839-843)
+//   * eta = 0.995, Armijo 1e-4 backtracking on the normalised residual sum with up
+//     to 15 halvings, then a centred direction (sigma_c = 1/2, common step, up to 30
+//     halvings) (:873-996)
+//   * normal-equation solves to ||r||_inf <= 1e-9 max(1, ||rp||_2) with up to 10
+//     steps of FP64 iterative refinement and rollback on stagnation
+//     (src/cuda/kkt.cu:620-870, src/ipm/mehrotra_device.cu:791)
+// Differences by design: the normal matrix is factored once per iteration (the
+// reference refactors on every solve), D (A Theta A^T) D + delta I with
+// delta = 1e-9 x 10^retry is the only factorisation (the reference's extra
+// unequilibrated factor is overwritten by its solve), reductions are
+// deterministic per LP, and in mixed precision the factor is FP32 until mu drops
+// below the switch threshold or an FP32 solve misses its tolerance.
+#include "cuda/device_ipm.hpp"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+
+namespace sankhya {
+namespace dev {
+
+namespace {
+
+constexpr int kChunk = 4096;
+constexpr int kMaxR = 10;
+enum { OP_SUM = 0, OP_MAX = 1, OP_MIN = 2 };
+
+inline int nblk(int64_t n, int t = 256) { return static_cast<int>((n + t - 1) / t); }
+
+// ---------------------------------------------------------------- SpMV
+
+template <int G, class Epi>
+__global__ void __launch_bounds__(256) k_spmv(int rows, const int* __restrict__ rp, const int* __restrict__ ci,
+                                              const double* __restrict__ v, const double* __restrict__ x, Epi epi) {
+    const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int row = gid / G, lane = gid % G;
+    const bool valid = row < rows;
+    double acc = 0.0;
+    if (valid)
+        for (int q = rp[row] + lane; q < rp[row + 1]; q += G) acc += v[q] * x[ci[q]];
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, G);
+    if (valid && lane == 0) epi(row, acc);
+}
+
+template <class Epi>
+void spmv(int rows, int group, const int* rp, const int* ci, const double* v, const double* x, Epi epi,
+          cudaStream_t st) {
+    if (rows <= 0) return;
+    const int64_t threads = static_cast<int64_t>(rows) * group;
+    switch (group) {
+    case 2: k_spmv<2><<<nblk(threads), 256, 0, st>>>(rows, rp, ci, v, x, epi); break;
+    case 4: k_spmv<4><<<nblk(threads), 256, 0, st>>>(rows, rp, ci, v, x, epi); break;
+    case 8: k_spmv<8><<<nblk(threads), 256, 0, st>>>(rows, rp, ci, v, x, epi); break;
+    case 16: k_spmv<16><<<nblk(threads), 256, 0, st>>>(rows, rp, ci, v, x, epi); break;
+    default: k_spmv<32><<<nblk(threads), 256, 0, st>>>(rows, rp, ci, v, x, epi); break;
+    }
+}
+
+int pick_group(int64_t nnz, int rows) {
+    const double avg = rows > 0 ? static_cast<double>(nnz) / rows : 0.0;
+    if (avg <= 3) return 2;
+    if (avg <= 6) return 4;
+    if (avg <= 12) return 8;
+    if (avg <= 24) return 16;
+    return 32;
+}
+
+struct EpiAxpby {
+    double alpha, beta;
+    double* y;
+    __device__ void operator()(int i, double d) const { y[i] = beta == 0.0 ? alpha * d : alpha * d + beta * y[i]; }
+};
+struct EpiSub {          // out = d - a
+    const double* a;
+    double* out;
+    __device__ void operator()(int i, double d) const { out[i] = d - a[i]; }
+};
+struct EpiAdd {          // out = d + a
+    const double* a;
+    double* out;
+    __device__ void operator()(int i, double d) const { out[i] = d + a[i]; }
+};
+struct EpiRd {           // rd = A^T y + s - c
+    const double* s;
+    const double* c;
+    double* rd;
+    __device__ void operator()(int j, double d) const { rd[j] = d + s[j] - c[j]; }
+};
+struct EpiRhsMinus {     // r = rhs - d
+    const double* rhs;
+    double* r;
+    __device__ void operator()(int i, double d) const { r[i] = rhs[i] - d; }
+};
+struct EpiTheta {        // out = theta * d
+    const double* theta;
+    double* out;
+    __device__ void operator()(int j, double d) const { out[j] = theta[j] * d; }
+};
+struct EpiDsDx {         // t = A^T dy: ds = -rd - t, dx = -theta ds + rxs / s, e2, e3
+    const double *rd, *theta, *rxs, *x, *s;
+    double *ds, *dx, *e2, *e3;
+    __device__ void operator()(int j, double t) const {
+        const double dsj = -rd[j] - t;
+        const double dxj = -theta[j] * dsj + rxs[j] / s[j];
+        ds[j] = dsj;
+        dx[j] = dxj;
+        e2[j] = rd[j] + dsj + t;
+        e3[j] = s[j] * dxj + x[j] * dsj - rxs[j];
+    }
+};
+
+// ------------------------------------------------------------ reductions
+
+template <int R, class F>
+__global__ void __launch_bounds__(256) k_reduce(const int* __restrict__ cstart, const int* __restrict__ cend, F f,
+                                                double* __restrict__ partial) {
+    __shared__ double sh[8][R];
+    double acc[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) acc[r] = F::op(r) == OP_SUM ? 0.0 : (F::op(r) == OP_MAX ? -HUGE_VAL : HUGE_VAL);
+    const int q = blockIdx.x;
+    for (int i = cstart[q] + threadIdx.x; i < cend[q]; i += blockDim.x) {
+        double v[R];
+        f(i, v);
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+            acc[r] = F::op(r) == OP_SUM ? acc[r] + v[r] : (F::op(r) == OP_MAX ? fmax(acc[r], v[r]) : fmin(acc[r], v[r]));
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        double a = acc[r];
+        if (F::op(r) == OP_SUM) a = warp_sum(a);
+        else if (F::op(r) == OP_MAX) a = warp_max(a);
+        else a = warp_min(a);
+        if (lane == 0) sh[wid][r] = a;
+    }
+    __syncthreads();
+    if (threadIdx.x < R) {
+        const int r = threadIdx.x;
+        double a = sh[0][r];
+        for (int w = 1; w < static_cast<int>(blockDim.x >> 5); ++w)
+            a = F::op(r) == OP_SUM ? a + sh[w][r] : (F::op(r) == OP_MAX ? fmax(a, sh[w][r]) : fmin(a, sh[w][r]));
+        partial[static_cast<int64_t>(q) * R + r] = a;
+    }
+}
+
+template <int R, class F>
+__global__ void k_reduce_final(int nlp, const int* __restrict__ cptr, const double* __restrict__ partial,
+                               double* __restrict__ out) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nlp * R) return;
+    const int k = t / R, r = t % R;
+    double a = F::op(r) == OP_SUM ? 0.0 : (F::op(r) == OP_MAX ? -HUGE_VAL : HUGE_VAL);
+    for (int q = cptr[k]; q < cptr[k + 1]; ++q) {
+        const double v = partial[static_cast<int64_t>(q) * R + r];
+        a = F::op(r) == OP_SUM ? a + v : (F::op(r) == OP_MAX ? fmax(a, v) : fmin(a, v));
+    }
+    out[k * R + r] = a;
+}
+
+struct RedResidM {       // [sum rp^2, max |rp/R|, sum b y]
+    const double *rp, *R, *b, *y;
+    __device__ static constexpr int op(int r) { return r == 1 ? OP_MAX : OP_SUM; }
+    __device__ void operator()(int i, double* v) const {
+        v[0] = rp[i] * rp[i];
+        v[1] = fabs(rp[i] / R[i]);
+        v[2] = b[i] * y[i];
+    }
+};
+struct RedResidN {       // [sum rd^2, max |rd/C|, sum x s, sum c x]
+    const double *rd, *C, *x, *s, *c;
+    __device__ static constexpr int op(int r) { return r == 1 ? OP_MAX : OP_SUM; }
+    __device__ void operator()(int j, double* v) const {
+        v[0] = rd[j] * rd[j];
+        v[1] = fabs(rd[j] / C[j]);
+        v[2] = x[j] * s[j];
+        v[3] = c[j] * x[j];
+    }
+};
+struct RedSq {           // [sum a^2]
+    const double* a;
+    __device__ static constexpr int op(int) { return OP_SUM; }
+    __device__ void operator()(int i, double* v) const { v[0] = a[i] * a[i]; }
+};
+struct RedAbsMax {       // [max |a|]
+    const double* a;
+    __device__ static constexpr int op(int) { return OP_MAX; }
+    __device__ void operator()(int i, double* v) const { v[0] = fabs(a[i]); }
+};
+struct RedDir {          // [e2^2, e3^2, rxs^2, ratio x, ratio s, x s, x ds, dx s, dx ds]
+    const double *e2, *e3, *rxs, *x, *s, *dx, *ds;
+    __device__ static constexpr int op(int r) { return (r == 3 || r == 4) ? OP_MIN : OP_SUM; }
+    __device__ void operator()(int j, double* v) const {
+        v[0] = e2[j] * e2[j];
+        v[1] = e3[j] * e3[j];
+        v[2] = rxs[j] * rxs[j];
+        v[3] = dx[j] < 0.0 ? -x[j] / dx[j] : 1.0e30;
+        v[4] = ds[j] < 0.0 ? -s[j] / ds[j] : 1.0e30;
+        v[5] = x[j] * s[j];
+        v[6] = x[j] * ds[j];
+        v[7] = dx[j] * s[j];
+        v[8] = dx[j] * ds[j];
+    }
+};
+struct RedTrialM {       // [sum rp^2, sum y^2]
+    const double *rp, *y;
+    __device__ static constexpr int op(int) { return OP_SUM; }
+    __device__ void operator()(int i, double* v) const {
+        v[0] = rp[i] * rp[i];
+        v[1] = y[i] * y[i];
+    }
+};
+struct RedTrialN {       // [sum rd^2, sum x s, min x, min s]
+    const double *rd, *x, *s;
+    __device__ static constexpr int op(int r) { return r >= 2 ? OP_MIN : OP_SUM; }
+    __device__ void operator()(int j, double* v) const {
+        v[0] = rd[j] * rd[j];
+        v[1] = x[j] * s[j];
+        v[2] = x[j];
+        v[3] = s[j];
+    }
+};
+
+// --------------------------------------------------------- elementwise
+
+__global__ void k_fill(int n, double* a, double v) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] = v;
+}
+__global__ void k_theta(int n, const double* __restrict__ x, const double* __restrict__ s,
+                        const int* __restrict__ col_lp, const double* __restrict__ mask, double* __restrict__ th) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < n) th[j] = mask[col_lp[j]] != 0.0 ? x[j] / s[j] : 1.0;
+}
+// r_xs = -x s + target[lp] - (dxa ds a if given); v = -theta rd - r_xs / s
+__global__ void k_rhs(int n, const double* __restrict__ x, const double* __restrict__ s,
+                      const double* __restrict__ theta, const double* __restrict__ rd, const double* __restrict__ dxa,
+                      const double* __restrict__ dsa, const double* __restrict__ target,
+                      const int* __restrict__ col_lp, double* __restrict__ rxs, double* __restrict__ v) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    double r = -x[j] * s[j] + (target ? target[col_lp[j]] : 0.0);
+    if (dxa) r -= dxa[j] * dsa[j];
+    rxs[j] = r;
+    v[j] = -theta[j] * rd[j] - r / s[j];
+}
+// trial point: xt = x + ap dx ; st = s + ad ds (n) ; yt = y + ad dy (m)
+__global__ void k_trial_n(int n, const double* __restrict__ x, const double* __restrict__ s,
+                          const double* __restrict__ dx, const double* __restrict__ ds, const double* __restrict__ ap,
+                          const double* __restrict__ ad, const int* __restrict__ col_lp, double* __restrict__ xt,
+                          double* __restrict__ st) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const int k = col_lp[j];
+    xt[j] = x[j] + ap[k] * dx[j];
+    st[j] = s[j] + ad[k] * ds[j];
+}
+__global__ void k_trial_m(int m, const double* __restrict__ y, const double* __restrict__ dy,
+                          const double* __restrict__ ad, const int* __restrict__ row_lp, double* __restrict__ yt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < m) yt[i] = y[i] + ad[row_lp[i]] * dy[i];
+}
+// dst = mask[lp] ? src : dst
+__global__ void k_masked_copy(int n, const double* __restrict__ src, const int* __restrict__ lp_of,
+                              const double* __restrict__ mask, double* __restrict__ dst) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && mask[lp_of[i]] != 0.0) dst[i] = src[i];
+}
+// dst += mask[lp] * src
+__global__ void k_masked_add(int n, const double* __restrict__ src, const int* __restrict__ lp_of,
+                             const double* __restrict__ mask, double* __restrict__ dst) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && mask[lp_of[i]] != 0.0) dst[i] += src[i];
+}
+
+}  // namespace
+
+void spmv_csr(int rows, const int* rp, const int* ci, const double* v, const double* x, double alpha, double beta,
+              double* y, cudaStream_t st) {
+    spmv(rows, 8, rp, ci, v, x, EpiAxpby{alpha, beta, y}, st);
+    SK_CUDA(cudaGetLastError());
+}
+
+// =====================================================================
+
+struct DeviceIPM::Impl {
+    sk_options opt;
+    int nlp = 0, M = 0, N = 0;
+    cudaStream_t st = nullptr;
+    Arena arena;
+    std::vector<int> m_of, n_of, row_off, col_off;
+    std::vector<double> R_h, C_h;           // Ruiz factors (batch order)
+    std::vector<double> binf, cinf;         // ||b||_inf, ||c||_inf of the unscaled LPs
+    // device vectors
+    Slot<int> a_rp, a_ci, t_rp, t_ci, row_lp, col_lp, mc_s, mc_e, mc_p, nc_s, nc_e, nc_p;
+    Slot<double> a_v, t_v, b, c, R, C;
+    Slot<double> x, y, s, rp, rd, theta, rxs, v, rkkt, dy, dx, ds, dxa, dya, dsa, e1, e2, e3;
+    Slot<double> xt, yt, stt, rpt, rdt, r, corr, bak, tm, cdx, cdy, cds, crxs;
+    Slot<double> scal;                      // per-LP scalars [8][nlp]
+    Slot<double> partial, redout;
+    int max_chunks = 0;
+    // host per-LP state
+    std::vector<LpResult> res;
+    std::vector<char> active, user_start;
+    std::vector<double> rp0, rd0, mu0;
+    int factorizations = 0, solves = 0, refine_steps = 0, precision_path = 0;
+    bool switched = false, used_fp32 = false;
+    double solve_ms = 0.0, device_ms = 0.0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::vector<double> hx0, hy0, hs0;      // user start (scaled)
+    int ga = 4, gt = 4;
+
+    double* sc(int which) { return scal.ptr + static_cast<size_t>(which) * nlp; }
+    void put_scalars(int which, const std::vector<double>& v) {
+        SK_CUDA(cudaMemcpyAsync(sc(which), v.data(), sizeof(double) * nlp, cudaMemcpyHostToDevice, st));
+    }
+
+    template <int R, class F>
+    void reduce_rows(F f, double* out_dev) {
+        k_reduce<R><<<static_cast<int>(mc_s.count), 256, 0, st>>>(mc_s.ptr, mc_e.ptr, f, partial.ptr);
+        k_reduce_final<R, F><<<nblk(static_cast<int64_t>(nlp) * R), 256, 0, st>>>(nlp, mc_p.ptr, partial.ptr, out_dev);
+    }
+    template <int R, class F>
+    void reduce_cols(F f, double* out_dev) {
+        k_reduce<R><<<static_cast<int>(nc_s.count), 256, 0, st>>>(nc_s.ptr, nc_e.ptr, f, partial.ptr);
+        k_reduce_final<R, F><<<nblk(static_cast<int64_t>(nlp) * R), 256, 0, st>>>(nlp, nc_p.ptr, partial.ptr, out_dev);
+    }
+    // copies `count` doubles of redout to host (synchronising)
+    std::vector<double> fetch(size_t count) {
+        std::vector<double> h(count);
+        SK_CUDA(cudaMemcpyAsync(h.data(), redout.ptr, sizeof(double) * count, cudaMemcpyDeviceToHost, st));
+        SK_CUDA(cudaStreamSynchronize(st));
+        return h;
+    }
+};
+
+DeviceIPM::DeviceIPM(const std::vector<ipm::LpView>& lps, const std::vector<const double*>& bvec,
+                     const std::vector<const double*>& cvec, const sk_options& opt)
+    : im_(new Impl) {
+    auto t0 = std::chrono::steady_clock::now();
+    Impl& I = *im_;
+    I.opt = opt;
+    nlp_ = I.nlp = static_cast<int>(lps.size());
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        throw api::sk_exception(SK_ERR_NO_DEVICE, "no CUDA device visible");
+    SK_CUDA(cudaStreamCreateWithFlags(&I.st, cudaStreamNonBlocking));
+    I.row_off.assign(I.nlp + 1, 0);
+    I.col_off.assign(I.nlp + 1, 0);
+    for (int k = 0; k < I.nlp; ++k) {
+        if (lps[k].m <= 0 || lps[k].n <= 0) throw api::sk_exception(SK_ERR_INVALID, "every LP needs m, n >= 1");
+        I.row_off[k + 1] = I.row_off[k] + lps[k].m;
+        I.col_off[k + 1] = I.col_off[k] + lps[k].n;
+    }
+    I.M = I.row_off[I.nlp];
+    I.N = I.col_off[I.nlp];
+    const int M = I.M, N = I.N;
+    // --- Ruiz scaling per LP (mehrotra_device.cu:289-323) and batch CSC / CSR
+    int64_t nnz = 0;
+    for (auto& l : lps) nnz += l.col_ptrs[l.n];
+    std::vector<int> cp(static_cast<size_t>(N) + 1, 0), ri(static_cast<size_t>(nnz));
+    std::vector<double> cv(static_cast<size_t>(nnz));
+    std::vector<double> hb(M), hc(N);
+    I.R_h.assign(M, 1.0);
+    I.C_h.assign(N, 1.0);
+    I.binf.assign(I.nlp, 0.0);
+    I.cinf.assign(I.nlp, 0.0);
+    {
+        int64_t pos = 0;
+        std::vector<double> rmax, cmax;
+        for (int k = 0; k < I.nlp; ++k) {
+            const auto& l = lps[k];
+            const int ro = I.row_off[k], co = I.col_off[k];
+            const int64_t base = pos;
+            for (int j = 0; j < l.n; ++j) {
+                cp[co + j] = static_cast<int>(pos);
+                for (int q = l.col_ptrs[j]; q < l.col_ptrs[j + 1]; ++q) {
+                    if (l.row_idx[q] < 0 || l.row_idx[q] >= l.m)
+                        throw api::sk_exception(SK_ERR_INVALID, "row index out of range");
+                    ri[pos] = ro + l.row_idx[q];
+                    cv[pos] = l.vals[q];
+                    ++pos;
+                }
+            }
+            for (int i = 0; i < l.m; ++i) { hb[ro + i] = bvec[k][i]; I.binf[k] = std::max(I.binf[k], std::fabs(bvec[k][i])); }
+            for (int j = 0; j < l.n; ++j) { hc[co + j] = cvec[k][j]; I.cinf[k] = std::max(I.cinf[k], std::fabs(cvec[k][j])); }
+            for (int pass = 0; pass < opt.ruiz_passes; ++pass) {
+                rmax.assign(l.m, 0.0);
+                cmax.assign(l.n, 0.0);
+                for (int j = 0; j < l.n; ++j)
+                    for (int64_t q = cp[co + j]; q < (j + 1 < l.n ? cp[co + j + 1] : pos); ++q) {
+                        const double a = std::fabs(cv[q]);
+                        rmax[ri[q] - ro] = std::max(rmax[ri[q] - ro], a);
+                        cmax[j] = std::max(cmax[j], a);
+                    }
+                for (int i = 0; i < l.m; ++i) {
+                    const double f = rmax[i] > 1e-8 ? 1.0 / std::sqrt(rmax[i]) : 1.0;
+                    I.R_h[ro + i] *= f; hb[ro + i] *= f; rmax[i] = f;
+                }
+                for (int j = 0; j < l.n; ++j) {
+                    const double f = cmax[j] > 1e-8 ? 1.0 / std::sqrt(cmax[j]) : 1.0;
+                    I.C_h[co + j] *= f; hc[co + j] *= f; cmax[j] = f;
+                }
+                for (int j = 0; j < l.n; ++j)
+                    for (int64_t q = cp[co + j]; q < (j + 1 < l.n ? cp[co + j + 1] : pos); ++q)
+                        cv[q] *= rmax[ri[q] - ro] * cmax[j];
+            }
+            (void)base;
+        }
+        cp[N] = static_cast<int>(pos);
+    }
+    for (double v : hb) if (!std::isfinite(v)) throw api::sk_exception(SK_ERR_INVALID, "non-finite b");
+    for (double v : hc) if (!std::isfinite(v)) throw api::sk_exception(SK_ERR_INVALID, "non-finite c");
+    for (double v : cv) if (!std::isfinite(v)) throw api::sk_exception(SK_ERR_INVALID, "non-finite A");
+    // batch CSR
+    core::CSRMatrix A;
+    A.rows = M;
+    A.cols = N;
+    A.row_ptrs.assign(static_cast<size_t>(M) + 1, 0);
+    for (int64_t q = 0; q < nnz; ++q) A.row_ptrs[ri[q] + 1]++;
+    for (int i = 0; i < M; ++i) A.row_ptrs[i + 1] += A.row_ptrs[i];
+    A.col_indices.resize(static_cast<size_t>(nnz));
+    A.values.resize(static_cast<size_t>(nnz));
+    {
+        std::vector<int> nx(A.row_ptrs.begin(), A.row_ptrs.end() - 1);
+        for (int j = 0; j < N; ++j)
+            for (int q = cp[j]; q < cp[j + 1]; ++q) {
+                const int d = nx[ri[q]]++;
+                A.col_indices[d] = j;
+                A.values[d] = cv[q];
+            }
+    }
+    // --- symbolic plan on the scaled batch
+    std::vector<ipm::LpView> sl(I.nlp);
+    std::vector<std::vector<int>> lcp(I.nlp), lri(I.nlp);
+    for (int k = 0; k < I.nlp; ++k) {
+        const int co = I.col_off[k], ro = I.row_off[k];
+        lcp[k].resize(lps[k].n + 1);
+        for (int j = 0; j <= lps[k].n; ++j) lcp[k][j] = cp[co + j] - cp[co];
+        lri[k].resize(lcp[k].back());
+        for (int q = 0; q < lcp[k].back(); ++q) lri[k][q] = ri[cp[co] + q] - ro;
+        sl[k].m = lps[k].m;
+        sl[k].n = lps[k].n;
+        sl[k].col_ptrs = lcp[k].data();
+        sl[k].row_idx = lri[k].data();
+        sl[k].vals = cv.data() + cp[co];
+    }
+    ipm::FrontPlan plan;
+    ipm::build_front_plan(sl, A, opt.ordering, plan);
+    lcp.clear();
+    lri.clear();
+    // --- device upload
+    std::vector<int> h_row_lp(M), h_col_lp(N);
+    for (int k = 0; k < I.nlp; ++k) {
+        for (int i = I.row_off[k]; i < I.row_off[k + 1]; ++i) h_row_lp[i] = k;
+        for (int j = I.col_off[k]; j < I.col_off[k + 1]; ++j) h_col_lp[j] = k;
+    }
+    std::vector<int> ms, me, mp, ns_, ne, np_;
+    make_chunks(I.row_off, kChunk, ms, me, mp);
+    make_chunks(I.col_off, kChunk, ns_, ne, np_);
+    I.max_chunks = static_cast<int>(std::max(ms.size(), ns_.size()));
+    Arena& ar = I.arena;
+    reserve(ar, I.a_rp, M + 1); reserve(ar, I.a_ci, nnz); reserve(ar, I.a_v, nnz);
+    reserve(ar, I.t_rp, N + 1); reserve(ar, I.t_ci, nnz); reserve(ar, I.t_v, nnz);
+    reserve(ar, I.b, M); reserve(ar, I.c, N); reserve(ar, I.R, M); reserve(ar, I.C, N);
+    reserve(ar, I.row_lp, M); reserve(ar, I.col_lp, N);
+    reserve(ar, I.mc_s, ms.size()); reserve(ar, I.mc_e, me.size()); reserve(ar, I.mc_p, mp.size());
+    reserve(ar, I.nc_s, ns_.size()); reserve(ar, I.nc_e, ne.size()); reserve(ar, I.nc_p, np_.size());
+    for (auto* sl2 : {&I.x, &I.s, &I.rd, &I.theta, &I.rxs, &I.v, &I.dx, &I.ds, &I.dxa, &I.dsa, &I.e2, &I.e3, &I.xt,
+                      &I.stt, &I.rdt, &I.cdx, &I.cds, &I.crxs})
+        reserve(ar, *sl2, N);
+    for (auto* sl2 : {&I.y, &I.rp, &I.rkkt, &I.dy, &I.dya, &I.e1, &I.yt, &I.rpt, &I.r, &I.corr, &I.bak, &I.tm, &I.cdy})
+        reserve(ar, *sl2, M);
+    reserve(ar, I.scal, static_cast<size_t>(8) * I.nlp);
+    reserve(ar, I.partial, static_cast<size_t>(I.max_chunks) * kMaxR);
+    reserve(ar, I.redout, static_cast<size_t>(I.nlp) * 2 * kMaxR);
+    ar.commit();
+    for (auto* sl2 : {&I.a_rp, &I.a_ci, &I.t_rp, &I.t_ci, &I.row_lp, &I.col_lp, &I.mc_s, &I.mc_e, &I.mc_p, &I.nc_s,
+                      &I.nc_e, &I.nc_p})
+        bind(ar, *sl2);
+    for (auto* sl2 : {&I.a_v, &I.t_v, &I.b, &I.c, &I.R, &I.C, &I.x, &I.s, &I.rd, &I.theta, &I.rxs, &I.v, &I.dx, &I.ds,
+                      &I.dxa, &I.dsa, &I.e2, &I.e3, &I.xt, &I.stt, &I.rdt, &I.cdx, &I.cds, &I.crxs, &I.y, &I.rp,
+                      &I.rkkt, &I.dy, &I.dya, &I.e1, &I.yt, &I.rpt, &I.r, &I.corr, &I.bak, &I.tm, &I.cdy, &I.scal,
+                      &I.partial, &I.redout})
+        bind(ar, *sl2);
+    upload(I.a_rp, A.row_ptrs, I.st); upload(I.a_ci, A.col_indices, I.st); upload(I.a_v, A.values, I.st);
+    upload(I.t_rp, cp, I.st); upload(I.t_ci, ri, I.st); upload(I.t_v, cv, I.st);
+    upload(I.b, hb, I.st); upload(I.c, hc, I.st); upload(I.R, I.R_h, I.st); upload(I.C, I.C_h, I.st);
+    upload(I.row_lp, h_row_lp, I.st); upload(I.col_lp, h_col_lp, I.st);
+    upload(I.mc_s, ms, I.st); upload(I.mc_e, me, I.st); upload(I.mc_p, mp, I.st);
+    upload(I.nc_s, ns_, I.st); upload(I.nc_e, ne, I.st); upload(I.nc_p, np_, I.st);
+    I.ga = pick_group(nnz, M);
+    I.gt = pick_group(nnz, N);
+    lp_.nlp = I.nlp; lp_.M = M; lp_.N = N; lp_.nnz = nnz;
+    lp_.a_rp = I.a_rp.ptr; lp_.a_ci = I.a_ci.ptr; lp_.a_v = I.a_v.ptr;
+    lp_.t_rp = I.t_rp.ptr; lp_.t_ci = I.t_ci.ptr; lp_.t_v = I.t_v.ptr;
+    lp_.b = I.b.ptr; lp_.c = I.c.ptr; lp_.R = I.R.ptr; lp_.C = I.C.ptr;
+    lp_.row_lp = I.row_lp.ptr; lp_.col_lp = I.col_lp.ptr;
+    lp_.n_mchunks = static_cast<int>(ms.size()); lp_.n_nchunks = static_cast<int>(ns_.size());
+    lp_.mc_start = I.mc_s.ptr; lp_.mc_end = I.mc_e.ptr; lp_.mc_ptr = I.mc_p.ptr;
+    lp_.nc_start = I.nc_s.ptr; lp_.nc_end = I.nc_e.ptr; lp_.nc_ptr = I.nc_p.ptr;
+    lp_.spmv_group_A = I.ga; lp_.spmv_group_T = I.gt;
+    kkt_.reset(new KktEngine(plan, lp_, I.st));
+    SK_CUDA(cudaStreamSynchronize(I.st));
+    I.res.assign(I.nlp, LpResult());
+    I.user_start.assign(I.nlp, 0);
+    setup_ms_ = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+void DeviceIPM::profile(bool fp32, double* out16) {
+    Impl& I = *im_;
+    std::vector<double> ones(I.nlp, 1.0);
+    I.put_scalars(0, ones);
+    k_theta<<<nblk(I.N), 256, 0, I.st>>>(I.N, I.x.ptr, I.s.ptr, I.col_lp.ptr, I.sc(0), I.theta.ptr);
+    k_fill<<<nblk(I.M), 256, 0, I.st>>>(I.M, I.r.ptr, 1.0);
+    kkt_->profile(I.theta.ptr, fp32 ? 1e-7 : 1e-9, fp32, I.r.ptr, I.corr.ptr, out16);
+}
+
+DeviceIPM::~DeviceIPM() {
+    if (im_ && im_->ev0) { cudaEventDestroy(im_->ev0); cudaEventDestroy(im_->ev1); }
+    kkt_.reset();
+    if (im_ && im_->st) cudaStreamDestroy(im_->st);
+}
+
+void DeviceIPM::set_start(int lp, const double* x, const double* y, const double* s) {
+    Impl& I = *im_;
+    if (lp < 0 || lp >= I.nlp || !x || !y || !s) throw api::sk_exception(SK_ERR_INVALID, "set_start: bad argument");
+    if (I.hx0.empty()) { I.hx0.assign(I.N, 1.0); I.hy0.assign(I.M, 0.0); I.hs0.assign(I.N, 1.0); }
+    const int ro = I.row_off[lp], co = I.col_off[lp];
+    for (int j = 0; j < I.col_off[lp + 1] - co; ++j) {
+        I.hx0[co + j] = x[j] / I.C_h[co + j];       // x_scaled = C^{-1} x
+        I.hs0[co + j] = s[j] * I.C_h[co + j];       // s_scaled = C s
+    }
+    for (int i = 0; i < I.row_off[lp + 1] - ro; ++i) I.hy0[ro + i] = y[i] / I.R_h[ro + i];
+    I.user_start[lp] = 1;
+}
+
+void DeviceIPM::run() {
+    Impl& I = *im_;
+    KktEngine& K = *kkt_;
+    const int M = I.M, N = I.N, nlp = I.nlp;
+    cudaStream_t st = I.st;
+    auto t0 = std::chrono::steady_clock::now();
+    if (!I.ev0) {
+        SK_CUDA(cudaEventCreate(&I.ev0));
+        SK_CUDA(cudaEventCreate(&I.ev1));
+    }
+    SK_CUDA(cudaEventRecord(I.ev0, st));
+    const auto& o = I.opt;
+    I.factorizations = I.solves = I.refine_steps = 0;
+    I.switched = false;
+    I.used_fp32 = false;
+    I.res.assign(nlp, LpResult());
+    I.active.assign(nlp, 1);
+    I.rp0.assign(nlp, 1.0);
+    I.rd0.assign(nlp, 1.0);
+    I.mu0.assign(nlp, 1.0);
+    // start point
+    k_fill<<<nblk(N), 256, 0, st>>>(N, I.x.ptr, 1.0);
+    k_fill<<<nblk(N), 256, 0, st>>>(N, I.s.ptr, 1.0);
+    k_fill<<<nblk(M), 256, 0, st>>>(M, I.y.ptr, 0.0);
+    if (o.start == SK_START_USER && !I.hx0.empty()) {
+        SK_CUDA(cudaMemcpyAsync(I.x.ptr, I.hx0.data(), sizeof(double) * N, cudaMemcpyHostToDevice, st));
+        SK_CUDA(cudaMemcpyAsync(I.y.ptr, I.hy0.data(), sizeof(double) * M, cudaMemcpyHostToDevice, st));
+        SK_CUDA(cudaMemcpyAsync(I.s.ptr, I.hs0.data(), sizeof(double) * N, cudaMemcpyHostToDevice, st));
+        for (int k = 0; k < nlp; ++k) I.res[k].learned_start = I.user_start[k];
+    }
+    std::vector<double> nrp(nlp), nrd(nlp), mu(nlp), nm(nlp), nn(nlp);
+    for (int k = 0; k < nlp; ++k) {
+        nm[k] = I.row_off[k + 1] - I.row_off[k];
+        nn[k] = I.col_off[k + 1] - I.col_off[k];
+    }
+    std::vector<double> mask(nlp), ap(nlp), ad(nlp), tgt(nlp), tol(nlp);
+    double* d_mask = I.sc(0);
+    double* d_ap = I.sc(1);
+    double* d_ad = I.sc(2);
+    double* d_tgt = I.sc(3);
+    double* d_rmask = I.sc(4);
+
+    auto residuals = [&](const double* x, const double* y, const double* s, double* rp, double* rd) {
+        spmv(M, I.ga, I.a_rp.ptr, I.a_ci.ptr, I.a_v.ptr, x, EpiSub{I.b.ptr, rp}, st);
+        spmv(N, I.gt, I.t_rp.ptr, I.t_ci.ptr, I.t_v.ptr, y, EpiRd{s, I.c.ptr, rd}, st);
+    };
+    // unscaled measures of LP k from the residual reductions
+    auto record = [&](int k, const double* hm, const double* hn) {
+        LpResult& r = I.res[k];
+        r.primal_residual = std::sqrt(hm[k * 3 + 0]);
+        r.dual_residual = std::sqrt(hn[k * 4 + 0]);
+        r.duality_gap = hn[k * 4 + 2] / nn[k];
+        r.objective = hn[k * 4 + 3];
+        const double by = hm[k * 3 + 2];
+        r.rel_pinf = hm[k * 3 + 1] / (1.0 + I.binf[k]);
+        r.rel_dinf = hn[k * 4 + 1] / (1.0 + I.cinf[k]);
+        r.rel_gap = std::fabs(r.objective - by) / (1.0 + std::fabs(r.objective) + std::fabs(by));
+    };
+    // ---- normal-equation solve with iterative refinement; returns per-LP success
+    auto solve = [&](const double* rhs, double* out, std::vector<char>& ok) {
+        ++I.solves;
+        const int max_ir = K.last_fp32() ? 30 : 10;
+        K.apply_inverse(rhs, out);
+        auto resid = [&](const double* xx) {
+            spmv(N, I.gt, I.t_rp.ptr, I.t_ci.ptr, I.t_v.ptr, xx, EpiTheta{I.theta.ptr, K.scratch_n()}, st);
+            spmv(M, I.ga, I.a_rp.ptr, I.a_ci.ptr, I.a_v.ptr, K.scratch_n(), EpiRhsMinus{rhs, I.r.ptr}, st);
+            I.reduce_rows<1>(RedAbsMax{I.r.ptr}, I.redout.ptr);
+            return I.fetch(nlp);
+        };
+        std::vector<double> rn = resid(out);
+        std::vector<char> done(nlp, 0), stag(nlp, 0);
+        for (int k = 0; k < nlp; ++k) done[k] = !I.active[k] || rn[k] <= tol[k];
+        for (int it = 0; it < max_ir; ++it) {
+            bool any = false;
+            std::vector<double> rm(nlp);
+            for (int k = 0; k < nlp; ++k) { rm[k] = (!done[k] && !stag[k]) ? 1.0 : 0.0; any |= rm[k] != 0.0; }
+            if (!any) break;
+            ++I.refine_steps;
+            I.put_scalars(4, rm);
+            SK_CUDA(cudaMemcpyAsync(I.bak.ptr, out, sizeof(double) * M, cudaMemcpyDeviceToDevice, st));
+            K.apply_inverse(I.r.ptr, I.corr.ptr);
+            k_masked_add<<<nblk(M), 256, 0, st>>>(M, I.corr.ptr, I.row_lp.ptr, d_rmask, out);
+            std::vector<double> rn2 = resid(out);
+            std::vector<double> roll(nlp, 0.0);
+            bool any_roll = false;
+            for (int k = 0; k < nlp; ++k) {
+                if (rm[k] == 0.0) continue;
+                if (rn2[k] <= tol[k]) { done[k] = 1; rn[k] = rn2[k]; }
+                else if (rn2[k] >= rn[k]) { stag[k] = 1; roll[k] = 1.0; any_roll = true; }
+                else rn[k] = rn2[k];
+            }
+            if (any_roll) {
+                I.put_scalars(4, roll);
+                k_masked_copy<<<nblk(M), 256, 0, st>>>(M, I.bak.ptr, I.row_lp.ptr, d_rmask, out);
+            }
+        }
+        ok.assign(nlp, 0);
+        for (int k = 0; k < nlp; ++k) ok[k] = !I.active[k] || rn[k] <= tol[k];
+    };
+    // ---- factorisation with delta retries and the precision policy
+    auto factor = [&](bool want_fp32) -> bool {
+        double delta = want_fp32 ? 1e-7 : 1e-9;
+        for (int retry = 0; retry < 5; ++retry, delta *= 10.0) {
+            ++I.factorizations;
+            if (K.factor(I.theta.ptr, delta, want_fp32)) {
+                if (want_fp32) I.used_fp32 = true;
+                return true;
+            }
+        }
+        return false;
+    };
+    // ---- direction: solve for rkkt -> (dx, dy, ds) and verify; returns per LP validity
+    struct DirStats { std::vector<double> e1, e2, e3, rxs, rx, rs, xs, xds, dxs, dxds; };
+    auto direction = [&](double* dxo, double* dyo, double* dso, const double* rxs, std::vector<char>& ok,
+                         DirStats& ds_) {
+        spmv(M, I.ga, I.a_rp.ptr, I.a_ci.ptr, I.a_v.ptr, I.v.ptr, EpiSub{I.rp.ptr, I.rkkt.ptr}, st);
+        solve(I.rkkt.ptr, dyo, ok);
+        spmv(N, I.gt, I.t_rp.ptr, I.t_ci.ptr, I.t_v.ptr, dyo,
+             EpiDsDx{I.rd.ptr, I.theta.ptr, rxs, I.x.ptr, I.s.ptr, dso, dxo, I.e2.ptr, I.e3.ptr}, st);
+        spmv(M, I.ga, I.a_rp.ptr, I.a_ci.ptr, I.a_v.ptr, dxo, EpiAdd{I.rp.ptr, I.e1.ptr}, st);
+        I.reduce_rows<1>(RedSq{I.e1.ptr}, I.redout.ptr);
+        I.reduce_cols<9>(RedDir{I.e2.ptr, I.e3.ptr, rxs, I.x.ptr, I.s.ptr, dxo, dso}, I.redout.ptr + nlp);
+        std::vector<double> h = I.fetch(static_cast<size_t>(nlp) * 10);
+        ds_ = DirStats();
+        for (int k = 0; k < nlp; ++k) {
+            const double* q = h.data() + nlp + k * 9;
+            ds_.e1.push_back(std::sqrt(h[k]) / std::max(1.0, nrp[k]));
+            ds_.e2.push_back(std::sqrt(q[0]) / std::max(1.0, nrd[k]));
+            ds_.e3.push_back(std::sqrt(q[1]) / std::max(1.0, std::sqrt(q[2])));
+            ds_.rx.push_back(q[3]);
+            ds_.rs.push_back(q[4]);
+            ds_.xs.push_back(q[5]);
+            ds_.xds.push_back(q[6]);
+            ds_.dxs.push_back(q[7]);
+            ds_.dxds.push_back(q[8]);
+        }
+        std::vector<char> valid(nlp, 0);
+        for (int k = 0; k < nlp; ++k)
+            valid[k] = ok[k] && !(ds_.e1[k] > 1e-8 || ds_.e2[k] > 1e-8 || ds_.e3[k] > 1e-8);
+        ok = valid;
+    };
+
+    int iter = 0;
+    std::vector<double> hm, hn;
+    for (iter = 0; iter < o.max_iter; ++iter) {
+        residuals(I.x.ptr, I.y.ptr, I.s.ptr, I.rp.ptr, I.rd.ptr);
+        I.reduce_rows<3>(RedResidM{I.rp.ptr, I.R.ptr, I.b.ptr, I.y.ptr}, I.redout.ptr);
+        I.reduce_cols<4>(RedResidN{I.rd.ptr, I.C.ptr, I.x.ptr, I.s.ptr, I.c.ptr}, I.redout.ptr + nlp * 3);
+        std::vector<double> h = I.fetch(static_cast<size_t>(nlp) * 7);
+        hm.assign(h.begin(), h.begin() + nlp * 3);
+        hn.assign(h.begin() + nlp * 3, h.end());
+        bool any = false;
+        double mumax = 0.0;
+        for (int k = 0; k < nlp; ++k) {
+            if (!I.active[k]) continue;
+            nrp[k] = std::sqrt(hm[k * 3]);
+            nrd[k] = std::sqrt(hn[k * 4]);
+            mu[k] = hn[k * 4 + 2] / nn[k];
+            if (iter == 0) {
+                I.rp0[k] = std::max(1.0, nrp[k]);
+                I.rd0[k] = std::max(1.0, nrd[k]);
+                I.mu0[k] = std::max(1.0, mu[k]);
+            }
+            record(k, hm.data(), hn.data());
+            LpResult& r = I.res[k];
+            r.iterations = iter;
+            bool conv;
+            if (o.criteria == SK_CRIT_REFERENCE) conv = nrp[k] < 1e-6 && nrd[k] < 1e-6 && mu[k] < 1e-6;
+            else conv = r.rel_pinf <= o.tol && r.rel_dinf <= o.tol && r.rel_gap <= o.tol;
+            if (o.verbose)
+                std::fprintf(stderr, "[sk] lp %d iter %d rp %.3e rd %.3e mu %.3e gap %.3e %s\n", k, iter, nrp[k],
+                             nrd[k], mu[k], r.rel_gap, I.switched || o.precision == SK_PREC_FP64 ? "fp64" : "fp32");
+            if (conv) { r.status = SK_STATUS_OPTIMAL; I.active[k] = 0; continue; }
+            any = true;
+            mumax = std::max(mumax, mu[k]);
+        }
+        if (!any) break;
+        for (int k = 0; k < nlp; ++k) mask[k] = I.active[k] ? 1.0 : 0.0;
+        I.put_scalars(0, mask);
+        k_theta<<<nblk(N), 256, 0, st>>>(N, I.x.ptr, I.s.ptr, I.col_lp.ptr, d_mask, I.theta.ptr);
+        // precision for this iteration
+        bool fp32 = o.precision == SK_PREC_MIXED && !I.switched && mumax >= o.mu_switch;
+        if (o.precision == SK_PREC_MIXED && !I.switched && !fp32) {
+            I.switched = true;
+            for (int k = 0; k < nlp; ++k) if (I.active[k]) I.res[k].switch_iteration = iter;
+        }
+        bool ok_fac = factor(fp32);
+        if (!ok_fac && fp32) {
+            I.switched = true;
+            for (int k = 0; k < nlp; ++k) if (I.active[k]) I.res[k].switch_iteration = iter;
+            fp32 = false;
+            ok_fac = factor(false);
+        }
+        if (!ok_fac) {   // the reference throws here (kkt.cu:600-602); report a numerical stop
+            for (int k = 0; k < nlp; ++k) if (I.active[k]) { I.res[k].status = SK_STATUS_ITERATION_LIMIT; I.active[k] = 0; }
+            break;
+        }
+        for (int k = 0; k < nlp; ++k) tol[k] = 1e-9 * std::max(1.0, nrp[k]);
+        // ---------------- predictor
+        DirStats pd;
+        std::vector<char> okp;
+        for (int attempt = 0; attempt < 2; ++attempt) {
+            k_rhs<<<nblk(N), 256, 0, st>>>(N, I.x.ptr, I.s.ptr, I.theta.ptr, I.rd.ptr, nullptr, nullptr, nullptr,
+                                          I.col_lp.ptr, I.rxs.ptr, I.v.ptr);
+            direction(I.dxa.ptr, I.dya.ptr, I.dsa.ptr, I.rxs.ptr, okp, pd);
+            bool all_ok = true;
+            for (int k = 0; k < nlp; ++k) if (I.active[k] && !okp[k]) all_ok = false;
+            if (all_ok || !fp32) break;
+            // an FP32 solve missed its tolerance: switch to FP64 for the rest of the solve
+            I.switched = true;
+            for (int k = 0; k < nlp; ++k) if (I.active[k]) I.res[k].switch_iteration = iter;
+            fp32 = false;
+            if (!factor(false)) break;
+        }
+        std::vector<double> sigmu(nlp, 0.0);
+        for (int k = 0; k < nlp; ++k) {
+            if (!I.active[k]) continue;
+            if (!okp[k]) { I.res[k].status = SK_STATUS_ITERATION_LIMIT; I.active[k] = 0; continue; }
+            const double apa = std::min(1.0, pd.rx[k]), ada = std::min(1.0, pd.rs[k]);
+            const double mua = (pd.xs[k] + ada * pd.xds[k] + apa * pd.dxs[k] + apa * ada * pd.dxds[k]) / nn[k];
+            const double sigma = std::min(1.0, std::pow(std::max(0.0, mua) / std::max(1e-16, mu[k]), 3.0));
+            sigmu[k] = sigma * mu[k];
+        }
+        // ---------------- corrector
+        I.put_scalars(3, sigmu);
+        k_rhs<<<nblk(N), 256, 0, st>>>(N, I.x.ptr, I.s.ptr, I.theta.ptr, I.rd.ptr, I.dxa.ptr, I.dsa.ptr, d_tgt,
+                                      I.col_lp.ptr, I.rxs.ptr, I.v.ptr);
+        DirStats cd;
+        std::vector<char> okc;
+        direction(I.dx.ptr, I.dy.ptr, I.ds.ptr, I.rxs.ptr, okc, cd);
+        const double eta = 0.995, armijo = 1e-4;
+        std::vector<int> dir(nlp, 0), bt(nlp, 0);
+        std::vector<char> decided(nlp, 1), accepted(nlp, 0);
+        std::vector<double> merit0(nlp, 0.0);
+        bool need_centred = false;
+        for (int k = 0; k < nlp; ++k) {
+            if (!I.active[k]) continue;
+            decided[k] = 0;
+            merit0[k] = nrp[k] / I.rp0[k] + nrd[k] / I.rd0[k] + mu[k] / I.mu0[k];
+            dir[k] = okc[k] ? 0 : 1;
+            ap[k] = std::min(1.0, eta * cd.rx[k]);
+            ad[k] = std::min(1.0, eta * cd.rs[k]);
+            if (dir[k] == 1) need_centred = true;
+        }
+        auto centred = [&]() {
+            // centred safeguard direction sigma_c = 1/2 for the LPs in direction 1
+            std::vector<double> half(nlp, 0.0), cm(nlp, 0.0);
+            for (int k = 0; k < nlp; ++k) {
+                half[k] = 0.5 * mu[k];
+                cm[k] = (!decided[k] && dir[k] == 1) ? 1.0 : 0.0;
+            }
+            I.put_scalars(3, half);
+            k_rhs<<<nblk(N), 256, 0, st>>>(N, I.x.ptr, I.s.ptr, I.theta.ptr, I.rd.ptr, nullptr, nullptr, d_tgt,
+                                          I.col_lp.ptr, I.crxs.ptr, I.v.ptr);
+            DirStats cs;
+            std::vector<char> okz;
+            direction(I.cdx.ptr, I.cdy.ptr, I.cds.ptr, I.crxs.ptr, okz, cs);
+            I.put_scalars(4, cm);
+            k_masked_copy<<<nblk(N), 256, 0, st>>>(N, I.cdx.ptr, I.col_lp.ptr, d_rmask, I.dx.ptr);
+            k_masked_copy<<<nblk(N), 256, 0, st>>>(N, I.cds.ptr, I.col_lp.ptr, d_rmask, I.ds.ptr);
+            k_masked_copy<<<nblk(M), 256, 0, st>>>(M, I.cdy.ptr, I.row_lp.ptr, d_rmask, I.dy.ptr);
+            for (int k = 0; k < nlp; ++k) {
+                if (cm[k] == 0.0) continue;
+                if (!okz[k]) { decided[k] = 1; continue; }   // failed safeguard solve: no step
+                const double bnd = std::min(cs.rx[k], cs.rs[k]);
+                ap[k] = ad[k] = std::min(1.0, eta * bnd);
+                bt[k] = 0;
+            }
+        };
+        if (need_centred) centred();
+        for (int round = 0; round < 64; ++round) {
+            bool pending = false;
+            for (int k = 0; k < nlp; ++k) pending |= !decided[k];
+            if (!pending) break;
+            std::vector<double> tap(nlp, 0.0), tad(nlp, 0.0);
+            for (int k = 0; k < nlp; ++k) if (!decided[k]) { tap[k] = ap[k]; tad[k] = ad[k]; }
+            I.put_scalars(1, tap);
+            I.put_scalars(2, tad);
+            k_trial_n<<<nblk(N), 256, 0, st>>>(N, I.x.ptr, I.s.ptr, I.dx.ptr, I.ds.ptr, d_ap, d_ad, I.col_lp.ptr,
+                                              I.xt.ptr, I.stt.ptr);
+            k_trial_m<<<nblk(M), 256, 0, st>>>(M, I.y.ptr, I.dy.ptr, d_ad, I.row_lp.ptr, I.yt.ptr);
+            residuals(I.xt.ptr, I.yt.ptr, I.stt.ptr, I.rpt.ptr, I.rdt.ptr);
+            I.reduce_rows<2>(RedTrialM{I.rpt.ptr, I.yt.ptr}, I.redout.ptr);
+            I.reduce_cols<4>(RedTrialN{I.rdt.ptr, I.xt.ptr, I.stt.ptr}, I.redout.ptr + nlp * 2);
+            std::vector<double> h = I.fetch(static_cast<size_t>(nlp) * 6);
+            bool want_centred = false;
+            for (int k = 0; k < nlp; ++k) {
+                if (decided[k]) continue;
+                const double rpn = std::sqrt(h[k * 2]), yn = std::sqrt(h[k * 2 + 1]);
+                const double* q = h.data() + nlp * 2 + k * 4;
+                const double rdn = std::sqrt(q[0]), mun = q[1] / nn[k], minx = q[2], mins = q[3];
+                const double merit = rpn / I.rp0[k] + rdn / I.rd0[k] + mun / I.mu0[k];
+                const double stp = std::min(ap[k], ad[k]);
+                const bool finite = std::isfinite(rpn) && std::isfinite(rdn) && std::isfinite(mun) &&
+                                    std::isfinite(merit) && std::isfinite(merit0[k]) && std::isfinite(minx) &&
+                                    std::isfinite(mins) && std::isfinite(ap[k]) && std::isfinite(ad[k]) &&
+                                    std::isfinite(yn);
+                const bool positive = minx > 0.0 && mins > 0.0 && mun > 0.0 && stp > 0.0;
+                const bool progress = merit < merit0[k] && merit <= (1.0 - armijo * stp) * merit0[k];
+                if (finite && positive && progress) { decided[k] = 1; accepted[k] = 1; continue; }
+                ap[k] *= 0.5;
+                ad[k] *= 0.5;
+                ++bt[k];
+                if (bt[k] >= (dir[k] == 0 ? 15 : 30)) {
+                    if (dir[k] == 0) { dir[k] = 1; want_centred = true; }
+                    else decided[k] = 1;
+                }
+            }
+            if (want_centred) centred();
+        }
+        std::vector<double> acc(nlp, 0.0);
+        for (int k = 0; k < nlp; ++k) acc[k] = accepted[k] ? 1.0 : 0.0;
+        I.put_scalars(4, acc);
+        // re-evaluate the accepted trials (the last trial buffers hold only the
+        // final round's points) and commit them
+        {
+            std::vector<double> tap(nlp, 0.0), tad(nlp, 0.0);
+            for (int k = 0; k < nlp; ++k) if (accepted[k]) { tap[k] = ap[k]; tad[k] = ad[k]; }
+            I.put_scalars(1, tap);
+            I.put_scalars(2, tad);
+            k_trial_n<<<nblk(N), 256, 0, st>>>(N, I.x.ptr, I.s.ptr, I.dx.ptr, I.ds.ptr, d_ap, d_ad, I.col_lp.ptr,
+                                              I.xt.ptr, I.stt.ptr);
+            k_trial_m<<<nblk(M), 256, 0, st>>>(M, I.y.ptr, I.dy.ptr, d_ad, I.row_lp.ptr, I.yt.ptr);
+            k_masked_copy<<<nblk(N), 256, 0, st>>>(N, I.xt.ptr, I.col_lp.ptr, d_rmask, I.x.ptr);
+            k_masked_copy<<<nblk(N), 256, 0, st>>>(N, I.stt.ptr, I.col_lp.ptr, d_rmask, I.s.ptr);
+            k_masked_copy<<<nblk(M), 256, 0, st>>>(M, I.yt.ptr, I.row_lp.ptr, d_rmask, I.y.ptr);
+        }
+        for (int k = 0; k < nlp; ++k)
+            if (I.active[k] && !accepted[k]) { I.res[k].status = SK_STATUS_ITERATION_LIMIT; I.active[k] = 0; }
+    }
+    // LPs still running at the iteration cap: final residuals (mehrotra_device.cu:1026-1035)
+    bool any_left = false;
+    for (int k = 0; k < nlp; ++k) any_left |= I.active[k] != 0;
+    residuals(I.x.ptr, I.y.ptr, I.s.ptr, I.rp.ptr, I.rd.ptr);
+    I.reduce_rows<3>(RedResidM{I.rp.ptr, I.R.ptr, I.b.ptr, I.y.ptr}, I.redout.ptr);
+    I.reduce_cols<4>(RedResidN{I.rd.ptr, I.C.ptr, I.x.ptr, I.s.ptr, I.c.ptr}, I.redout.ptr + nlp * 3);
+    std::vector<double> h = I.fetch(static_cast<size_t>(nlp) * 7);
+    for (int k = 0; k < nlp; ++k) {
+        if (I.res[k].status == SK_STATUS_OPTIMAL) continue;
+        record(k, h.data(), h.data() + nlp * 3);
+        if (I.active[k]) I.res[k].iterations = o.max_iter;
+        I.res[k].status = SK_STATUS_ITERATION_LIMIT;
+    }
+    (void)any_left;
+    I.precision_path = o.precision == SK_PREC_FP64 ? 0 : (I.switched ? (I.used_fp32 ? 2 : 0) : 1);
+    SK_CUDA(cudaEventRecord(I.ev1, st));
+    SK_CUDA(cudaStreamSynchronize(st));
+    {
+        float ms = 0.f;
+        SK_CUDA(cudaEventElapsedTime(&ms, I.ev0, I.ev1));
+        I.device_ms = ms;
+    }
+    I.solve_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+void DeviceIPM::result(int lp, double* x, double* y, double* s, sk_info* info) const {
+    const Impl& I = *im_;
+    if (lp < 0 || lp >= I.nlp) throw api::sk_exception(SK_ERR_INVALID, "result: lp out of range");
+    const int ro = I.row_off[lp], co = I.col_off[lp];
+    const int m = I.row_off[lp + 1] - ro, n = I.col_off[lp + 1] - co;
+    std::vector<double> hx(n), hy(m), hs(n);
+    SK_CUDA(cudaMemcpyAsync(hx.data(), I.x.ptr + co, sizeof(double) * n, cudaMemcpyDeviceToHost, I.st));
+    SK_CUDA(cudaMemcpyAsync(hy.data(), I.y.ptr + ro, sizeof(double) * m, cudaMemcpyDeviceToHost, I.st));
+    SK_CUDA(cudaMemcpyAsync(hs.data(), I.s.ptr + co, sizeof(double) * n, cudaMemcpyDeviceToHost, I.st));
+    SK_CUDA(cudaStreamSynchronize(I.st));
+    if (x) for (int j = 0; j < n; ++j) x[j] = hx[j] * I.C_h[co + j];
+    if (y) for (int i = 0; i < m; ++i) y[i] = hy[i] * I.R_h[ro + i];
+    if (s) for (int j = 0; j < n; ++j) s[j] = hs[j] / I.C_h[co + j];
+    if (info) {
+        const LpResult& r = I.res[lp];
+        const auto& p = kkt_->plan();
+        info->status = r.status;
+        info->iterations = r.iterations;
+        info->objective = r.objective;
+        info->primal_residual = r.primal_residual;
+        info->dual_residual = r.dual_residual;
+        info->duality_gap = r.duality_gap;
+        info->rel_pinf = r.rel_pinf;
+        info->rel_dinf = r.rel_dinf;
+        info->rel_gap = r.rel_gap;
+        info->precision_path = I.precision_path;
+        info->switch_iteration = r.switch_iteration;
+        info->factorizations = I.factorizations;
+        info->solves = I.solves;
+        info->refine_steps = I.refine_steps;
+        info->learned_start = r.learned_start;
+        info->setup_ms = setup_ms_;
+        info->solve_ms = I.solve_ms;
+        info->nnz_factor = p.nnz_factor;
+        info->num_supernodes = p.ns;
+        info->dense_front = p.dense_mode ? 1 : 0;
+        info->device_ms = I.device_ms;
+        info->flops_factor = p.flops_factor;
+    }
+}
+
+}  // namespace dev
+}  // namespace sankhya

@@ -1,0 +1,92 @@
+// Device normal-equation engine: assembly of D (A Theta A^T) D + delta I into
+// multifrontal fronts, level-scheduled tiled Cholesky (FP64 or FP32 fronts), and
+// the multifrontal triangular solves. Replaces the reference's
+// gpu::GPUKKTCholeskySolver (src/cuda/kkt.cu:177-870).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <vector>
+
+#include "cuda/dev_common.cuh"
+#include "cuda/device_lp.hpp"
+#include "ipm/front_plan.hpp"
+
+namespace sankhya {
+namespace dev {
+
+class KktEngine {
+public:
+    // The plan is copied into device memory; lp must stay alive.
+    KktEngine(const ipm::FrontPlan& plan, const DeviceLP& lp, cudaStream_t stream);
+    ~KktEngine();
+
+    // Assembles and factors D (A diag(theta) A^T) D + delta I, D = 1/sqrt(max(|m_ii|, 1e-12)),
+    // in FP64 (fp32 = false) or FP32 fronts. Returns true when every pivot was
+    // positive (one host synchronisation).
+    bool factor(const double* d_theta, double delta, bool fp32);
+    // dst = D L^{-T} L^{-1} D src (batch row order), using the last factor. src
+    // and dst may alias. Asynchronous on the engine stream.
+    void apply_inverse(const double* d_src, double* d_dst);
+    // dst = A diag(theta) A^T src (FP64, matrix-free).
+    void apply_normal(const double* d_theta, const double* d_src, double* d_dst);
+
+    // Diagnostics: one factorisation + one solve (of d_rhs) without graphs, with
+    // CUDA events around every launch; fills out[16] as sk_solver_profile documents.
+    void profile(const double* d_theta, double delta, bool fp32, const double* d_rhs, double* d_out, double* out);
+
+    bool last_fp32() const { return fp32_; }
+    int failed_supernode() const { return failed_sn_; }
+    const ipm::FrontPlan& plan() const { return plan_; }
+    double* diag_D() const { return D_.ptr; }
+    // Copies the factored fronts to the host (FP64) for inspection.
+    std::vector<double> fronts_host();
+    cudaStream_t stream() const { return st_; }
+    // Work vectors of length N available to callers between calls.
+    double* scratch_n() const { return tn_.ptr; }
+
+private:
+    void run_factor_levels(bool fp32);
+    void run_solve_levels();
+    struct Prof;
+    template <class T> void launch_factor(T* F, Prof* prof = nullptr);
+    template <class T> void launch_solve(const T* F, Prof* prof = nullptr);
+
+    ipm::FrontPlan plan_;
+    const DeviceLP& lp_;
+    cudaStream_t st_;
+    Arena arena_;
+    Arena f32_arena_, f64_arena_;
+    Slot<float> F32_;
+    Slot<double> F64_;
+    // plan arrays
+    Slot<int> sn_first_, sn_ncols_, sn_nrows_, sn_parent_, rows_, ea_map_, ch_ptr_, ch_list_, perm_;
+    Slot<int64_t> sn_F_off_, sn_f_off_, sn_rows_off_, ea_off_;
+    Slot<int> step_items_, step_prefix_, round_items_, round_prefix_, level_sn_;
+    Slot<int64_t> slot_pos_, w_ptr_;
+    Slot<int> slot_i_, slot_j_, w_col_;
+    Slot<double> w_val_;
+    // numeric work
+    Slot<double> D_, Mdiag_, zp_, xp_, fvec_, partial_, tn_, params_;
+    Slot<int> err_;
+    int64_t max_partial_ = 0;
+    bool fp32_ = false;
+    int failed_sn_ = -1;
+    const double* theta_bound_ = nullptr;
+    cudaGraphExec_t gfac_[2] = {nullptr, nullptr};
+    cudaGraphExec_t gsol_[2] = {nullptr, nullptr};
+    const double* gfac_theta_[2] = {nullptr, nullptr};
+};
+
+}  // namespace dev
+}  // namespace sankhya
+
+namespace sankhya {
+namespace dev {
+// max |a_i| over n entries (synchronises; scratch64 holds 64 doubles).
+double absmax_device(int n, const double* a, double* scratch64, cudaStream_t st);
+void vec_diff(int n, const double* a, const double* b, double* out, cudaStream_t st);   // out = a - b
+void vec_add(int n, const double* a, double* out, cudaStream_t st);                      // out += a
+}  // namespace dev
+}  // namespace sankhya

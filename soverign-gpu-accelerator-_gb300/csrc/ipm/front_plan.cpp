@@ -1,0 +1,506 @@
+// Multifrontal plan construction (see front_plan.hpp).
+#include "ipm/front_plan.hpp"
+
+#include <algorithm>
+#include <numeric>
+#include <stdexcept>
+
+#include "ipm/symbolic.hpp"
+
+namespace sankhya {
+namespace ipm {
+
+bool prefer_dense_front(const LpView& lp) {
+    if (lp.m <= 256) return true;
+    double pairs = 0.0;
+    for (Index j = 0; j < lp.n; ++j) {
+        const double c = lp.col_ptrs[j + 1] - lp.col_ptrs[j];
+        pairs += c * (c - 1.0);
+    }
+    return pairs >= 0.05 * static_cast<double>(lp.m) * (lp.m - 1.0);
+}
+
+namespace {
+
+int64_t tri(int64_t t) { return t * (t + 1) / 2; }
+int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// Postorder of a forest: roots in increasing order, children in increasing order.
+std::vector<Index> postorder(const std::vector<Index>& parent) {
+    const Index m = static_cast<Index>(parent.size());
+    std::vector<Index> head(static_cast<size_t>(m), -1), next(static_cast<size_t>(m), -1);
+    for (Index j = m - 1; j >= 0; --j) {  // push in reverse so lists come out increasing
+        const Index p = parent[j];
+        if (p >= 0) { next[j] = head[p]; head[p] = j; }
+    }
+    std::vector<Index> post;
+    post.reserve(static_cast<size_t>(m));
+    std::vector<Index> stack;
+    std::vector<Index> it(static_cast<size_t>(m), -2);
+    for (Index r = 0; r < m; ++r) {
+        if (parent[r] >= 0) continue;
+        stack.push_back(r);
+        it[r] = head[r];
+        while (!stack.empty()) {
+            const Index v = stack.back();
+            const Index c = it[v];
+            if (c >= 0) {
+                it[v] = next[c];
+                stack.push_back(c);
+                it[c] = head[c];
+            } else {
+                post.push_back(v);
+                stack.pop_back();
+            }
+        }
+    }
+    return post;
+}
+
+}  // namespace
+
+static void build_schedule(FrontPlan& p) {
+    // levels
+    p.sn_level.assign(static_cast<size_t>(p.ns), 0);
+    for (int s = 0; s < p.ns; ++s) {  // children precede parents (postorder)
+        const int par = p.sn_parent[s];
+        if (par >= 0) p.sn_level[par] = std::max(p.sn_level[par], p.sn_level[s] + 1);
+    }
+    p.nlevels = 0;
+    for (int s = 0; s < p.ns; ++s) p.nlevels = std::max(p.nlevels, p.sn_level[s] + 1);
+    p.level_ptr.assign(static_cast<size_t>(p.nlevels) + 1, 0);
+    for (int s = 0; s < p.ns; ++s) p.level_ptr[p.sn_level[s] + 1]++;
+    for (int l = 0; l < p.nlevels; ++l) p.level_ptr[l + 1] += p.level_ptr[l];
+    p.level_sn.assign(static_cast<size_t>(p.ns), 0);
+    {
+        std::vector<int> nx(p.level_ptr.begin(), p.level_ptr.end() - 1);
+        for (int s = 0; s < p.ns; ++s) p.level_sn[nx[p.sn_level[s]]++] = s;
+    }
+    // tile steps
+    p.steps.clear();
+    p.step_items.clear();
+    p.step_prefix.clear();
+    p.step_level_ptr.assign(static_cast<size_t>(p.nlevels) + 1, 0);
+    for (int l = 0; l < p.nlevels; ++l) {
+        int kmax = 0;
+        for (int q = p.level_ptr[l]; q < p.level_ptr[l + 1]; ++q) kmax = std::max(kmax, p.sn_ncols[p.level_sn[q]]);
+        const int nsteps = static_cast<int>(ceil_div(kmax, kTile));
+        for (int k = 0; k < nsteps; ++k) {
+            PlanStep st;
+            st.level = l;
+            st.k = k;
+            st.item_off = static_cast<int>(p.step_items.size());
+            std::vector<int> items;
+            for (int q = p.level_ptr[l]; q < p.level_ptr[l + 1]; ++q) {
+                const int s = p.level_sn[q];
+                if (p.sn_ncols[s] > k * kTile) items.push_back(s);
+            }
+            st.nitems = static_cast<int>(items.size());
+            p.step_items.insert(p.step_items.end(), items.begin(), items.end());
+            st.trsm_prefix_off = static_cast<int>(p.step_prefix.size());
+            int64_t acc = 0;
+            p.step_prefix.push_back(0);
+            for (int s : items) {
+                const int64_t w = std::min<int64_t>(kTile, p.sn_ncols[s] - static_cast<int64_t>(k) * kTile);
+                const int64_t below = p.sn_nrows[s] - static_cast<int64_t>(k) * kTile - w;
+                acc += ceil_div(below, kTile);
+                p.step_prefix.push_back(static_cast<int>(acc));
+            }
+            st.trsm_tiles = acc;
+            st.upd_prefix_off = static_cast<int>(p.step_prefix.size());
+            acc = 0;
+            p.step_prefix.push_back(0);
+            for (int s : items) {
+                const int64_t w = std::min<int64_t>(kTile, p.sn_ncols[s] - static_cast<int64_t>(k) * kTile);
+                const int64_t t = p.sn_nrows[s] - static_cast<int64_t>(k) * kTile - w;
+                acc += tri(ceil_div(t, kTile));
+                if (acc > INT32_MAX) throw std::runtime_error("front plan: too many tiles in one step");
+                p.step_prefix.push_back(static_cast<int>(acc));
+            }
+            st.upd_tiles = acc;
+            p.steps.push_back(st);
+        }
+        p.step_level_ptr[l + 1] = static_cast<int>(p.steps.size());
+    }
+    // extend-add rounds and children lists
+    std::vector<int> rank(static_cast<size_t>(p.ns), 0), nseen(static_cast<size_t>(p.ns), 0);
+    std::vector<std::vector<int>> kids(static_cast<size_t>(p.ns));
+    for (int l = 0; l < p.nlevels; ++l) {
+        for (int q = p.level_ptr[l]; q < p.level_ptr[l + 1]; ++q) {
+            const int s = p.level_sn[q];
+            const int par = p.sn_parent[s];
+            if (par < 0) continue;
+            kids[par].push_back(s);
+        }
+        // per-level ranks: reset counters of parents touched at this level
+        for (int q = p.level_ptr[l]; q < p.level_ptr[l + 1]; ++q) {
+            const int par = p.sn_parent[p.level_sn[q]];
+            if (par >= 0) nseen[par] = 0;
+        }
+        for (int q = p.level_ptr[l]; q < p.level_ptr[l + 1]; ++q) {
+            const int s = p.level_sn[q];
+            const int par = p.sn_parent[s];
+            if (par >= 0) rank[s] = nseen[par]++;
+        }
+    }
+    p.ch_ptr.assign(static_cast<size_t>(p.ns) + 1, 0);
+    p.ch_list.clear();
+    for (int s = 0; s < p.ns; ++s) {
+        p.ch_list.insert(p.ch_list.end(), kids[s].begin(), kids[s].end());
+        p.ch_ptr[s + 1] = static_cast<Index>(p.ch_list.size());
+    }
+    p.rounds.clear();
+    p.round_items.clear();
+    p.round_prefix.clear();
+    p.round_level_ptr.assign(static_cast<size_t>(p.nlevels) + 1, 0);
+    for (int l = 0; l < p.nlevels; ++l) {
+        int maxr = -1;
+        for (int q = p.level_ptr[l]; q < p.level_ptr[l + 1]; ++q) {
+            const int s = p.level_sn[q];
+            if (p.sn_parent[s] >= 0 && p.sn_nrows[s] > p.sn_ncols[s]) maxr = std::max(maxr, rank[s]);
+        }
+        for (int r = 0; r <= maxr; ++r) {
+            PlanRound rd;
+            rd.level = l;
+            rd.item_off = static_cast<int>(p.round_items.size());
+            rd.prefix_off = static_cast<int>(p.round_prefix.size());
+            p.round_prefix.push_back(0);
+            int64_t acc = 0;
+            for (int q = p.level_ptr[l]; q < p.level_ptr[l + 1]; ++q) {
+                const int s = p.level_sn[q];
+                if (p.sn_parent[s] < 0 || rank[s] != r) continue;
+                const int64_t u = p.sn_nrows[s] - p.sn_ncols[s];
+                if (u <= 0) continue;
+                p.round_items.push_back(s);
+                acc += tri(ceil_div(u, 32));
+                if (acc > INT32_MAX) throw std::runtime_error("front plan: too many extend-add tiles");
+                p.round_prefix.push_back(static_cast<int>(acc));
+            }
+            rd.nitems = static_cast<int>(p.round_items.size()) - rd.item_off;
+            rd.tiles = acc;
+            if (rd.nitems > 0) p.rounds.push_back(rd);
+            else p.round_prefix.pop_back();
+        }
+        p.round_level_ptr[l + 1] = static_cast<int>(p.rounds.size());
+    }
+}
+
+static void finish_offsets(FrontPlan& p) {
+    p.sn_F_off.assign(static_cast<size_t>(p.ns), 0);
+    p.sn_f_off.assign(static_cast<size_t>(p.ns), 0);
+    p.F_size = 0;
+    p.f_size = 0;
+    p.nnz_factor = 0;
+    p.flops_factor = 0.0;
+    for (int s = 0; s < p.ns; ++s) {
+        const int64_t N = p.sn_nrows[s], K = p.sn_ncols[s];
+        p.sn_F_off[s] = p.F_size;
+        p.F_size += (N * N + 1) & ~int64_t(1);   // keep every front 16-byte aligned in FP64
+        p.sn_f_off[s] = p.f_size;
+        p.f_size += N;
+        p.nnz_factor += N * K - K * (K - 1) / 2;
+        for (int64_t c = 0; c < K; ++c) {
+            const double len = static_cast<double>(N - c);
+            p.flops_factor += len * len;
+        }
+    }
+}
+
+void build_front_plan(const std::vector<LpView>& lps, const core::CSRMatrix& A, int ordering, FrontPlan& p,
+                      const std::vector<Index>* explicit_perm) {
+    p = FrontPlan();
+    p.nlp = static_cast<int>(lps.size());
+    p.row_off.assign(static_cast<size_t>(p.nlp) + 1, 0);
+    p.col_off.assign(static_cast<size_t>(p.nlp) + 1, 0);
+    bool all_dense = true;
+    for (int k = 0; k < p.nlp; ++k) {
+        p.row_off[k + 1] = p.row_off[k] + lps[k].m;
+        p.col_off[k + 1] = p.col_off[k] + lps[k].n;
+        all_dense = all_dense && prefer_dense_front(lps[k]);
+    }
+    p.M = p.row_off[p.nlp];
+    p.N = p.col_off[p.nlp];
+    p.nnzA = A.row_ptrs.empty() ? 0 : A.row_ptrs.back();
+    p.dense_mode = !explicit_perm && (ordering == 0 || ordering == 2) && all_dense;
+
+    if (p.dense_mode) {
+        p.ordering_used = 2;
+        p.perm.resize(static_cast<size_t>(p.M));
+        std::iota(p.perm.begin(), p.perm.end(), 0);
+        p.iperm = p.perm;
+        p.ns = p.nlp;
+        for (int k = 0; k < p.nlp; ++k) {
+            p.sn_first.push_back(p.row_off[k]);
+            p.sn_ncols.push_back(lps[k].m);
+            p.sn_nrows.push_back(lps[k].m);
+            p.sn_parent.push_back(-1);
+            p.sn_lp.push_back(k);
+            p.sn_rows_off.push_back(static_cast<int64_t>(p.rows.size()));
+            for (Index i = 0; i < lps[k].m; ++i) p.rows.push_back(p.row_off[k] + i);
+            p.ea_off.push_back(static_cast<int64_t>(p.ea_map.size()));
+        }
+        p.sn_of_col.resize(static_cast<size_t>(p.M));
+        for (int k = 0; k < p.nlp; ++k)
+            for (Index i = p.row_off[k]; i < p.row_off[k + 1]; ++i) p.sn_of_col[i] = k;
+        finish_offsets(p);
+        build_schedule(p);
+        return;
+    }
+
+    // 1. ordering
+    std::vector<Index> perm0;
+    if (explicit_perm) {
+        if (static_cast<Index>(explicit_perm->size()) != p.M) throw std::invalid_argument("front plan: |P| != m");
+        perm0 = *explicit_perm;
+        std::vector<char> seen(static_cast<size_t>(p.M), 0);
+        for (Index v : perm0) {
+            if (v < 0 || v >= p.M || seen[v]) throw std::invalid_argument("front plan: P is not a permutation");
+            seen[v] = 1;
+        }
+        p.ordering_used = 3;
+    } else if (ordering == 1) {
+        perm0 = compute_amd_ordering(A);
+        p.ordering_used = 1;
+    } else if (ordering == 2) {
+        perm0.resize(static_cast<size_t>(p.M));
+        std::iota(perm0.begin(), perm0.end(), 0);
+        p.ordering_used = 2;
+    } else {
+        perm0 = fill_reducing_ordering(A);
+        p.ordering_used = 0;
+    }
+    std::vector<Index> iperm0(static_cast<size_t>(p.M));
+    for (Index k = 0; k < p.M; ++k) iperm0[perm0[k]] = k;
+    std::vector<Index> rp, ci;
+    permuted_lower_pattern(A, iperm0, rp, ci);
+    std::vector<Index> parent0 = elimination_tree(p.M, rp, ci);
+    // 2. postorder relabel (kept off for an explicit order)
+    std::vector<Index> post = postorder(parent0);
+    if (explicit_perm) std::iota(post.begin(), post.end(), 0);
+    std::vector<Index> ipost(static_cast<size_t>(p.M));
+    for (Index k = 0; k < p.M; ++k) ipost[post[k]] = k;
+    p.perm.resize(static_cast<size_t>(p.M));
+    p.iperm.resize(static_cast<size_t>(p.M));
+    for (Index k = 0; k < p.M; ++k) p.perm[k] = perm0[post[k]];
+    for (Index k = 0; k < p.M; ++k) p.iperm[p.perm[k]] = k;
+    std::vector<Index> parent(static_cast<size_t>(p.M), -1);
+    for (Index k = 0; k < p.M; ++k) {
+        const Index q = parent0[post[k]];
+        parent[k] = q >= 0 ? ipost[q] : -1;
+    }
+    permuted_lower_pattern(A, p.iperm, rp, ci);
+    // 3. column counts by row-subtree traversal
+    std::vector<int64_t> colcount(static_cast<size_t>(p.M), 1);
+    {
+        std::vector<Index> mark(static_cast<size_t>(p.M), -1);
+        for (Index i = 0; i < p.M; ++i) {
+            mark[i] = i;
+            for (Index q = rp[i]; q < rp[i + 1]; ++q)
+                for (Index j = ci[q]; j != -1 && mark[j] != i; j = parent[j]) {
+                    mark[j] = i;
+                    colcount[j]++;
+                }
+        }
+    }
+    std::vector<Index> nchild(static_cast<size_t>(p.M), 0);
+    for (Index j = 0; j < p.M; ++j) if (parent[j] >= 0) nchild[parent[j]]++;
+    // 4. fundamental supernodes
+    std::vector<Index> sfirst;
+    for (Index j = 0; j < p.M; ++j) {
+        const bool extend = j > 0 && parent[j - 1] == j && colcount[j - 1] == colcount[j] + 1 && nchild[j] == 1;
+        if (!extend) sfirst.push_back(j);
+    }
+    const Index nfund = static_cast<Index>(sfirst.size());
+    std::vector<Index> fsn(static_cast<size_t>(p.M));
+    for (Index s = 0; s < nfund; ++s) {
+        const Index e = s + 1 < nfund ? sfirst[s + 1] : p.M;
+        for (Index j = sfirst[s]; j < e; ++j) fsn[j] = s;
+    }
+    // 5. relaxed amalgamation of a supernode into its parent when it is the
+    //    parent's last child (its columns end right before the parent's).
+    std::vector<int64_t> s_ncols(static_cast<size_t>(nfund)), s_nrows(static_cast<size_t>(nfund)),
+        s_zeros(static_cast<size_t>(nfund), 0);
+    std::vector<Index> s_first(sfirst), s_par(static_cast<size_t>(nfund), -1);
+    for (Index s = 0; s < nfund; ++s) {
+        const Index e = s + 1 < nfund ? sfirst[s + 1] : p.M;
+        s_ncols[s] = e - sfirst[s];
+        s_nrows[s] = colcount[sfirst[s]];
+        const Index last = e - 1;
+        s_par[s] = parent[last] >= 0 ? fsn[parent[last]] : -1;
+    }
+    std::vector<Index> merged_into(static_cast<size_t>(nfund), -1);
+    auto find = [&](Index s) {
+        while (merged_into[s] >= 0) s = merged_into[s];
+        return s;
+    };
+    for (Index s = 0; s < nfund; ++s) {  // postorder: children first
+        const Index par0 = s_par[s];
+        if (par0 < 0) continue;
+        const Index par = find(par0);
+        const int64_t lastc = s_first[s] + s_ncols[s];
+        if (lastc != s_first[par]) continue;  // not the parent's last child
+        const int64_t nc = s_ncols[s] + s_ncols[par];
+        const int64_t nr = s_ncols[s] + s_nrows[par];
+        const int64_t z = s_zeros[s] + s_zeros[par] + s_ncols[s] * (s_ncols[s] + s_nrows[par] - s_nrows[s]);
+        const int64_t total = nc * nr - nc * (nc - 1) / 2;
+        const double frac = static_cast<double>(z) / static_cast<double>(total);
+        const bool merge = nc <= 16 || (nc <= 48 && frac < 0.5) || (nc <= 160 && frac < 0.2) || frac < 0.06;
+        if (!merge) continue;
+        merged_into[s] = par;
+        s_first[par] = s_first[s];
+        s_ncols[par] = nc;
+        s_nrows[par] = nr;
+        s_zeros[par] = z;
+    }
+    // final supernodes in column order
+    std::vector<Index> final_id(static_cast<size_t>(nfund), -1);
+    for (Index s = 0; s < nfund; ++s) {
+        if (merged_into[s] >= 0) continue;
+        final_id[s] = 0;
+    }
+    std::vector<std::pair<Index, Index>> roots;  // (first col, fund id)
+    for (Index s = 0; s < nfund; ++s) if (merged_into[s] < 0) roots.push_back({s_first[s], s});
+    std::sort(roots.begin(), roots.end());
+    p.ns = static_cast<int>(roots.size());
+    for (int t = 0; t < p.ns; ++t) final_id[roots[t].second] = t;
+    p.sn_first.resize(static_cast<size_t>(p.ns));
+    p.sn_ncols.resize(static_cast<size_t>(p.ns));
+    p.sn_parent.assign(static_cast<size_t>(p.ns), -1);
+    p.sn_lp.assign(static_cast<size_t>(p.ns), 0);
+    p.sn_of_col.assign(static_cast<size_t>(p.M), -1);
+    for (int t = 0; t < p.ns; ++t) {
+        const Index s = roots[t].second;
+        p.sn_first[t] = s_first[s];
+        p.sn_ncols[t] = static_cast<Index>(s_ncols[s]);
+        for (Index j = s_first[s]; j < s_first[s] + s_ncols[s]; ++j) p.sn_of_col[j] = t;
+    }
+    for (int t = 0; t < p.ns; ++t) {
+        const Index last = p.sn_first[t] + p.sn_ncols[t] - 1;
+        p.sn_parent[t] = parent[last] >= 0 ? p.sn_of_col[parent[last]] : -1;
+        const Index row = p.perm[p.sn_first[t]];
+        p.sn_lp[t] = static_cast<Index>(std::upper_bound(p.row_off.begin(), p.row_off.end(), row) - p.row_off.begin() - 1);
+    }
+    // 6. row structures (children precede parents in column order)
+    std::vector<Index> cp(static_cast<size_t>(p.M) + 1, 0), crow(ci.size());
+    for (Index q : ci) cp[static_cast<size_t>(q) + 1]++;
+    for (Index j = 0; j < p.M; ++j) cp[j + 1] += cp[j];
+    {
+        std::vector<Index> nx(cp.begin(), cp.end() - 1);
+        for (Index i = 0; i < p.M; ++i)
+            for (Index q = rp[i]; q < rp[i + 1]; ++q) crow[nx[ci[q]]++] = i;
+    }
+    std::vector<std::vector<Index>> kids(static_cast<size_t>(p.ns));
+    for (int t = 0; t < p.ns; ++t) if (p.sn_parent[t] >= 0) kids[p.sn_parent[t]].push_back(t);
+    std::vector<Index> mark(static_cast<size_t>(p.M), -1);
+    std::vector<Index> buf;
+    p.sn_rows_off.assign(static_cast<size_t>(p.ns), 0);
+    p.sn_nrows.assign(static_cast<size_t>(p.ns), 0);
+    for (int t = 0; t < p.ns; ++t) {
+        const Index f = p.sn_first[t], l = f + p.sn_ncols[t];
+        buf.clear();
+        for (Index j = f; j < l; ++j) { mark[j] = t; buf.push_back(j); }
+        for (Index j = f; j < l; ++j)
+            for (Index q = cp[j]; q < cp[j + 1]; ++q) {
+                const Index i = crow[q];
+                if (i >= l && mark[i] != t) { mark[i] = t; buf.push_back(i); }
+            }
+        for (int c : kids[t]) {
+            const int64_t o = p.sn_rows_off[c];
+            for (Index q = p.sn_ncols[c]; q < p.sn_nrows[c]; ++q) {
+                const Index i = p.rows[o + q];
+                if (i >= l && mark[i] != t) { mark[i] = t; buf.push_back(i); }
+            }
+        }
+        std::sort(buf.begin() + (l - f), buf.end());
+        p.sn_rows_off[t] = static_cast<int64_t>(p.rows.size());
+        p.sn_nrows[t] = static_cast<Index>(buf.size());
+        p.rows.insert(p.rows.end(), buf.begin(), buf.end());
+    }
+    // 7. extend-add maps
+    p.ea_off.assign(static_cast<size_t>(p.ns), 0);
+    std::vector<Index> pos(static_cast<size_t>(p.M), -1);
+    for (int t = 0; t < p.ns; ++t) {
+        p.ea_off[t] = static_cast<int64_t>(p.ea_map.size());
+        const int par = p.sn_parent[t];
+        if (par < 0) continue;
+        const int64_t po = p.sn_rows_off[par];
+        for (Index q = 0; q < p.sn_nrows[par]; ++q) pos[p.rows[po + q]] = q;
+        const int64_t o = p.sn_rows_off[t];
+        for (Index q = p.sn_ncols[t]; q < p.sn_nrows[t]; ++q) {
+            const Index r = pos[p.rows[o + q]];
+            if (r < 0) throw std::runtime_error("front plan: child row missing from parent structure");
+            p.ea_map.push_back(r);
+        }
+        for (Index q = 0; q < p.sn_nrows[par]; ++q) pos[p.rows[po + q]] = -1;
+    }
+    finish_offsets(p);
+    build_schedule(p);
+    // 8. Khatri-Rao assembly map W
+    const int64_t noff = static_cast<int64_t>(ci.size());
+    p.nslots = p.M + noff;
+    std::vector<int64_t> cnt(static_cast<size_t>(p.nslots) + 1, 0);
+    // CSC view of the batch: column k of lp L lives at col_off[L] + local
+    auto slot_of = [&](Index pi, Index pj) -> int64_t {
+        if (pi == pj) return pi;
+        const Index* b = ci.data() + rp[pi];
+        const Index* e = ci.data() + rp[pi + 1];
+        const Index* it = std::lower_bound(b, e, pj);
+        return p.M + (it - ci.data());
+    };
+    for (int L = 0; L < p.nlp; ++L) {
+        const LpView& v = lps[L];
+        for (Index j = 0; j < v.n; ++j)
+            for (Index a = v.col_ptrs[j]; a < v.col_ptrs[j + 1]; ++a)
+                for (Index b = a; b < v.col_ptrs[j + 1]; ++b) {
+                    const Index pa = p.iperm[p.row_off[L] + v.row_idx[a]];
+                    const Index pb = p.iperm[p.row_off[L] + v.row_idx[b]];
+                    cnt[slot_of(std::max(pa, pb), std::min(pa, pb)) + 1]++;
+                }
+    }
+    for (int64_t s = 0; s < p.nslots; ++s) cnt[s + 1] += cnt[s];
+    p.w_ptr = cnt;
+    p.w_col.resize(static_cast<size_t>(cnt.back()));
+    p.w_val.resize(static_cast<size_t>(cnt.back()));
+    {
+        std::vector<int64_t> nx(cnt.begin(), cnt.end() - 1);
+        for (int L = 0; L < p.nlp; ++L) {
+            const LpView& v = lps[L];
+            for (Index j = 0; j < v.n; ++j)
+                for (Index a = v.col_ptrs[j]; a < v.col_ptrs[j + 1]; ++a)
+                    for (Index b = a; b < v.col_ptrs[j + 1]; ++b) {
+                        const Index pa = p.iperm[p.row_off[L] + v.row_idx[a]];
+                        const Index pb = p.iperm[p.row_off[L] + v.row_idx[b]];
+                        const int64_t sl = slot_of(std::max(pa, pb), std::min(pa, pb));
+                        const int64_t d = nx[sl]++;
+                        p.w_col[d] = p.col_off[L] + j;
+                        p.w_val[d] = v.vals[a] * v.vals[b];
+                    }
+        }
+    }
+    p.slot_pos.resize(static_cast<size_t>(p.nslots));
+    p.slot_i.resize(static_cast<size_t>(p.nslots));
+    p.slot_j.resize(static_cast<size_t>(p.nslots));
+    auto fpos = [&](Index i, Index j) -> int64_t {
+        const int t = p.sn_of_col[j];
+        const Index* b = p.rows.data() + p.sn_rows_off[t];
+        const Index* e = b + p.sn_nrows[t];
+        const Index* it = std::lower_bound(b + (j - p.sn_first[t]), e, i);
+        if (it == e || *it != i) throw std::runtime_error("front plan: M entry outside the factor structure");
+        return p.sn_F_off[t] + (it - b) + static_cast<int64_t>(j - p.sn_first[t]) * p.sn_nrows[t];
+    };
+    for (Index i = 0; i < p.M; ++i) {
+        p.slot_i[i] = i;
+        p.slot_j[i] = i;
+        p.slot_pos[i] = fpos(i, i);
+    }
+    for (Index i = 0; i < p.M; ++i)
+        for (Index q = rp[i]; q < rp[i + 1]; ++q) {
+            const int64_t sl = p.M + q;
+            p.slot_i[sl] = i;
+            p.slot_j[sl] = ci[q];
+            p.slot_pos[sl] = fpos(i, ci[q]);
+        }
+}
+
+}  // namespace ipm
+}  // namespace sankhya

@@ -37,7 +37,8 @@ class Info(C.Structure):
                 ("precision_path", C.c_int), ("switch_iteration", C.c_int), ("factorizations", C.c_int),
                 ("solves", C.c_int), ("refine_steps", C.c_int), ("learned_start", C.c_int),
                 ("setup_ms", C.c_double), ("solve_ms", C.c_double), ("nnz_factor", C.c_longlong),
-                ("num_supernodes", C.c_int), ("dense_front", C.c_int)]
+                ("num_supernodes", C.c_int), ("dense_front", C.c_int), ("device_ms", C.c_double),
+                ("flops_factor", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -62,6 +63,7 @@ def _declare(L):
     L.sk_lp_generate.argtypes = [C.c_int, C.c_int, C.POINTER(vp)]
     L.sk_lp_random.argtypes = [C.c_int, C.c_int, C.c_double, C.c_ulonglong, C.POINTER(vp)]
     L.sk_lp_read_mps.argtypes = [C.c_char_p, C.POINTER(vp)]
+    L.sk_lp_block_angular.argtypes = [C.c_ulonglong, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(vp)]
     L.sk_lp_dims.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
     L.sk_lp_arrays.argtypes = [vp] + [C.POINTER(vp)] * 5
     L.sk_lp_bounds.argtypes = [vp, C.POINTER(vp), C.POINTER(vp)]
@@ -77,6 +79,7 @@ def _declare(L):
         L.sk_solver_run.argtypes = [vp]
         L.sk_solver_result.argtypes = [vp, C.c_int, vp, vp, vp, C.POINTER(Info)]
         L.sk_solver_destroy.argtypes = [vp]
+        L.sk_solver_profile.argtypes = [vp, C.c_int, _f64p, C.c_int]
         L.sk_kkt_create.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p, vp, C.c_int, C.POINTER(vp)]
         L.sk_kkt_factorize_device.argtypes = [vp, vp]
         L.sk_kkt_solve_device.argtypes = [vp, vp, C.c_double]
@@ -168,6 +171,13 @@ def random_lp(m, n, density, seed):
     return _lp_from_handle(h, "random%dx%d" % (m, n))
 
 
+def block_angular(seed, blocks, block_rows=500, block_cols=1200, link_rows=2000, nnz_per_col=5):
+    h = C.c_void_p()
+    check(lib().sk_lp_block_angular(seed, blocks, block_rows, block_cols, link_rows, nnz_per_col, C.byref(h)),
+          "sk_lp_block_angular")
+    return _lp_from_handle(h, "block_angular%dx%d" % (blocks, link_rows))
+
+
 def read_mps(path):
     h = C.c_void_p()
     check(lib().sk_lp_read_mps(path.encode(), C.byref(h)), "sk_lp_read_mps")
@@ -197,3 +207,119 @@ def symbolic(m, n, rp, ci, P, cap=None):
     if nnz < 0:
         raise RuntimeError("sk_compute_symbolic failed (%d): %s" % (nnz, last_error()))
     return Pinv, parent, Lrp, Lci[:nnz].copy()
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def solve(lp, x0=None, y0=None, s0=None, **opts):
+    """One-shot device solve of an LP (sk_ipm_solve_csc). Returns (info dict, x, y, s)."""
+    L = lib()
+    o = options(**opts)
+    x = np.zeros(lp.n)
+    y = np.zeros(lp.m)
+    s = np.zeros(lp.n)
+    info = Info()
+    rc = L.sk_ipm_solve_csc(lp.m, lp.n, lp.col_ptrs, lp.row_idx, lp.vals, lp.b, lp.c, C.byref(o), _ptr(x), _ptr(y),
+                            _ptr(s), C.byref(info))
+    check(rc, "sk_ipm_solve_csc")
+    return info.as_dict(), x, y, s
+
+
+class Solver:
+    """Persistent device solver over a batch of LPs (sk_solver_*): the data stays
+    resident between run() calls, so run() times the IPM alone."""
+
+    def __init__(self, lps, **opts):
+        L = lib()
+        self.lps = list(lps)
+        k = len(self.lps)
+        self._keep = self.lps
+        m = (C.c_int * k)(*[lp.m for lp in self.lps])
+        n = (C.c_int * k)(*[lp.n for lp in self.lps])
+        vp = C.c_void_p
+        cp = (vp * k)(*[lp.col_ptrs.ctypes.data for lp in self.lps])
+        ri = (vp * k)(*[lp.row_idx.ctypes.data for lp in self.lps])
+        va = (vp * k)(*[lp.vals.ctypes.data for lp in self.lps])
+        b = (vp * k)(*[lp.b.ctypes.data for lp in self.lps])
+        c = (vp * k)(*[lp.c.ctypes.data for lp in self.lps])
+        self.opts = options(**opts)
+        self.h = C.c_void_p()
+        check(L.sk_solver_create(k, m, n, cp, ri, va, b, c, C.byref(self.opts), C.byref(self.h)), "sk_solver_create")
+
+    def set_start(self, k, x, y, s):
+        x, y, s = (np.ascontiguousarray(v, dtype=np.float64) for v in (x, y, s))
+        check(lib().sk_solver_set_start(self.h, k, _ptr(x), _ptr(y), _ptr(s)), "sk_solver_set_start")
+
+    def run(self):
+        check(lib().sk_solver_run(self.h), "sk_solver_run")
+
+    def result(self, k, want_vectors=True):
+        lp = self.lps[k]
+        info = Info()
+        if want_vectors:
+            x, y, s = np.zeros(lp.n), np.zeros(lp.m), np.zeros(lp.n)
+            check(lib().sk_solver_result(self.h, k, _ptr(x), _ptr(y), _ptr(s), C.byref(info)), "sk_solver_result")
+            return info.as_dict(), x, y, s
+        check(lib().sk_solver_result(self.h, k, None, None, None, C.byref(info)), "sk_solver_result")
+        return info.as_dict(), None, None, None
+
+    def profile(self, fp32=True):
+        out = np.zeros(16)
+        n = lib().sk_solver_profile(self.h, 1 if fp32 else 0, out, 16)
+        if n < 0:
+            raise RuntimeError("sk_solver_profile failed (%d): %s" % (n, last_error()))
+        names = ["assembly", "potrf", "trsm", "update", "extend_add", "fwd_solve", "bwd_solve"]
+        d = {nm: {"ms": out[2 * i], "launches": int(out[2 * i + 1])} for i, nm in enumerate(names)}
+        d["update_flops"] = out[14]
+        d["update_min_bytes"] = out[15]
+        return d
+
+    def close(self):
+        if self.h:
+            lib().sk_solver_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Kkt:
+    """Normal-equation engine (sk_kkt_*), mirror of the reference's GPUKKTCholeskySolver."""
+
+    def __init__(self, m, n, rp, ci, vals, P=None, precision=PREC_FP64):
+        self.m, self.n = m, n
+        self._keep = (rp, ci, vals)
+        self.h = C.c_void_p()
+        Pp = None if P is None else np.ascontiguousarray(P, dtype=np.int32)
+        self._P = Pp
+        check(lib().sk_kkt_create(m, n, rp, ci, vals, _ptr(Pp), precision, C.byref(self.h)), "sk_kkt_create")
+
+    def factorize(self, theta):
+        return lib().sk_kkt_factorize(self.h, np.ascontiguousarray(theta, dtype=np.float64))
+
+    def solve(self, rhs, tol=1e-10):
+        r = np.ascontiguousarray(rhs, dtype=np.float64).copy()
+        rc = lib().sk_kkt_solve(self.h, r, tol)
+        return rc, r
+
+    def factor_dense(self):
+        L = np.zeros((self.m, self.m))
+        D = np.zeros(self.m)
+        check(lib().sk_kkt_get_factor(self.h, L, D), "sk_kkt_get_factor")
+        return L, D
+
+    def close(self):
+        if self.h:
+            lib().sk_kkt_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,80 @@
+"""Product symbolic analysis (C ABI) against the reference: bit-exact ordering,
+elimination tree and L pattern (golden fixtures from the reference build, and the
+reference build itself when present)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def test_reference_golden_vectors(sk):
+    # tests/unit/test_ipm_symbolic.cpp (star, cycle) and test_gpu_kkt.cu ordering
+    rp = np.array([0, 4, 5, 6, 7, 8], dtype=np.int32)
+    ci = np.array([0, 1, 2, 3, 0, 1, 2, 3], dtype=np.int32)
+    P = sk.amd_ordering(5, 5, rp, ci)
+    assert P.tolist() == [1, 2, 3, 0, 4]
+    Pinv, parent, Lrp, Lci = sk.symbolic(5, 5, rp, ci, P)
+    assert parent.tolist() == [3, 3, 3, 4, -1] and Lrp[5] == 4
+    rp = np.array([0, 2, 4, 6, 8, 9], dtype=np.int32)
+    ci = np.array([0, 3, 0, 1, 1, 2, 2, 3, 4], dtype=np.int32)
+    P = sk.amd_ordering(5, 5, rp, ci)
+    assert P.tolist() == [4, 0, 1, 2, 3]
+    Pinv, parent, Lrp, Lci = sk.symbolic(5, 5, rp, ci, P)
+    assert Lrp.tolist() == [0, 0, 0, 1, 2, 5]
+    assert Lci.tolist() == [1, 2, 1, 2, 3]
+    assert parent.tolist() == [-1, 2, 3, 4, -1]
+    rp = np.array([0, 3, 5, 7], dtype=np.int32)
+    ci = np.array([0, 3, 4, 1, 3, 2, 4], dtype=np.int32)
+    assert sk.amd_ordering(3, 5, rp, ci).tolist() == [1, 0, 2]
+
+
+def test_symbolic_matches_reference_fixtures(sk):
+    with open(os.path.join(HERE, "golden", "reference_symbolic.json")) as f:
+        cases = json.load(f)["cases"]
+    for c in cases:
+        lp = sk.random_lp(c["m"], c["n"], c["density"], c["seed"])
+        assert lp.nnz == c["digest"]["nnz"]
+        rp, ci, _ = lp.csr()
+        P = sk.amd_ordering(lp.m, lp.n, rp, ci)
+        assert P.tolist() == c["P"]
+        Pinv, parent, Lrp, Lci = sk.symbolic(lp.m, lp.n, rp, ci, P)
+        assert parent.tolist() == c["parent"]
+        assert Lrp.tolist() == c["L_row_ptrs"]
+        assert Lci.tolist() == c["L_cols"]
+
+
+def test_symbolic_matches_oracle_and_reference_build(sk, oracle):
+    for (m, n, d, seed) in [(30, 60, 0.1, 5), (150, 320, 0.03, 6), (500, 1000, 0.01, 0xC0)]:
+        lp = sk.random_lp(m, n, d, seed)
+        rp, ci, _ = lp.csr()
+        P = sk.amd_ordering(m, n, rp, ci)
+        assert np.array_equal(P, oracle.min_degree(m, n, rp, ci))
+        a = sk.symbolic(m, n, rp, ci, P)
+        b = oracle.symbolic(m, n, rp, ci, P)
+        for u, v in zip(a, b):
+            assert np.array_equal(u, v)
+        if oracle.have_reference():
+            assert np.array_equal(P, oracle.ref_min_degree(m, n, rp, ci))
+            for u, v in zip(a, oracle.ref_symbolic(m, n, rp, ci, P)):
+                assert np.array_equal(u, v)
+
+
+def test_fill_ordering_is_permutation_and_competitive(sk):
+    lp = sk.random_lp(400, 900, 0.012, 9)
+    rp, ci, _ = lp.csr()
+    Pf = sk.fill_ordering(lp.m, lp.n, rp, ci)
+    assert sorted(Pf.tolist()) == list(range(lp.m))
+    Pr = sk.amd_ordering(lp.m, lp.n, rp, ci)
+    nf = len(sk.symbolic(lp.m, lp.n, rp, ci, Pf)[3])
+    nr = len(sk.symbolic(lp.m, lp.n, rp, ci, Pr)[3])
+    assert nf <= 1.15 * nr
+
+
+def test_symbolic_rejects_bad_permutation(sk):
+    rp = np.array([0, 1, 2], dtype=np.int32)
+    ci = np.array([0, 1], dtype=np.int32)
+    with pytest.raises(RuntimeError):
+        sk.symbolic(2, 2, rp, ci, np.array([0, 0], dtype=np.int32))
