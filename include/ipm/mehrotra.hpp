@@ -29,6 +29,7 @@ struct MehrotraOptions {
     int verbose = 0;
     double mu_switch = 1e-6;
     int ruiz_passes = 10;
+    int strict = 0;
 };
 
 struct MehrotraResult {

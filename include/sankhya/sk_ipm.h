@@ -57,6 +57,12 @@ typedef struct sk_options {
     int verbose;          /* 0 = silent; >0 prints per-iteration lines on stderr */
     double mu_switch;     /* mixed precision: switch the factor to FP64 once mu < mu_switch (default 1e-6) */
     int ruiz_passes;      /* default 10 (src/ipm/mehrotra_device.cu:293) */
+    int strict;           /* 1: a normal-equation solve that misses 1e-9 max(1, ||rp||_2) or a direction
+                           * with e1, e2 or e3 > 1e-8 ends the LP with IterationLimit, as the reference
+                           * does (src/ipm/mehrotra_device.cu:793-797, 814-822). 0 (default): such a
+                           * miss first switches a mixed-precision solve to the FP64 factor; an FP64
+                           * direction is then used when it is finite with e1, e2, e3 <= 1e-6, and the
+                           * merit line search plus the exact stopping test decide progress. */
 } sk_options;
 
 typedef struct sk_info {

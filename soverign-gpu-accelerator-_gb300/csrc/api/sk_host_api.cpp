@@ -84,6 +84,7 @@ void sk_options_default(sk_options* opt) {
     opt->verbose = 0;
     opt->mu_switch = 1e-6;
     opt->ruiz_passes = 10;
+    opt->strict = 0;
 }
 
 int sk_lp_generate(int family, int instance, sk_lp** out) {

@@ -286,6 +286,36 @@ __global__ void k_masked_add(int n, const double* __restrict__ src, const int* _
     if (i < n && mask[lp_of[i]] != 0.0) dst[i] += src[i];
 }
 
+// y += a[lp] * x
+__global__ void k_axpy_lp(int n, const double* __restrict__ a, const double* __restrict__ x,
+                          const int* __restrict__ lp_of, double* __restrict__ y) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        const double al = a[lp_of[i]];
+        if (al != 0.0) y[i] += al * x[i];
+    }
+}
+// p = z + b[lp] * p
+__global__ void k_xpby_lp(int n, const double* __restrict__ z, const double* __restrict__ b,
+                          const int* __restrict__ lp_of, double* __restrict__ p) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = z[i] + b[lp_of[i]] * p[i];
+}
+
+struct RedRZ {           // [max |r|, sum r z]
+    const double *r, *z;
+    __device__ static constexpr int op(int k) { return k == 0 ? OP_MAX : OP_SUM; }
+    __device__ void operator()(int i, double* v) const {
+        v[0] = fabs(r[i]);
+        v[1] = r[i] * z[i];
+    }
+};
+struct RedDot {          // [sum a b]
+    const double *a, *b;
+    __device__ static constexpr int op(int) { return OP_SUM; }
+    __device__ void operator()(int i, double* v) const { v[0] = a[i] * b[i]; }
+};
+
 }  // namespace
 
 void spmv_csr(int rows, const int* rp, const int* ci, const double* v, const double* x, double alpha, double beta,
@@ -308,7 +338,7 @@ struct DeviceIPM::Impl {
     Slot<int> a_rp, a_ci, t_rp, t_ci, row_lp, col_lp, mc_s, mc_e, mc_p, nc_s, nc_e, nc_p;
     Slot<double> a_v, t_v, b, c, R, C;
     Slot<double> x, y, s, rp, rd, theta, rxs, v, rkkt, dy, dx, ds, dxa, dya, dsa, e1, e2, e3;
-    Slot<double> xt, yt, stt, rpt, rdt, r, corr, bak, tm, cdx, cdy, cds, crxs;
+    Slot<double> xt, yt, stt, rpt, rdt, r, corr, bak, tm, cdx, cdy, cds, crxs, pz, pp, pq;
     Slot<double> scal;                      // per-LP scalars [8][nlp]
     Slot<double> partial, redout;
     int max_chunks = 0;
@@ -316,7 +346,7 @@ struct DeviceIPM::Impl {
     std::vector<LpResult> res;
     std::vector<char> active, user_start;
     std::vector<double> rp0, rd0, mu0;
-    int factorizations = 0, solves = 0, refine_steps = 0, precision_path = 0;
+    int factorizations = 0, solves = 0, refine_steps = 0, precision_path = 0, last_pcg = 0, max_pcg_iter = 0;
     bool switched = false, used_fp32 = false;
     double solve_ms = 0.0, device_ms = 0.0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -482,7 +512,8 @@ DeviceIPM::DeviceIPM(const std::vector<ipm::LpView>& lps, const std::vector<cons
     for (auto* sl2 : {&I.x, &I.s, &I.rd, &I.theta, &I.rxs, &I.v, &I.dx, &I.ds, &I.dxa, &I.dsa, &I.e2, &I.e3, &I.xt,
                       &I.stt, &I.rdt, &I.cdx, &I.cds, &I.crxs})
         reserve(ar, *sl2, N);
-    for (auto* sl2 : {&I.y, &I.rp, &I.rkkt, &I.dy, &I.dya, &I.e1, &I.yt, &I.rpt, &I.r, &I.corr, &I.bak, &I.tm, &I.cdy})
+    for (auto* sl2 : {&I.y, &I.rp, &I.rkkt, &I.dy, &I.dya, &I.e1, &I.yt, &I.rpt, &I.r, &I.corr, &I.bak, &I.tm, &I.cdy,
+                      &I.pz, &I.pp, &I.pq})
         reserve(ar, *sl2, M);
     reserve(ar, I.scal, static_cast<size_t>(8) * I.nlp);
     reserve(ar, I.partial, static_cast<size_t>(I.max_chunks) * kMaxR);
@@ -494,7 +525,7 @@ DeviceIPM::DeviceIPM(const std::vector<ipm::LpView>& lps, const std::vector<cons
     for (auto* sl2 : {&I.a_v, &I.t_v, &I.b, &I.c, &I.R, &I.C, &I.x, &I.s, &I.rd, &I.theta, &I.rxs, &I.v, &I.dx, &I.ds,
                       &I.dxa, &I.dsa, &I.e2, &I.e3, &I.xt, &I.stt, &I.rdt, &I.cdx, &I.cds, &I.crxs, &I.y, &I.rp,
                       &I.rkkt, &I.dy, &I.dya, &I.e1, &I.yt, &I.rpt, &I.r, &I.corr, &I.bak, &I.tm, &I.cdy, &I.scal,
-                      &I.partial, &I.redout})
+                      &I.partial, &I.redout, &I.pz, &I.pp, &I.pq})
         bind(ar, *sl2);
     upload(I.a_rp, A.row_ptrs, I.st); upload(I.a_ci, A.col_indices, I.st); upload(I.a_v, A.values, I.st);
     upload(I.t_rp, cp, I.st); upload(I.t_ci, ri, I.st); upload(I.t_v, cv, I.st);
@@ -606,51 +637,126 @@ void DeviceIPM::run() {
         r.rel_dinf = hn[k * 4 + 1] / (1.0 + I.cinf[k]);
         r.rel_gap = std::fabs(r.objective - by) / (1.0 + std::fabs(r.objective) + std::fabs(by));
     };
-    // ---- normal-equation solve with iterative refinement; returns per-LP success
+    // ---- normal-equation solve M0 dy = rhs, returns per-LP success (||r||_inf <= tol).
+    // Strict mode: the reference's iterative refinement (up to 10 steps, rollback on
+    // stagnation; src/cuda/kkt.cu:778-842). Default: preconditioned conjugate
+    // gradients with the regularised factor as preconditioner (the iterative
+    // refinement stalls once A Theta A^T is nearly singular), keeping each LP's best
+    // iterate. Vectors and the operator are FP64 in both cases.
+    auto normal_apply = [&](const double* xx, double* out) {   // out = A Theta A^T xx
+        spmv(N, I.gt, I.t_rp.ptr, I.t_ci.ptr, I.t_v.ptr, xx, EpiTheta{I.theta.ptr, K.scratch_n()}, st);
+        spmv(M, I.ga, I.a_rp.ptr, I.a_ci.ptr, I.a_v.ptr, K.scratch_n(), EpiAxpby{1.0, 0.0, out}, st);
+    };
+    auto resid_norm = [&](const double* rhs, const double* xx) {   // I.r = rhs - M0 xx, returns max|r| per LP
+        spmv(N, I.gt, I.t_rp.ptr, I.t_ci.ptr, I.t_v.ptr, xx, EpiTheta{I.theta.ptr, K.scratch_n()}, st);
+        spmv(M, I.ga, I.a_rp.ptr, I.a_ci.ptr, I.a_v.ptr, K.scratch_n(), EpiRhsMinus{rhs, I.r.ptr}, st);
+        I.reduce_rows<1>(RedAbsMax{I.r.ptr}, I.redout.ptr);
+        return I.fetch(nlp);
+    };
     auto solve = [&](const double* rhs, double* out, std::vector<char>& ok) {
         ++I.solves;
-        const int max_ir = K.last_fp32() ? 30 : 10;
         K.apply_inverse(rhs, out);
-        auto resid = [&](const double* xx) {
-            spmv(N, I.gt, I.t_rp.ptr, I.t_ci.ptr, I.t_v.ptr, xx, EpiTheta{I.theta.ptr, K.scratch_n()}, st);
-            spmv(M, I.ga, I.a_rp.ptr, I.a_ci.ptr, I.a_v.ptr, K.scratch_n(), EpiRhsMinus{rhs, I.r.ptr}, st);
-            I.reduce_rows<1>(RedAbsMax{I.r.ptr}, I.redout.ptr);
-            return I.fetch(nlp);
-        };
-        std::vector<double> rn = resid(out);
+        std::vector<double> rn = resid_norm(rhs, out);
         std::vector<char> done(nlp, 0), stag(nlp, 0);
+        I.last_pcg = 0;
         for (int k = 0; k < nlp; ++k) done[k] = !I.active[k] || rn[k] <= tol[k];
-        for (int it = 0; it < max_ir; ++it) {
-            bool any = false;
-            std::vector<double> rm(nlp);
-            for (int k = 0; k < nlp; ++k) { rm[k] = (!done[k] && !stag[k]) ? 1.0 : 0.0; any |= rm[k] != 0.0; }
-            if (!any) break;
-            ++I.refine_steps;
-            I.put_scalars(4, rm);
-            SK_CUDA(cudaMemcpyAsync(I.bak.ptr, out, sizeof(double) * M, cudaMemcpyDeviceToDevice, st));
-            K.apply_inverse(I.r.ptr, I.corr.ptr);
-            k_masked_add<<<nblk(M), 256, 0, st>>>(M, I.corr.ptr, I.row_lp.ptr, d_rmask, out);
-            std::vector<double> rn2 = resid(out);
-            std::vector<double> roll(nlp, 0.0);
-            bool any_roll = false;
-            for (int k = 0; k < nlp; ++k) {
-                if (rm[k] == 0.0) continue;
-                if (rn2[k] <= tol[k]) { done[k] = 1; rn[k] = rn2[k]; }
-                else if (rn2[k] >= rn[k]) { stag[k] = 1; roll[k] = 1.0; any_roll = true; }
-                else rn[k] = rn2[k];
+        if (o.strict) {
+            for (int it = 0; it < 10; ++it) {
+                bool any = false;
+                std::vector<double> rm(nlp);
+                for (int k = 0; k < nlp; ++k) { rm[k] = (!done[k] && !stag[k]) ? 1.0 : 0.0; any |= rm[k] != 0.0; }
+                if (!any) break;
+                ++I.refine_steps;
+                I.put_scalars(4, rm);
+                SK_CUDA(cudaMemcpyAsync(I.bak.ptr, out, sizeof(double) * M, cudaMemcpyDeviceToDevice, st));
+                K.apply_inverse(I.r.ptr, I.corr.ptr);
+                k_masked_add<<<nblk(M), 256, 0, st>>>(M, I.corr.ptr, I.row_lp.ptr, d_rmask, out);
+                std::vector<double> rn2 = resid_norm(rhs, out);
+                std::vector<double> roll(nlp, 0.0);
+                bool any_roll = false;
+                for (int k = 0; k < nlp; ++k) {
+                    if (rm[k] == 0.0) continue;
+                    if (rn2[k] <= tol[k]) { done[k] = 1; rn[k] = rn2[k]; }
+                    else if (rn2[k] >= rn[k]) { stag[k] = 1; roll[k] = 1.0; any_roll = true; }
+                    else rn[k] = rn2[k];
+                }
+                if (any_roll) {
+                    I.put_scalars(4, roll);
+                    k_masked_copy<<<nblk(M), 256, 0, st>>>(M, I.bak.ptr, I.row_lp.ptr, d_rmask, out);
+                }
             }
-            if (any_roll) {
-                I.put_scalars(4, roll);
-                k_masked_copy<<<nblk(M), 256, 0, st>>>(M, I.bak.ptr, I.row_lp.ptr, d_rmask, out);
+        } else {
+            bool any = false;
+            for (int k = 0; k < nlp; ++k) any |= !done[k];
+            if (any) {
+                const int max_it = K.last_fp32() ? 30 : 60;
+                std::vector<double> best = rn, rz(nlp, 0.0), al(nlp, 0.0), be(nlp, 0.0), imp(nlp, 0.0);
+                SK_CUDA(cudaMemcpyAsync(I.bak.ptr, out, sizeof(double) * M, cudaMemcpyDeviceToDevice, st));
+                K.apply_inverse(I.r.ptr, I.pz.ptr);
+                SK_CUDA(cudaMemcpyAsync(I.pp.ptr, I.pz.ptr, sizeof(double) * M, cudaMemcpyDeviceToDevice, st));
+                I.reduce_rows<1>(RedDot{I.r.ptr, I.pz.ptr}, I.redout.ptr);
+                rz = I.fetch(nlp);
+                int last_best_it = 0;
+                for (int it = 0; it < max_it; ++it) {
+                    ++I.refine_steps;
+                    normal_apply(I.pp.ptr, I.pq.ptr);
+                    I.reduce_rows<1>(RedDot{I.pp.ptr, I.pq.ptr}, I.redout.ptr);
+                    std::vector<double> pq = I.fetch(nlp);
+                    bool run = false;
+                    for (int k = 0; k < nlp; ++k) {
+                        al[k] = 0.0;
+                        if (done[k] || stag[k]) continue;
+                        if (!(pq[k] > 0.0) || !(rz[k] > 0.0) || !std::isfinite(pq[k])) { stag[k] = 1; continue; }
+                        al[k] = rz[k] / pq[k];
+                        run = true;
+                    }
+                    if (!run) break;
+                    I.put_scalars(1, al);
+                    k_axpy_lp<<<nblk(M), 256, 0, st>>>(M, d_ap, I.pp.ptr, I.row_lp.ptr, out);
+                    for (auto& v : al) v = -v;
+                    I.put_scalars(1, al);
+                    k_axpy_lp<<<nblk(M), 256, 0, st>>>(M, d_ap, I.pq.ptr, I.row_lp.ptr, I.r.ptr);
+                    K.apply_inverse(I.r.ptr, I.pz.ptr);
+                    I.reduce_rows<2>(RedRZ{I.r.ptr, I.pz.ptr}, I.redout.ptr);
+                    std::vector<double> h = I.fetch(static_cast<size_t>(nlp) * 2);
+                    bool improved = false;
+                    for (int k = 0; k < nlp; ++k) {
+                        imp[k] = 0.0;
+                        be[k] = 0.0;
+                        if (done[k] || stag[k]) continue;
+                        const double rnk = h[k * 2], rz2 = h[k * 2 + 1];
+                        if (rnk < best[k]) { best[k] = rnk; imp[k] = 1.0; improved = true; }
+                        if (rnk <= tol[k]) { done[k] = 1; continue; }
+                        if (!(rz2 > 0.0) || !std::isfinite(rz2)) { stag[k] = 1; continue; }
+                        be[k] = rz2 / rz[k];
+                        rz[k] = rz2;
+                    }
+                    if (improved) {
+                        last_best_it = it;
+                        I.put_scalars(4, imp);
+                        k_masked_copy<<<nblk(M), 256, 0, st>>>(M, out, I.row_lp.ptr, d_rmask, I.bak.ptr);
+                    }
+                    if (it - last_best_it > 8) break;   // no progress for a while
+                    I.put_scalars(2, be);
+                    k_xpby_lp<<<nblk(M), 256, 0, st>>>(M, I.pz.ptr, d_ad, I.row_lp.ptr, I.pp.ptr);
+                }
+                SK_CUDA(cudaMemcpyAsync(out, I.bak.ptr, sizeof(double) * M, cudaMemcpyDeviceToDevice, st));
+                rn = resid_norm(rhs, out);
+                I.last_pcg = last_best_it + 1;
+                if (o.verbose > 1)
+                    std::fprintf(stderr, "[sk]   pcg steps %d resid %.3e tol %.3e\n", last_best_it + 1, rn[0], tol[0]);
             }
         }
         ok.assign(nlp, 0);
         for (int k = 0; k < nlp; ++k) ok[k] = !I.active[k] || rn[k] <= tol[k];
     };
     // ---- factorisation with delta retries and the precision policy
+    // delta: the reference's 1e-9 x10 ladder in strict mode (src/cuda/kkt.cu:35, 665-669);
+    // otherwise 1e-12 x10 for FP64 fronts (a tighter preconditioner keeps PCG short
+    // once A Theta A^T is nearly singular) and 1e-7 x10 for FP32 fronts.
     auto factor = [&](bool want_fp32) -> bool {
-        double delta = want_fp32 ? 1e-7 : 1e-9;
-        for (int retry = 0; retry < 5; ++retry, delta *= 10.0) {
+        double delta = want_fp32 ? 1e-7 : (o.strict ? 1e-9 : 1e-12);
+        for (int retry = 0; retry < (o.strict ? 5 : 6); ++retry, delta *= 10.0) {
             ++I.factorizations;
             if (K.factor(I.theta.ptr, delta, want_fp32)) {
                 if (want_fp32) I.used_fp32 = true;
@@ -659,12 +765,15 @@ void DeviceIPM::run() {
         }
         return false;
     };
-    // ---- direction: solve for rkkt -> (dx, dy, ds) and verify; returns per LP validity
-    struct DirStats { std::vector<double> e1, e2, e3, rxs, rx, rs, xs, xds, dxs, dxds; };
-    auto direction = [&](double* dxo, double* dyo, double* dso, const double* rxs, std::vector<char>& ok,
-                         DirStats& ds_) {
+    // ---- direction: solve for rkkt -> (dx, dy, ds) and check it (mehrotra_device.cu:494-587).
+    // acc[k]: the solve met its tolerance and e1, e2, e3 <= 1e-8 (the reference's test);
+    // use[k]: the direction may be used (strict: acc; otherwise finite with e1, e2, e3 <= 1e-6).
+    struct DirStats { std::vector<double> e1, e2, e3, rx, rs, xs, xds, dxs, dxds; };
+    auto direction = [&](double* dxo, double* dyo, double* dso, const double* rxs, std::vector<char>& acc,
+                         std::vector<char>& use, DirStats& ds_) {
+        std::vector<char> solved;
         spmv(M, I.ga, I.a_rp.ptr, I.a_ci.ptr, I.a_v.ptr, I.v.ptr, EpiSub{I.rp.ptr, I.rkkt.ptr}, st);
-        solve(I.rkkt.ptr, dyo, ok);
+        solve(I.rkkt.ptr, dyo, solved);
         spmv(N, I.gt, I.t_rp.ptr, I.t_ci.ptr, I.t_v.ptr, dyo,
              EpiDsDx{I.rd.ptr, I.theta.ptr, rxs, I.x.ptr, I.s.ptr, dso, dxo, I.e2.ptr, I.e3.ptr}, st);
         spmv(M, I.ga, I.a_rp.ptr, I.a_ci.ptr, I.a_v.ptr, dxo, EpiAdd{I.rp.ptr, I.e1.ptr}, st);
@@ -684,10 +793,30 @@ void DeviceIPM::run() {
             ds_.dxs.push_back(q[7]);
             ds_.dxds.push_back(q[8]);
         }
-        std::vector<char> valid(nlp, 0);
-        for (int k = 0; k < nlp; ++k)
-            valid[k] = ok[k] && !(ds_.e1[k] > 1e-8 || ds_.e2[k] > 1e-8 || ds_.e3[k] > 1e-8);
-        ok = valid;
+        acc.assign(nlp, 0);
+        use.assign(nlp, 0);
+        if (o.verbose > 1)
+            for (int k = 0; k < nlp && k < 4; ++k)
+                if (I.active[k])
+                    std::fprintf(stderr, "[sk]   dir lp %d solved %d e1 %.2e e2 %.2e e3 %.2e ratio_x %.3e ratio_s %.3e tol %.2e %s\n",
+                                 k, (int)solved[k], ds_.e1[k], ds_.e2[k], ds_.e3[k], ds_.rx[k], ds_.rs[k], tol[k],
+                                 K.last_fp32() ? "fp32" : "fp64");
+        for (int k = 0; k < nlp; ++k) {
+            const double e = std::max(ds_.e1[k], std::max(ds_.e2[k], ds_.e3[k]));
+            const bool fin = std::isfinite(ds_.e1[k]) && std::isfinite(ds_.e2[k]) && std::isfinite(ds_.e3[k]) &&
+                             std::isfinite(ds_.rx[k]) && std::isfinite(ds_.rs[k]);
+            acc[k] = solved[k] && fin && e <= 1e-8;
+            use[k] = o.strict ? acc[k] : (fin && e <= 1e-6);
+        }
+    };
+    auto any_active_missing = [&](const std::vector<char>& v) {
+        for (int k = 0; k < nlp; ++k) if (I.active[k] && !v[k]) return true;
+        return false;
+    };
+    auto switch_to_fp64 = [&](int it) -> bool {
+        I.switched = true;
+        for (int k = 0; k < nlp; ++k) if (I.active[k] && I.res[k].switch_iteration < 0) I.res[k].switch_iteration = it;
+        return factor(false);
     };
 
     int iter = 0;
@@ -748,24 +877,26 @@ void DeviceIPM::run() {
         for (int k = 0; k < nlp; ++k) tol[k] = 1e-9 * std::max(1.0, nrp[k]);
         // ---------------- predictor
         DirStats pd;
-        std::vector<char> okp;
+        std::vector<char> acc_p, use_p;
+        bool fac_ok = true;
         for (int attempt = 0; attempt < 2; ++attempt) {
             k_rhs<<<nblk(N), 256, 0, st>>>(N, I.x.ptr, I.s.ptr, I.theta.ptr, I.rd.ptr, nullptr, nullptr, nullptr,
                                           I.col_lp.ptr, I.rxs.ptr, I.v.ptr);
-            direction(I.dxa.ptr, I.dya.ptr, I.dsa.ptr, I.rxs.ptr, okp, pd);
-            bool all_ok = true;
-            for (int k = 0; k < nlp; ++k) if (I.active[k] && !okp[k]) all_ok = false;
-            if (all_ok || !fp32) break;
-            // an FP32 solve missed its tolerance: switch to FP64 for the rest of the solve
-            I.switched = true;
-            for (int k = 0; k < nlp; ++k) if (I.active[k]) I.res[k].switch_iteration = iter;
+            direction(I.dxa.ptr, I.dya.ptr, I.dsa.ptr, I.rxs.ptr, acc_p, use_p, pd);
+            I.max_pcg_iter = I.last_pcg;
+            if (!fp32 || !any_active_missing(acc_p)) break;
+            // an FP32 direction missed the reference accuracy: FP64 factor from here on
             fp32 = false;
-            if (!factor(false)) break;
+            if (!(fac_ok = switch_to_fp64(iter))) break;
+        }
+        if (!fac_ok) {
+            for (int k = 0; k < nlp; ++k) if (I.active[k]) { I.res[k].status = SK_STATUS_ITERATION_LIMIT; I.active[k] = 0; }
+            break;
         }
         std::vector<double> sigmu(nlp, 0.0);
         for (int k = 0; k < nlp; ++k) {
             if (!I.active[k]) continue;
-            if (!okp[k]) { I.res[k].status = SK_STATUS_ITERATION_LIMIT; I.active[k] = 0; continue; }
+            if (!use_p[k]) { I.res[k].status = SK_STATUS_ITERATION_LIMIT; I.active[k] = 0; continue; }
             const double apa = std::min(1.0, pd.rx[k]), ada = std::min(1.0, pd.rs[k]);
             const double mua = (pd.xs[k] + ada * pd.xds[k] + apa * pd.dxs[k] + apa * ada * pd.dxds[k]) / nn[k];
             const double sigma = std::min(1.0, std::pow(std::max(0.0, mua) / std::max(1e-16, mu[k]), 3.0));
@@ -773,11 +904,22 @@ void DeviceIPM::run() {
         }
         // ---------------- corrector
         I.put_scalars(3, sigmu);
-        k_rhs<<<nblk(N), 256, 0, st>>>(N, I.x.ptr, I.s.ptr, I.theta.ptr, I.rd.ptr, I.dxa.ptr, I.dsa.ptr, d_tgt,
-                                      I.col_lp.ptr, I.rxs.ptr, I.v.ptr);
         DirStats cd;
-        std::vector<char> okc;
-        direction(I.dx.ptr, I.dy.ptr, I.ds.ptr, I.rxs.ptr, okc, cd);
+        std::vector<char> acc_c, okc;
+        for (int attempt = 0; attempt < 2; ++attempt) {
+            k_rhs<<<nblk(N), 256, 0, st>>>(N, I.x.ptr, I.s.ptr, I.theta.ptr, I.rd.ptr, I.dxa.ptr, I.dsa.ptr, d_tgt,
+                                          I.col_lp.ptr, I.rxs.ptr, I.v.ptr);
+            direction(I.dx.ptr, I.dy.ptr, I.ds.ptr, I.rxs.ptr, acc_c, okc, cd);
+            I.max_pcg_iter = std::max(I.max_pcg_iter, I.last_pcg);
+            if (!fp32 || !any_active_missing(acc_c)) break;
+            fp32 = false;
+            if (!switch_to_fp64(iter)) { okc.assign(nlp, 0); break; }
+        }
+        // FP32 fronts that needed many PCG steps are not worth keeping: FP64 from the next iteration
+        if (fp32 && I.max_pcg_iter > 20) {
+            I.switched = true;
+            for (int k = 0; k < nlp; ++k) if (I.active[k] && I.res[k].switch_iteration < 0) I.res[k].switch_iteration = iter + 1;
+        }
         const double eta = 0.995, armijo = 1e-4;
         std::vector<int> dir(nlp, 0), bt(nlp, 0);
         std::vector<char> decided(nlp, 1), accepted(nlp, 0);
@@ -803,8 +945,8 @@ void DeviceIPM::run() {
             k_rhs<<<nblk(N), 256, 0, st>>>(N, I.x.ptr, I.s.ptr, I.theta.ptr, I.rd.ptr, nullptr, nullptr, d_tgt,
                                           I.col_lp.ptr, I.crxs.ptr, I.v.ptr);
             DirStats cs;
-            std::vector<char> okz;
-            direction(I.cdx.ptr, I.cdy.ptr, I.cds.ptr, I.crxs.ptr, okz, cs);
+            std::vector<char> accz, okz;
+            direction(I.cdx.ptr, I.cdy.ptr, I.cds.ptr, I.crxs.ptr, accz, okz, cs);
             I.put_scalars(4, cm);
             k_masked_copy<<<nblk(N), 256, 0, st>>>(N, I.cdx.ptr, I.col_lp.ptr, d_rmask, I.dx.ptr);
             k_masked_copy<<<nblk(N), 256, 0, st>>>(N, I.cds.ptr, I.col_lp.ptr, d_rmask, I.ds.ptr);
@@ -847,6 +989,10 @@ void DeviceIPM::run() {
                                     std::isfinite(yn);
                 const bool positive = minx > 0.0 && mins > 0.0 && mun > 0.0 && stp > 0.0;
                 const bool progress = merit < merit0[k] && merit <= (1.0 - armijo * stp) * merit0[k];
+                if (o.verbose > 1 && k < 4)
+                    std::fprintf(stderr, "[sk]   trial lp %d dir %d bt %d ap %.3e ad %.3e merit %.6e -> %.6e minx %.2e mins %.2e %s\n",
+                                 k, dir[k], bt[k], ap[k], ad[k], merit0[k], merit, minx, mins,
+                                 !finite ? "non-finite" : !positive ? "positivity" : !progress ? "no-decrease" : "accept");
                 if (finite && positive && progress) { decided[k] = 1; accepted[k] = 1; continue; }
                 ap[k] *= 0.5;
                 ad[k] *= 0.5;

@@ -16,6 +16,8 @@
 namespace sankhya {
 namespace dev {
 
+struct PlanDev;
+
 class KktEngine {
 public:
     // The plan is copied into device memory; lp must stay alive.
@@ -50,27 +52,31 @@ private:
     void run_factor_levels(bool fp32);
     void run_solve_levels();
     struct Prof;
-    template <class T> void launch_factor(T* F, Prof* prof = nullptr);
-    template <class T> void launch_solve(const T* F, Prof* prof = nullptr);
+    template <class T> void launch_factor(T* F, T* Linv, Prof* prof = nullptr);
+    template <class T> void launch_solve(const T* F, const T* Linv, Prof* prof = nullptr);
+    void ensure_fronts(bool fp32);
+    PlanDev pd() const;
 
     ipm::FrontPlan plan_;
     const DeviceLP& lp_;
     cudaStream_t st_;
     Arena arena_;
     Arena f32_arena_, f64_arena_;
-    Slot<float> F32_;
-    Slot<double> F64_;
+    Slot<float> F32_, Linv32_;
+    Slot<double> F64_, Linv64_;
+    int64_t inv_size_ = 0;
+    std::vector<int> cb_level_off_, cb_level_tot_;
     // plan arrays
     Slot<int> sn_first_, sn_ncols_, sn_nrows_, sn_parent_, rows_, ea_map_, ch_ptr_, ch_list_, perm_;
     Slot<int64_t> sn_F_off_, sn_f_off_, sn_rows_off_, ea_off_;
-    Slot<int> step_items_, step_prefix_, round_items_, round_prefix_, level_sn_;
+    Slot<int> step_items_, step_prefix_, round_items_, round_prefix_, level_sn_, cb_prefix_;
+    Slot<int64_t> inv_off_;
     Slot<int64_t> slot_pos_, w_ptr_;
     Slot<int> slot_i_, slot_j_, w_col_;
     Slot<double> w_val_;
     // numeric work
-    Slot<double> D_, Mdiag_, zp_, xp_, fvec_, partial_, tn_, params_;
+    Slot<double> D_, Mdiag_, zp_, xp_, zsol_, fvec_, tn_, params_;
     Slot<int> err_;
-    int64_t max_partial_ = 0;
     bool fp32_ = false;
     int failed_sn_ = -1;
     const double* theta_bound_ = nullptr;

@@ -22,6 +22,7 @@ sk_options to_c(const MehrotraOptions& o) {
     c.verbose = o.verbose;
     c.mu_switch = o.mu_switch;
     c.ruiz_passes = o.ruiz_passes;
+    c.strict = o.strict;
     return c;
 }
 
