@@ -155,6 +155,18 @@ int sk_compute_symbolic(int m, int n, const int* row_ptrs, const int* col_idx, c
  * reference counterpart beyond compute_amd_ordering's role). */
 int sk_fill_ordering(int m, int n, const int* row_ptrs, const int* col_idx, int* P);
 
+/* Host-only analysis of one LP's normal matrix (no device needed): builds the
+ * multifrontal plan the solver would use and writes out[0..15] =
+ * {supernodes, levels, tile steps, extend-add rounds, stored factor entries,
+ *  factorisation flops (sum c_j^2), front storage entries, largest front rows,
+ *  supernodes with <= 64 columns, assembly slots, Khatri-Rao map entries,
+ *  dense front (0/1), ordering used, consistency check (1 = every normal-matrix
+ *  entry maps into its front and every front lists its own columns first),
+ *  solve launches per triangular solve, factor launches per factorisation}.
+ * Returns 16. No reference counterpart. */
+int sk_plan_stats(int m, int n, const int* col_ptrs, const int* row_idx, const double* vals, int ordering,
+                  double* out, int cap);
+
 /* ---- Device kernels exposed for parity tests (device pointers, stream may be NULL) ---- */
 /* y = alpha * A x + beta * y for CSR A (rows x ?). Replaces cusparseSpMV CSR FP64
  * (src/ipm/mehrotra_device.cu:512,603,635,936). */

@@ -274,6 +274,10 @@ int sk_kkt_solve_device(sk_kkt* k, double* d_rhs, double tol) {
         }
         SK_CUDA(cudaMemcpyAsync(d_rhs, k->out.ptr, sizeof(double) * m, cudaMemcpyDeviceToDevice, st));
         SK_CUDA(cudaStreamSynchronize(st));
+        if (E.solve_error()) {
+            api::set_error("triangular solve: a task timed out waiting for a dependency");
+            return SK_ERR_CUDA;
+        }
         return rn <= t ? SK_OK : SK_ERR_NUMERICAL;
     } catch (...) {
         return api::status_of_current_exception();
@@ -327,7 +331,7 @@ int sk_kkt_get_factor(sk_kkt* k, double* L_dense, double* D) {
             const int* R = p.rows.data() + p.sn_rows_off[s];
             for (int c = 0; c < K; ++c)
                 for (int r = c; r < N; ++r)
-                    L_dense[static_cast<size_t>(R[r]) * m + (f + c)] = F[p.sn_F_off[s] + r + static_cast<int64_t>(c) * N];
+                    L_dense[static_cast<size_t>(R[r]) * m + (f + c)] = F[p.sn_F_off[s] + r + static_cast<int64_t>(c) * p.sn_lda[s]];
         }
         if (D) {
             SK_CUDA(cudaMemcpyAsync(D, k->eng->diag_D(), sizeof(double) * m, cudaMemcpyDeviceToHost, k->st));

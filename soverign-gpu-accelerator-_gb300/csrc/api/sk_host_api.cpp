@@ -8,6 +8,7 @@
 #include "api/sk_error.hpp"
 #include "core/problem.hpp"
 #include "gen/lpgen.hpp"
+#include "ipm/front_plan.hpp"
 #include "ipm/symbolic.hpp"
 #include "parsers/mps_reader.hpp"
 #include "sankhya/sk_ipm.h"
@@ -226,6 +227,60 @@ int sk_compute_symbolic(int m, int n, const int* row_ptrs, const int* col_idx, c
         std::memcpy(L_row_ptrs, sym.L_pattern.row_ptrs.data(), sizeof(int) * static_cast<size_t>(m + 1));
         if (nnz > 0) std::memcpy(L_cols, sym.L_pattern.col_indices.data(), sizeof(int) * static_cast<size_t>(nnz));
         return nnz;
+    } catch (...) {
+        return -api::status_of_current_exception();
+    }
+}
+
+int sk_plan_stats(int m, int n, const int* col_ptrs, const int* row_idx, const double* vals, int ordering,
+                  double* out, int cap) {
+    api::clear_error();
+    if (!out || cap < 16 || m <= 0 || n <= 0 || !col_ptrs) return -SK_ERR_INVALID;
+    try {
+        core::Model md = core::Model::from_csc(m, n, col_ptrs, row_idx, vals, std::vector<double>(m, 0.0).data(),
+                                               std::vector<double>(n, 0.0).data());
+        core::CSRMatrix A = core::to_csr(md.A);
+        ipm::LpView v;
+        v.m = m; v.n = n;
+        v.col_ptrs = md.A.col_ptrs.data(); v.row_idx = md.A.row_indices.data(); v.vals = md.A.values.data();
+        ipm::FrontPlan p;
+        ipm::build_front_plan({v}, A, ordering, p);
+        int64_t maxrows = 0, small = 0;
+        for (int s = 0; s < p.ns; ++s) {
+            maxrows = std::max<int64_t>(maxrows, p.sn_nrows[s]);
+            small += p.sn_ncols[s] <= ipm::kTile;
+        }
+        // consistency: own columns first in each front, rows sorted, slots inside fronts
+        bool ok = true;
+        int64_t cols = 0;
+        for (int s = 0; s < p.ns && ok; ++s) {
+            const Index* R = p.rows.data() + p.sn_rows_off[s];
+            cols += p.sn_ncols[s];
+            for (Index q = 0; q < p.sn_ncols[s]; ++q) ok = ok && R[q] == p.sn_first[s] + q;
+            for (Index q = 1; q < p.sn_nrows[s]; ++q) ok = ok && R[q] > R[q - 1];
+        }
+        ok = ok && cols == p.M;
+        for (int64_t q = 0; q < p.nslots && ok; ++q) {
+            const int t = p.sn_of_col[p.slot_j[q]];
+            ok = p.slot_pos[q] >= p.sn_F_off[t] &&
+                 p.slot_pos[q] < p.sn_F_off[t] + static_cast<int64_t>(p.sn_lda[t]) * p.sn_nrows[t];
+        }
+        int64_t solve_launches = 0, factor_launches = 0;
+        for (int l = 0; l < p.nlevels; ++l) {
+            const int ns = p.step_level_ptr[l + 1] - p.step_level_ptr[l];
+            solve_launches += 1 + ns;
+            factor_launches += (p.round_level_ptr[l + 1] - p.round_level_ptr[l]);
+        }
+        for (const auto& st : p.steps) factor_launches += 1 + (st.trsm_tiles > 0) + (st.upd_tiles > 0);
+        const double vals16[16] = {static_cast<double>(p.ns), static_cast<double>(p.nlevels),
+                                   static_cast<double>(p.steps.size()), static_cast<double>(p.rounds.size()),
+                                   static_cast<double>(p.nnz_factor), p.flops_factor, static_cast<double>(p.F_size),
+                                   static_cast<double>(maxrows), static_cast<double>(small),
+                                   static_cast<double>(p.nslots), static_cast<double>(p.w_col.size()),
+                                   p.dense_mode ? 1.0 : 0.0, static_cast<double>(p.ordering_used), ok ? 1.0 : 0.0,
+                                   static_cast<double>(solve_launches), static_cast<double>(factor_launches)};
+        for (int q = 0; q < 16; ++q) out[q] = vals16[q];
+        return 16;
     } catch (...) {
         return -api::status_of_current_exception();
     }

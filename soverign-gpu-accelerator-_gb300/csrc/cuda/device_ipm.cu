@@ -747,6 +747,8 @@ void DeviceIPM::run() {
                     std::fprintf(stderr, "[sk]   pcg steps %d resid %.3e tol %.3e\n", last_best_it + 1, rn[0], tol[0]);
             }
         }
+        if (K.solve_error())
+            throw api::sk_exception(SK_ERR_CUDA, "triangular solve: a task timed out waiting for a dependency");
         ok.assign(nlp, 0);
         for (int k = 0; k < nlp; ++k) ok[k] = !I.active[k] || rn[k] <= tol[k];
     };

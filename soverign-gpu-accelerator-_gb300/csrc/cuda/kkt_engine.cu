@@ -22,6 +22,7 @@ struct PlanDev {
     const int* sn_first;
     const int* sn_ncols;
     const int* sn_nrows;
+    const int* sn_lda;
     const int64_t* F_off;
     const int64_t* f_off;
     const int64_t* rows_off;
@@ -125,7 +126,7 @@ __global__ void k_asm_cols_dense(int M, const int* __restrict__ rp, const int* _
     const int s = row_lp[j];
     const int first = pd.sn_first[s];
     const int N = pd.sn_nrows[s];
-    T* col = F + pd.F_off[s] + static_cast<int64_t>(j - first) * N - first;
+    T* col = F + pd.F_off[s] + static_cast<int64_t>(j - first) * pd.sn_lda[s] - first;
     const double dj = D[j];
     for (int q = rp[j]; q < rp[j + 1]; ++q) {
         const int k = ci[q];
@@ -143,66 +144,90 @@ __global__ void k_asm_cols_dense(int M, const int* __restrict__ rp, const int* _
 
 // Cholesky of the 64x64 diagonal tile of step k of one front, in the front's
 // precision T, plus the explicit inverse of the factored tile (used by the panel
-// solve and by both triangular solves), stored column-major in Linv. One warp:
-// lane l owns rows l and l+32 during the factorisation and columns l and l+32 of
-// the inverse, so no block-wide barrier is needed.
+// solve and by both triangular solves), stored column-major in Linv.
+// 256 threads on a shared tile: four threads per row share each rank-1 update,
+// four threads per column share each inverse substitution (shuffle-reduced);
+// loops stay rolled so the code is small. A partial tile is padded with the identity.
 template <class T>
-__global__ void __launch_bounds__(32) k_potrf(StepArgs a, const int* __restrict__ items, PlanDev pd, T* F,
-                                              T* __restrict__ Linv, const int64_t* __restrict__ inv_off,
-                                              int* err) {
+__global__ void __launch_bounds__(256) k_potrf(StepArgs a, const int* __restrict__ items, PlanDev pd, T* F,
+                                               T* __restrict__ Linv, const int64_t* __restrict__ inv_off,
+                                               int* err) {
     extern __shared__ __align__(16) unsigned char smraw[];
     T* A = reinterpret_cast<T*>(smraw);
-    T* Iv = A + T64 * LDS;
+    T* X = A + T64 * LDS;
+    T* rdiag = X + T64 * LDS;
+    T* col = rdiag + T64;                 // scaled column c, read by all rows
     const int s = items[a.item_off + blockIdx.x];
-    const int N = pd.sn_nrows[s], K = pd.sn_ncols[s];
+    const int K = pd.sn_ncols[s];
+    const int LD = pd.sn_lda[s];
     const int k0 = a.k * T64;
     const int w = min(T64, K - k0);
     T* Fs = F + pd.F_off[s];
-    const int lane = threadIdx.x;
-    for (int c = 0; c < w; ++c)
-        for (int r = lane; r < w; r += 32)
-            A[r * LDS + c] = r >= c ? Fs[(k0 + r) + static_cast<int64_t>(k0 + c) * N] : T(0);
-    __syncwarp();
-    const int r0 = lane, r1 = lane + 32;
-    for (int c = 0; c < w; ++c) {
-        T piv = A[c * LDS + c];
-        if (!(piv > T(0))) {
-            if (lane == 0 && atomicCAS(err, 0, 1) == 0) err[1] = s;
-            piv = T(1);
+    const int tid = threadIdx.x;
+#pragma unroll 4
+    for (int it = 0; it < 16; ++it) {
+        const int idx = tid + it * 256;
+        const int r = idx & 63, c = idx >> 6;
+        T x = T(0);
+        if (r < w && c < w && c <= r) x = Fs[(k0 + r) + static_cast<int64_t>(k0 + c) * LD];
+        else if (r == c) x = T(1);
+        A[r * LDS + c] = x;
+    }
+    auto pivot = [&](int c) {
+        T p = A[c * LDS + c];
+        if (!(p > T(0))) {
+            if (atomicCAS(err, 0, 1) == 0) err[1] = s;
+            p = T(1);
         }
-        const T d = sqrt(piv);
-        __syncwarp();
-        if (r0 > c && r0 < w) A[r0 * LDS + c] /= d;
-        if (r1 > c && r1 < w) A[r1 * LDS + c] /= d;
-        if (lane == (c & 31)) A[c * LDS + c] = d;
-        __syncwarp();
-        const T l0 = (r0 > c && r0 < w) ? A[r0 * LDS + c] : T(0);
-        const T l1 = (r1 > c && r1 < w) ? A[r1 * LDS + c] : T(0);
-        for (int cc = c + 1; cc < w; ++cc) {
-            const T lc = A[cc * LDS + c];
-            if (r0 >= cc && r0 < w) A[r0 * LDS + cc] -= l0 * lc;
-            if (r1 >= cc && r1 < w) A[r1 * LDS + cc] -= l1 * lc;
+        const T d = sqrt(p);
+        A[c * LDS + c] = d;
+        rdiag[c] = T(1) / d;
+    };
+    __syncthreads();
+    if (tid == 0) pivot(0);
+    __syncthreads();
+    const int rr = tid >> 2, part = tid & 3;
+    for (int c = 0; c < T64; ++c) {
+        if (tid < T64 && tid > c) {
+            const T l = A[tid * LDS + c] * rdiag[c];
+            A[tid * LDS + c] = l;
+            col[tid] = l;
         }
+        __syncthreads();
+        if (rr > c) {
+            const T l = col[rr];
+            T* Ar = A + rr * LDS;
+            for (int cc = c + 1 + part; cc <= rr; cc += 4) Ar[cc] -= l * col[cc];
+        }
+        __syncthreads();
+        if (tid == 0 && c + 1 < T64) pivot(c + 1);
+        __syncthreads();
+    }
+#pragma unroll 4
+    for (int it = 0; it < 16; ++it) {
+        const int idx = tid + it * 256;
+        const int r = idx & 63, c = idx >> 6;
+        if (r < w && c < w && c <= r) Fs[(k0 + r) + static_cast<int64_t>(k0 + c) * LD] = A[r * LDS + c];
+    }
+    // X = L^{-1}, column j by four threads: X(i,j) = (delta_ij - sum_{q=j}^{i-1} L(i,q) X(q,j)) / L(i,i)
+    const int j = tid >> 2;
+    for (int i = 0; i < T64; ++i) {
+        T acc = T(0);
+        if (i > j)
+            for (int q = j + part; q < i; q += 4) acc += A[i * LDS + q] * X[q * LDS + j];
+        acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+        acc += __shfl_xor_sync(0xffffffffu, acc, 2);
+        if (part == 0) X[i * LDS + j] = (i < j) ? T(0) : (((i == j) ? T(1) : T(0)) - acc) * rdiag[i];
         __syncwarp();
     }
-    // inverse: lane owns columns j0 = lane, j1 = lane + 32 of X = L^{-1}
-    for (int jj = 0; jj < 2; ++jj) {
-        const int j = lane + 32 * jj;
-        if (j >= w) continue;
-        for (int i = j; i < w; ++i) {
-            T acc = (i == j) ? T(1) : T(0);
-            for (int q = j; q < i; ++q) acc -= A[i * LDS + q] * Iv[q * LDS + j];
-            Iv[i * LDS + j] = acc / A[i * LDS + i];
-        }
-    }
-    __syncwarp();
+    __syncthreads();
     T* Li = Linv + inv_off[s] + static_cast<int64_t>(a.k) * T64 * T64;
-    for (int c = 0; c < T64; ++c)
-        for (int r = lane; r < T64; r += 32) {
-            const bool in = r < w && c < w && r >= c;
-            if (in) Fs[(k0 + r) + static_cast<int64_t>(k0 + c) * N] = A[r * LDS + c];
-            Li[r + c * T64] = in ? Iv[r * LDS + c] : T(0);
-        }
+#pragma unroll 4
+    for (int it = 0; it < 16; ++it) {
+        const int idx = tid + it * 256;
+        const int i = idx & 63, jj = idx >> 6;
+        Li[i + jj * T64] = (i < w && jj < w) ? X[i * LDS + jj] : T(0);
+    }
 }
 
 // Panel rows below the diagonal tile: X = B L_kk^{-T} = B Linv^T (a small GEMM).
@@ -217,6 +242,7 @@ __global__ void __launch_bounds__(256) k_trsm(StepArgs a, const int* __restrict_
     const int s = items[a.item_off + i];
     const int lt = blockIdx.x - prefix[a.tp_off + i];
     const int N = pd.sn_nrows[s], K = pd.sn_ncols[s];
+    const int LD = pd.sn_lda[s];
     const int k0 = a.k * T64;
     const int w = min(T64, K - k0);
     const int r0 = k0 + w + lt * T64;
@@ -227,7 +253,7 @@ __global__ void __launch_bounds__(256) k_trsm(StepArgs a, const int* __restrict_
     for (int idx = tid; idx < T64 * T64; idx += blockDim.x) Iv[idx] = Li[idx];
     for (int idx = tid; idx < T64 * T64; idx += blockDim.x) {
         const int r = idx & 63, c = idx >> 6;
-        B[c * T64 + r] = (r < nr && c < w) ? Fs[(r0 + r) + static_cast<int64_t>(k0 + c) * N] : T(0);
+        B[c * T64 + r] = (r < nr && c < w) ? Fs[(r0 + r) + static_cast<int64_t>(k0 + c) * LD] : T(0);
     }
     __syncthreads();
     // X[r][c] = sum_{q <= c} B[r][q] Linv[c][q]; thread: row r, 16 columns
@@ -244,11 +270,13 @@ __global__ void __launch_bounds__(256) k_trsm(StepArgs a, const int* __restrict_
 #pragma unroll
         for (int t = 0; t < 16; ++t) {
             const int c = cg * 16 + t;
-            if (c < w) Fs[(r0 + r) + static_cast<int64_t>(k0 + c) * N] = acc[t];
+            if (c < w) Fs[(r0 + r) + static_cast<int64_t>(k0 + c) * LD] = acc[t];
         }
 }
 
-// C(64x64) -= A_i (64 x w) A_j^T; 256 threads, 4x4 outputs each.
+// C(64x64) -= A_i (64 x w) A_j^T; 256 threads, 4x4 outputs each. The C tile is
+// read into registers and both panel tiles are staged with fully unrolled loads
+// before any arithmetic, so every global load of a thread is in flight at once.
 template <class T>
 __global__ void __launch_bounds__(256) k_update(StepArgs a, const int* __restrict__ items,
                                                 const int* __restrict__ prefix, PlanDev pd, T* F) {
@@ -261,6 +289,7 @@ __global__ void __launch_bounds__(256) k_update(StepArgs a, const int* __restric
     int ti, tj;
     tri_index(lt, ti, tj);
     const int N = pd.sn_nrows[s], K = pd.sn_ncols[s];
+    const int LD = pd.sn_lda[s];
     const int k0 = a.k * T64;
     const int w = min(T64, K - k0);
     const int t0 = k0 + w;
@@ -268,24 +297,38 @@ __global__ void __launch_bounds__(256) k_update(StepArgs a, const int* __restric
     const int nri = min(T64, N - ri0), ncj = min(T64, N - cj0);
     T* Fs = F + pd.F_off[s];
     const int tid = threadIdx.x;
-    for (int idx = tid; idx < T64 * T64; idx += blockDim.x) {
-        const int r = idx & (T64 - 1), kk = idx >> 6;
-        T va = T(0), vb = T(0);
-        if (kk < w) {
-            const int64_t cofs = static_cast<int64_t>(k0 + kk) * N;
-            if (r < nri) va = Fs[ri0 + r + cofs];
-            if (r < ncj) vb = Fs[cj0 + r + cofs];
+    const int tx = tid & 15, ty = tid >> 4;
+    T cv[4][4];
+#pragma unroll
+    for (int p = 0; p < 4; ++p)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int r = ty * 4 + q, c = tx * 4 + p;
+            const bool in = r < nri && c < ncj && (ti != tj || r >= c);
+            cv[q][p] = in ? Fs[(ri0 + r) + static_cast<int64_t>(cj0 + c) * LD] : T(0);
         }
-        As[kk * T64 + r] = va;
-        Bs[kk * T64 + r] = vb;
+    T va[16], vb[16];
+#pragma unroll
+    for (int it = 0; it < 16; ++it) {
+        const int idx = tid + it * 256;
+        const int r = idx & (T64 - 1), kk = idx >> 6;
+        const int64_t cofs = static_cast<int64_t>(k0 + kk) * LD;
+        va[it] = (kk < w && r < nri) ? Fs[ri0 + r + cofs] : T(0);
+        vb[it] = (kk < w && r < ncj) ? Fs[cj0 + r + cofs] : T(0);
+    }
+#pragma unroll
+    for (int it = 0; it < 16; ++it) {
+        const int idx = tid + it * 256;
+        As[idx] = va[it];
+        Bs[idx] = vb[it];
     }
     __syncthreads();
-    const int tx = tid & 15, ty = tid >> 4;
     T acc[4][4];
 #pragma unroll
     for (int q = 0; q < 4; ++q)
 #pragma unroll
         for (int p = 0; p < 4; ++p) acc[q][p] = T(0);
+#pragma unroll 4
     for (int kk = 0; kk < w; ++kk) {
         T av[4], bv[4];
 #pragma unroll
@@ -296,18 +339,13 @@ __global__ void __launch_bounds__(256) k_update(StepArgs a, const int* __restric
             for (int p = 0; p < 4; ++p) acc[q][p] += av[q] * bv[p];
     }
 #pragma unroll
-    for (int p = 0; p < 4; ++p) {
-        const int c = tx * 4 + p;
-        if (c >= ncj) continue;
+    for (int p = 0; p < 4; ++p)
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-            const int r = ty * 4 + q;
-            if (r >= nri) continue;
-            if (ti == tj && r < c) continue;
-            T* dst = Fs + (ri0 + r) + static_cast<int64_t>(cj0 + c) * N;
-            *dst = *dst - acc[q][p];
+            const int r = ty * 4 + q, c = tx * 4 + p;
+            if (r < nri && c < ncj && (ti != tj || r >= c))
+                Fs[(ri0 + r) + static_cast<int64_t>(cj0 + c) * LD] = cv[q][p] - acc[q][p];
         }
-    }
 }
 
 template <class T>
@@ -321,7 +359,6 @@ __global__ void k_extend_add(int item_off, int nitems, int prefix_off, const int
     const int Kc = pd.sn_ncols[c], Nc = pd.sn_nrows[c];
     const int u = Nc - Kc;
     const int p = pd.sn_parent[c];
-    const int Np = pd.sn_nrows[p];
     const T* Fc = F + pd.F_off[c];
     T* Fp = F + pd.F_off[p];
     const int* map = pd.ea_map + pd.ea_off[c];
@@ -330,8 +367,8 @@ __global__ void k_extend_add(int item_off, int nitems, int prefix_off, const int
     const int mr = map[rr];
     for (int cc = tj * 32 + threadIdx.y; cc < tj * 32 + 32 && cc < u; cc += blockDim.y) {
         if (rr < cc) continue;
-        const T v = Fc[(Kc + rr) + static_cast<int64_t>(Kc + cc) * Nc];
-        T* dst = Fp + mr + static_cast<int64_t>(map[cc]) * Np;
+        const T v = Fc[(Kc + rr) + static_cast<int64_t>(Kc + cc) * pd.sn_lda[c]];
+        T* dst = Fp + mr + static_cast<int64_t>(map[cc]) * pd.sn_lda[p];
         *dst = *dst + v;
     }
 }
@@ -360,6 +397,7 @@ __global__ void k_fwd_init(const int* __restrict__ level_sn, PlanDev pd, const T
                            T* __restrict__ fv) {
     const int s = level_sn[blockIdx.x];
     const int N = pd.sn_nrows[s], K = pd.sn_ncols[s], first = pd.sn_first[s];
+    const int LD = pd.sn_lda[s];
     T* f = fv + pd.f_off[s];
     for (int q = threadIdx.x; q < N; q += blockDim.x) f[q] = q < K ? zp[first + q] : T(0);
     __syncthreads();
@@ -373,136 +411,190 @@ __global__ void k_fwd_init(const int* __restrict__ level_sn, PlanDev pd, const T
     }
 }
 
-// Forward tile step: every block forms z = Linv f_blk; block 0 of a front stores
-// z, the others subtract L(rows, blk) z from their 64 rows below the block.
-template <class T>
-__global__ void __launch_bounds__(256) k_fwd_step(StepArgs a, const int* __restrict__ items,
-                                                  const int* __restrict__ prefix, PlanDev pd,
-                                                  const T* __restrict__ F, const T* __restrict__ Linv,
-                                                  const int64_t* __restrict__ inv_off, T* __restrict__ fv,
-                                                  T* __restrict__ zsol) {
-    __shared__ T fb[T64];
-    __shared__ T z[T64];
-    __shared__ T part[4][T64];
-    // block b -> (item i, tile lt) with 1 + trsm tiles per item
-    int lo = 0, hi = a.nitems - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (prefix[a.tp_off + mid] + mid <= static_cast<int>(blockIdx.x)) lo = mid; else hi = mid - 1;
+// ---- dependency-driven triangular solves -------------------------------------
+// Each front's rows are split into 64-row blocks; block i of front s is one task.
+// Tasks of a level are handed out in dependency order by an atomic counter, so a
+// task only ever waits for tasks that have already started; results are
+// published through per-block flags. Every wait is bounded: on time-out the task
+// sets *err and returns (the host checks *err and reports an error).
+
+constexpr int kSpinLimit = 1 << 24;
+
+__device__ __forceinline__ bool wait_flag(const int* flag, int target, int* err, int* abort_sh) {
+    int spins = 0;
+    while (*reinterpret_cast<const volatile int*>(flag) < target) {
+        if (*reinterpret_cast<const volatile int*>(err) != 0 || ++spins > kSpinLimit) {
+            atomicExch(err, 1);
+            *abort_sh = 1;
+            return false;
+        }
+        __nanosleep(40);
     }
-    const int i = lo;
-    const int lt = blockIdx.x - prefix[a.tp_off + i] - i;
-    const int s = items[a.item_off + i];
-    const int N = pd.sn_nrows[s], K = pd.sn_ncols[s], first = pd.sn_first[s];
-    const int k0 = a.k * T64;
-    const int w = min(T64, K - k0);
-    const T* Fs = F + pd.F_off[s];
-    const T* Li = Linv + inv_off[s] + static_cast<int64_t>(a.k) * T64 * T64;
-    T* f = fv + pd.f_off[s];
-    const int tid = threadIdx.x;
-    if (tid < T64) fb[tid] = tid < w ? f[k0 + tid] : T(0);
-    __syncthreads();
-    {   // z[c] = sum_{q <= c} Linv[c][q] fb[q]; 4 threads per c
-        const int c = tid >> 2, part4 = tid & 3;
-        T acc = T(0);
-        if (c < w)
-            for (int q = part4; q <= c; q += 4) acc += Li[c + q * T64] * fb[q];
-        acc += __shfl_xor_sync(0xffffffffu, acc, 1);
-        acc += __shfl_xor_sync(0xffffffffu, acc, 2);
-        if (part4 == 0 && c < T64) z[c] = c < w ? acc : T(0);
-    }
-    __syncthreads();
-    if (lt == 0) {
-        if (tid < w) zsol[first + k0 + tid] = z[tid];
-        return;
-    }
-    const int r0 = k0 + w + (lt - 1) * T64;
-    const int nr = min(T64, N - r0);
-    const int row = tid & 63, cg = tid >> 6;
-    T acc = T(0);
-    if (row < nr)
-        for (int c = cg * 16; c < cg * 16 + 16 && c < w; ++c)
-            acc += Fs[(r0 + row) + static_cast<int64_t>(k0 + c) * N] * z[c];
-    part[cg][row] = acc;
-    __syncthreads();
-    if (tid < nr) f[r0 + tid] -= (part[0][tid] + part[1][tid]) + (part[2][tid] + part[3][tid]);
+    __threadfence();
+    return true;
 }
 
-// Backward, external rows: f[c] = z[c] - sum_{r >= K} L(r, c) x(R[r]) for the own
-// columns c of one 64-column block (warp per 8 columns, lanes over rows).
 template <class T>
-__global__ void __launch_bounds__(256) k_bwd_ext(const int* __restrict__ level_sn, const int* __restrict__ cb_prefix,
-                                                 int nsn, PlanDev pd, const T* __restrict__ F,
-                                                 const T* __restrict__ xp, const T* __restrict__ zsol,
-                                                 T* __restrict__ fv) {
-    int lo = 0, hi = nsn - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (cb_prefix[mid] <= static_cast<int>(blockIdx.x)) lo = mid; else hi = mid - 1;
+__device__ __forceinline__ T ld_cg(const T* p) { return __ldcg(p); }
+
+// Forward: task (s, i). Own block i < nb covers rows [64 i, min(64 i + 64, K));
+// external block i >= nb covers rows [K + 64 (i - nb), ...) < N. The task forms
+// f_rows - sum_{j < min(i, nb)} L(rows, block j) z_j; an own block then stores
+// z_i = Linv_i (..) in zsol and flags 1, an external block stores the parent's
+// update vector in f.
+template <class T>
+__global__ void __launch_bounds__(256) k_fwd_tasks(const int2* __restrict__ tasks, int ntasks, int* counter,
+                                                   PlanDev pd, const T* __restrict__ F, const T* __restrict__ Linv,
+                                                   const int64_t* __restrict__ inv_off,
+                                                   const int* __restrict__ blk_off, int* flags, T* fv, T* zsol,
+                                                   int* err) {
+    __shared__ int task_sh, abort_sh;
+    __shared__ T zj[T64];
+    __shared__ T red[4][T64];
+    __shared__ T fb[T64];
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        task_sh = atomicAdd(counter, 1);
+        abort_sh = 0;
     }
-    const int s = level_sn[lo];
-    const int kb = blockIdx.x - cb_prefix[lo];
+    __syncthreads();
+    const int t = task_sh;
+    if (t >= ntasks) return;
+    const int s = tasks[t].x, i = tasks[t].y;
     const int N = pd.sn_nrows[s], K = pd.sn_ncols[s], first = pd.sn_first[s];
+    const int LD = pd.sn_lda[s];
+    const int nb = (K + T64 - 1) / T64;
+    const T* Fs = F + pd.F_off[s];
+    T* f = fv + pd.f_off[s];
+    int* fl = flags + blk_off[s];
+    const int r = tid & 63, cg = tid >> 6;
+    const bool own = i < nb;
+    const int row0 = own ? i * T64 : K + (i - nb) * T64;
+    const int rend = own ? K : N;
+    const int row = row0 + r;
+    const bool rv = row < rend;
+    T acc = T(0);
+    const int jmax = own ? i : nb;
+    for (int j = 0; j < jmax; ++j) {
+        if (tid == 0) wait_flag(fl + j, 1, err, &abort_sh);
+        __syncthreads();
+        if (abort_sh) return;
+        if (tid < T64) zj[tid] = (j * T64 + tid < K) ? ld_cg(zsol + first + j * T64 + tid) : T(0);
+        __syncthreads();
+        if (rv) {
+            const T* Lc = Fs + row + static_cast<int64_t>(j * T64 + cg * 16) * LD;
+#pragma unroll
+            for (int c = 0; c < 16; ++c)
+                if (j * T64 + cg * 16 + c < K) acc += Lc[static_cast<int64_t>(c) * LD] * zj[cg * 16 + c];
+        }
+        __syncthreads();
+    }
+    red[cg][r] = acc;
+    __syncthreads();
+    if (tid < T64) {
+        const int rw = row0 + tid;
+        fb[tid] = rw < rend ? f[rw] - ((red[0][tid] + red[1][tid]) + (red[2][tid] + red[3][tid])) : T(0);
+    }
+    __syncthreads();
+    if (own) {
+        const int w = min(T64, K - i * T64);
+        const T* Li = Linv + inv_off[s] + static_cast<int64_t>(i) * T64 * T64;
+        const int c = tid >> 2, part = tid & 3;
+        T z = T(0);
+        if (c < w)
+            for (int q = part; q <= c; q += 4) z += Li[c + q * T64] * fb[q];
+        z += __shfl_xor_sync(0xffffffffu, z, 1);
+        z += __shfl_xor_sync(0xffffffffu, z, 2);
+        if (part == 0 && c < w) zsol[first + i * T64 + c] = z;
+        __threadfence();
+        __syncthreads();
+        if (tid == 0) atomicExch(fl + i, 1);
+    } else {
+        if (tid < T64 && row0 + tid < N) f[row0 + tid] = fb[tid];
+    }
+}
+
+// Backward: task (s, i), i descending: x_i = Linv_i^T (z_i - sum_{rows r below
+// block i} L(r, block i)^T x_r); rows of own later blocks wait for their flag (2),
+// rows outside the front's columns come from ancestors (earlier levels).
+template <class T>
+__global__ void __launch_bounds__(256) k_bwd_tasks(const int2* __restrict__ tasks, int ntasks, int* counter,
+                                                   PlanDev pd, const T* __restrict__ F, const T* __restrict__ Linv,
+                                                   const int64_t* __restrict__ inv_off,
+                                                   const int* __restrict__ blk_off, int* flags, T* xp,
+                                                   const T* __restrict__ zsol, int* err) {
+    __shared__ int task_sh, abort_sh;
+    __shared__ T xb[T64];
+    __shared__ T tb[T64];
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        task_sh = atomicAdd(counter, 1);
+        abort_sh = 0;
+    }
+    __syncthreads();
+    const int t = task_sh;
+    if (t >= ntasks) return;
+    const int s = tasks[t].x, i = tasks[t].y;
+    const int N = pd.sn_nrows[s], K = pd.sn_ncols[s], first = pd.sn_first[s];
+    const int LD = pd.sn_lda[s];
+    const int nb = (K + T64 - 1) / T64;
+    const int w = min(T64, K - i * T64);
     const T* Fs = F + pd.F_off[s];
     const int* R = pd.rows + pd.rows_off[s];
-    T* f = fv + pd.f_off[s];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    for (int t = 0; t < 8; ++t) {
-        const int c = kb * T64 + wid * 8 + t;
-        if (c >= K) break;
-        double acc = 0.0;
-        for (int r = K + lane; r < N; r += 32)
-            acc += static_cast<double>(Fs[r + static_cast<int64_t>(c) * N]) * static_cast<double>(xp[R[r]]);
-        acc = warp_sum(acc);
-        if (lane == 0) f[c] = static_cast<T>(static_cast<double>(zsol[first + c]) - acc);
-    }
-}
-
-// Backward tile step k (descending): every block forms x = Linv^T f_blk; block 0
-// stores x, block j >= 1 subtracts L(blk rows, column block j-1)^T x from f.
-template <class T>
-__global__ void __launch_bounds__(256) k_bwd_step(StepArgs a, const int* __restrict__ items, PlanDev pd,
-                                                  const T* __restrict__ F, const T* __restrict__ Linv,
-                                                  const int64_t* __restrict__ inv_off, T* __restrict__ fv,
-                                                  T* __restrict__ xp) {
-    __shared__ T fb[T64];
-    __shared__ T x[T64];
-    const int per = a.k + 1;
-    const int i = blockIdx.x / per;
-    const int j = blockIdx.x % per;
-    const int s = items[a.item_off + i];
-    const int N = pd.sn_nrows[s], K = pd.sn_ncols[s], first = pd.sn_first[s];
-    const int k0 = a.k * T64;
-    const int w = min(T64, K - k0);
-    const T* Fs = F + pd.F_off[s];
-    const T* Li = Linv + inv_off[s] + static_cast<int64_t>(a.k) * T64 * T64;
-    T* f = fv + pd.f_off[s];
-    const int tid = threadIdx.x;
-    if (tid < T64) fb[tid] = tid < w ? f[k0 + tid] : T(0);
-    __syncthreads();
-    {   // x[c] = sum_{q >= c} Linv[q][c] fb[q]
-        const int c = tid >> 2, part4 = tid & 3;
-        T acc = T(0);
-        if (c < w)
-            for (int q = c + part4; q < w; q += 4) acc += Li[q + c * T64] * fb[q];
-        acc += __shfl_xor_sync(0xffffffffu, acc, 1);
-        acc += __shfl_xor_sync(0xffffffffu, acc, 2);
-        if (part4 == 0 && c < T64) x[c] = c < w ? acc : T(0);
-    }
-    __syncthreads();
-    if (j == 0) {
-        if (tid < w) xp[first + k0 + tid] = x[tid];
-        return;
-    }
-    const int cb = j - 1;                       // column block < k
+    int* fl = flags + blk_off[s];
     const int lane = tid & 31, wid = tid >> 5;
-    for (int t = 0; t < 8; ++t) {
-        const int c = cb * T64 + wid * 8 + t;   // c < k0 <= K
-        T acc = T(0);
-        for (int r = lane; r < w; r += 32) acc += Fs[(k0 + r) + static_cast<int64_t>(c) * N] * x[r];
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        if (lane == 0) f[c] -= acc;
+    T part[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) part[q] = T(0);
+    const int c0 = i * T64 + wid * 8;
+    // rows outside the front's own columns (solved by ancestors)
+    for (int r = K + lane; r < N; r += 32) {
+        const T xr = xp[R[r]];
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+            if (c0 + q < K) part[q] += Fs[r + static_cast<int64_t>(c0 + q) * LD] * xr;
     }
+    // rows of own later blocks: the oldest (already solved) first, the newest
+    // dependency (block i + 1) last, so the wavefront does not serialise
+    for (int j = nb - 1; j > i; --j) {
+        if (tid == 0) wait_flag(fl + j, 2, err, &abort_sh);
+        __syncthreads();
+        if (abort_sh) return;
+        if (tid < T64) xb[tid] = (j * T64 + tid < K) ? ld_cg(xp + first + j * T64 + tid) : T(0);
+        __syncthreads();
+        for (int rr = lane; rr < T64; rr += 32) {
+            const int r = j * T64 + rr;
+            if (r >= K) break;
+            const T xr = xb[rr];
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+                if (c0 + q < K) part[q] += Fs[r + static_cast<int64_t>(c0 + q) * LD] * xr;
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        T v = part[q];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) {
+            const int c = wid * 8 + q;
+            tb[c] = c < w ? zsol[first + i * T64 + c] - v : T(0);
+        }
+    }
+    __syncthreads();
+    {
+        const T* Li = Linv + inv_off[s] + static_cast<int64_t>(i) * T64 * T64;
+        const int c = tid >> 2, pq = tid & 3;
+        T x = T(0);
+        if (c < w)
+            for (int q = c + pq; q < w; q += 4) x += Li[q + c * T64] * tb[q];
+        x += __shfl_xor_sync(0xffffffffu, x, 1);
+        x += __shfl_xor_sync(0xffffffffu, x, 2);
+        if (pq == 0 && c < w) xp[first + i * T64 + c] = x;
+    }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) atomicExch(fl + i, 2);
 }
 
 // ------------------------------------------------------- normal-matrix apply
@@ -542,7 +634,7 @@ struct KktEngine::Prof {
 template <class T>
 static void set_smem_attrs() {
     SK_CUDA(cudaFuncSetAttribute(k_potrf<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 static_cast<int>(2 * T64 * LDS * sizeof(T))));
+                                 static_cast<int>((2 * T64 * LDS + 2 * T64) * sizeof(T))));
     SK_CUDA(cudaFuncSetAttribute(k_trsm<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  static_cast<int>(2 * T64 * T64 * sizeof(T))));
     SK_CUDA(cudaFuncSetAttribute(k_update<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -559,28 +651,42 @@ KktEngine::KktEngine(const ipm::FrontPlan& plan, const DeviceLP& lp, cudaStream_
         inv_off[s] = inv_size_;
         inv_size_ += static_cast<int64_t>((p.sn_ncols[s] + T64 - 1) / T64) * T64 * T64;
     }
-    std::vector<int> cbp;
-    cb_level_off_.assign(static_cast<size_t>(p.nlevels) + 1, 0);
-    cb_level_tot_.assign(static_cast<size_t>(p.nlevels), 0);
-    for (int l = 0; l < p.nlevels; ++l) {
-        cb_level_off_[l] = static_cast<int>(cbp.size());
-        int acc = 0;
-        for (int q = p.level_ptr[l]; q < p.level_ptr[l + 1]; ++q) {
-            cbp.push_back(acc);
-            acc += (p.sn_ncols[p.level_sn[q]] + T64 - 1) / T64;
-        }
-        cbp.push_back(acc);
-        cb_level_tot_[l] = acc;
+    // solve task lists per level (forward: row blocks ascending; backward: own
+    // column blocks descending) and per-front flag offsets
+    std::vector<int> blk_off(static_cast<size_t>(p.ns), 0);
+    nflags_ = 0;
+    for (int s = 0; s < p.ns; ++s) {
+        blk_off[s] = nflags_;
+        nflags_ += (p.sn_ncols[s] + T64 - 1) / T64;
     }
-    cb_level_off_[p.nlevels] = static_cast<int>(cbp.size());
+    std::vector<int2> ftask, btask;
+    fwd_task_off_.assign(static_cast<size_t>(p.nlevels) + 1, 0);
+    bwd_task_off_.assign(static_cast<size_t>(p.nlevels) + 1, 0);
+    for (int l = 0; l < p.nlevels; ++l) {
+        fwd_task_off_[l] = static_cast<int>(ftask.size());
+        bwd_task_off_[l] = static_cast<int>(btask.size());
+        for (int q = p.level_ptr[l]; q < p.level_ptr[l + 1]; ++q) {
+            const int s = p.level_sn[q];
+            const int nb = (p.sn_ncols[s] + T64 - 1) / T64;
+            const int neb = (p.sn_nrows[s] - p.sn_ncols[s] + T64 - 1) / T64;
+            for (int i = 0; i < nb + neb; ++i) ftask.push_back(make_int2(s, i));
+            for (int i = nb - 1; i >= 0; --i) btask.push_back(make_int2(s, i));
+        }
+    }
+    fwd_task_off_[p.nlevels] = static_cast<int>(ftask.size());
+    bwd_task_off_[p.nlevels] = static_cast<int>(btask.size());
     auto rsv = [&](auto& slot, const auto& vec) { reserve(arena_, slot, vec.size()); };
-    rsv(sn_first_, p.sn_first); rsv(sn_ncols_, p.sn_ncols); rsv(sn_nrows_, p.sn_nrows); rsv(sn_parent_, p.sn_parent);
+    rsv(sn_first_, p.sn_first); rsv(sn_ncols_, p.sn_ncols); rsv(sn_nrows_, p.sn_nrows); rsv(sn_lda_, p.sn_lda); rsv(sn_parent_, p.sn_parent);
     rsv(rows_, p.rows); rsv(ea_map_, p.ea_map); rsv(ch_ptr_, p.ch_ptr); rsv(ch_list_, p.ch_list);
     rsv(perm_, p.perm); rsv(sn_F_off_, p.sn_F_off); rsv(sn_f_off_, p.sn_f_off); rsv(sn_rows_off_, p.sn_rows_off);
     rsv(ea_off_, p.ea_off); rsv(step_items_, p.step_items); rsv(step_prefix_, p.step_prefix);
     rsv(round_items_, p.round_items); rsv(round_prefix_, p.round_prefix); rsv(level_sn_, p.level_sn);
     rsv(slot_pos_, p.slot_pos); rsv(w_ptr_, p.w_ptr); rsv(slot_i_, p.slot_i); rsv(slot_j_, p.slot_j);
-    rsv(w_col_, p.w_col); rsv(w_val_, p.w_val); rsv(inv_off_, inv_off); rsv(cb_prefix_, cbp);
+    rsv(w_col_, p.w_col); rsv(w_val_, p.w_val); rsv(inv_off_, inv_off); rsv(blk_off_, blk_off);
+    rsv(fwd_tasks_, ftask); rsv(bwd_tasks_, btask);
+    reserve(arena_, flags_, static_cast<size_t>(std::max(1, nflags_)));
+    reserve(arena_, counters_, static_cast<size_t>(2 * std::max(1, p.nlevels)));
+    reserve(arena_, solve_err_, 1);
     reserve(arena_, D_, static_cast<size_t>(p.M));
     reserve(arena_, Mdiag_, static_cast<size_t>(p.M));
     reserve(arena_, zp_, static_cast<size_t>(p.M));
@@ -592,12 +698,14 @@ KktEngine::KktEngine(const ipm::FrontPlan& plan, const DeviceLP& lp, cudaStream_
     reserve(arena_, err_, 2);
     arena_.commit();
     auto bnd = [&](auto& slot) { bind(arena_, slot); };
-    bnd(sn_first_); bnd(sn_ncols_); bnd(sn_nrows_); bnd(sn_parent_); bnd(rows_); bnd(ea_map_); bnd(ch_ptr_);
+    bnd(sn_first_); bnd(sn_ncols_); bnd(sn_nrows_); bnd(sn_lda_); bnd(sn_parent_); bnd(rows_); bnd(ea_map_); bnd(ch_ptr_);
     bnd(ch_list_); bnd(perm_); bnd(sn_F_off_); bnd(sn_f_off_); bnd(sn_rows_off_); bnd(ea_off_); bnd(step_items_);
     bnd(step_prefix_); bnd(round_items_); bnd(round_prefix_); bnd(level_sn_); bnd(slot_pos_); bnd(w_ptr_);
-    bnd(slot_i_); bnd(slot_j_); bnd(w_col_); bnd(w_val_); bnd(inv_off_); bnd(cb_prefix_); bnd(D_); bnd(Mdiag_);
+    bnd(slot_i_); bnd(slot_j_); bnd(w_col_); bnd(w_val_); bnd(inv_off_); bnd(blk_off_); bnd(fwd_tasks_);
+    bnd(bwd_tasks_); bnd(flags_); bnd(counters_); bnd(solve_err_); bnd(D_); bnd(Mdiag_);
     bnd(zp_); bnd(xp_); bnd(zsol_); bnd(fvec_); bnd(tn_); bnd(params_); bnd(err_);
     upload(sn_first_, p.sn_first, st_); upload(sn_ncols_, p.sn_ncols, st_); upload(sn_nrows_, p.sn_nrows, st_);
+    upload(sn_lda_, p.sn_lda, st_);
     upload(sn_parent_, p.sn_parent, st_); upload(rows_, p.rows, st_); upload(ea_map_, p.ea_map, st_);
     upload(ch_ptr_, p.ch_ptr, st_); upload(ch_list_, p.ch_list, st_); upload(perm_, p.perm, st_);
     upload(sn_F_off_, p.sn_F_off, st_); upload(sn_f_off_, p.sn_f_off, st_); upload(sn_rows_off_, p.sn_rows_off, st_);
@@ -605,7 +713,9 @@ KktEngine::KktEngine(const ipm::FrontPlan& plan, const DeviceLP& lp, cudaStream_
     upload(round_items_, p.round_items, st_); upload(round_prefix_, p.round_prefix, st_);
     upload(level_sn_, p.level_sn, st_); upload(slot_pos_, p.slot_pos, st_); upload(w_ptr_, p.w_ptr, st_);
     upload(slot_i_, p.slot_i, st_); upload(slot_j_, p.slot_j, st_); upload(w_col_, p.w_col, st_);
-    upload(w_val_, p.w_val, st_); upload(inv_off_, inv_off, st_); upload(cb_prefix_, cbp, st_);
+    upload(w_val_, p.w_val, st_); upload(inv_off_, inv_off, st_); upload(blk_off_, blk_off, st_);
+    upload(fwd_tasks_, ftask, st_); upload(bwd_tasks_, btask, st_);
+    SK_CUDA(cudaMemsetAsync(solve_err_.ptr, 0, sizeof(int), st_));
     SK_CUDA(cudaStreamSynchronize(st_));
     set_smem_attrs<float>();
     set_smem_attrs<double>();
@@ -619,7 +729,7 @@ KktEngine::~KktEngine() {
 }
 
 PlanDev KktEngine::pd() const {
-    return PlanDev{sn_first_.ptr, sn_ncols_.ptr, sn_nrows_.ptr, sn_F_off_.ptr, sn_f_off_.ptr, sn_rows_off_.ptr,
+    return PlanDev{sn_first_.ptr, sn_ncols_.ptr, sn_nrows_.ptr, sn_lda_.ptr, sn_F_off_.ptr, sn_f_off_.ptr, sn_rows_off_.ptr,
                    rows_.ptr, ea_off_.ptr, ea_map_.ptr, ch_ptr_.ptr, ch_list_.ptr, sn_parent_.ptr};
 }
 
@@ -653,8 +763,8 @@ void KktEngine::launch_factor(T* F, T* Linv, Prof* prof) {
             const auto& st = p.steps[q];
             StepArgs a{st.k, st.item_off, st.nitems, st.trsm_prefix_off, st.upd_prefix_off};
             run(1, [&] {
-                k_potrf<T><<<st.nitems, 32, 2 * T64 * LDS * sizeof(T), st_>>>(a, step_items_.ptr, pdv, F, Linv,
-                                                                              inv_off_.ptr, err_.ptr);
+                k_potrf<T><<<st.nitems, 256, (2 * T64 * LDS + 2 * T64) * sizeof(T), st_>>>(a, step_items_.ptr, pdv, F,
+                                                                                    Linv, inv_off_.ptr, err_.ptr);
             });
             if (st.trsm_tiles > 0)
                 run(2, [&] {
@@ -699,34 +809,34 @@ void KktEngine::launch_solve(const T* F, const T* Linv, Prof* prof) {
     T* xp = reinterpret_cast<T*>(xp_.ptr);
     T* zs = reinterpret_cast<T*>(zsol_.ptr);
     T* fv = reinterpret_cast<T*>(fvec_.ptr);
+    SK_CUDA(cudaMemsetAsync(flags_.ptr, 0, sizeof(int) * static_cast<size_t>(std::max(1, nflags_)), st_));
+    SK_CUDA(cudaMemsetAsync(counters_.ptr, 0, sizeof(int) * 2 * static_cast<size_t>(std::max(1, p.nlevels)), st_));
     for (int l = 0; l < p.nlevels; ++l) {
         const int nl = p.level_ptr[l + 1] - p.level_ptr[l];
-        run(5, [&] { k_fwd_init<T><<<nl, 256, 0, st_>>>(level_sn_.ptr + p.level_ptr[l], pdv, zp, fv); });
-        for (int q = p.step_level_ptr[l]; q < p.step_level_ptr[l + 1]; ++q) {
-            const auto& st = p.steps[q];
-            StepArgs a{st.k, st.item_off, st.nitems, st.trsm_prefix_off, st.upd_prefix_off};
-            run(5, [&] {
-                k_fwd_step<T><<<static_cast<int>(st.trsm_tiles) + st.nitems, 256, 0, st_>>>(
-                    a, step_items_.ptr, step_prefix_.ptr, pdv, F, Linv, inv_off_.ptr, fv, zs);
-            });
-        }
+        const int nt = fwd_task_off_[l + 1] - fwd_task_off_[l];
+        run(5, [&] {
+            k_fwd_init<T><<<nl, 256, 0, st_>>>(level_sn_.ptr + p.level_ptr[l], pdv, zp, fv);
+            k_fwd_tasks<T><<<nt, 256, 0, st_>>>(fwd_tasks_.ptr + fwd_task_off_[l], nt, counters_.ptr + l, pdv, F,
+                                                Linv, inv_off_.ptr, blk_off_.ptr, flags_.ptr, fv, zs,
+                                                solve_err_.ptr);
+        });
     }
     for (int l = p.nlevels - 1; l >= 0; --l) {
-        const int nl = p.level_ptr[l + 1] - p.level_ptr[l];
+        const int nt = bwd_task_off_[l + 1] - bwd_task_off_[l];
         run(6, [&] {
-            k_bwd_ext<T><<<cb_level_tot_[l], 256, 0, st_>>>(level_sn_.ptr + p.level_ptr[l],
-                                                            cb_prefix_.ptr + cb_level_off_[l], nl, pdv, F, xp, zs, fv);
+            k_bwd_tasks<T><<<nt, 256, 0, st_>>>(bwd_tasks_.ptr + bwd_task_off_[l], nt, counters_.ptr + p.nlevels + l,
+                                                pdv, F, Linv, inv_off_.ptr, blk_off_.ptr, flags_.ptr, xp, zs,
+                                                solve_err_.ptr);
         });
-        for (int q = p.step_level_ptr[l + 1] - 1; q >= p.step_level_ptr[l]; --q) {
-            const auto& st = p.steps[q];
-            StepArgs a{st.k, st.item_off, st.nitems, st.trsm_prefix_off, st.upd_prefix_off};
-            run(6, [&] {
-                k_bwd_step<T><<<st.nitems * (st.k + 1), 256, 0, st_>>>(a, step_items_.ptr, pdv, F, Linv, inv_off_.ptr,
-                                                                      fv, xp);
-            });
-        }
     }
     SK_CUDA(cudaGetLastError());
+}
+
+int KktEngine::solve_error() {
+    int h = 0;
+    SK_CUDA(cudaMemcpyAsync(&h, solve_err_.ptr, sizeof(int), cudaMemcpyDeviceToHost, st_));
+    SK_CUDA(cudaStreamSynchronize(st_));
+    return h;
 }
 
 void KktEngine::ensure_fronts(bool fp32) {

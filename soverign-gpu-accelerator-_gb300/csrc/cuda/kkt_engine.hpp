@@ -45,6 +45,9 @@ public:
     // Copies the factored fronts to the host (FP64) for inspection.
     std::vector<double> fronts_host();
     cudaStream_t stream() const { return st_; }
+    // Non-zero when a triangular-solve task gave up waiting for a dependency
+    // (synchronises). The solve result is then invalid.
+    int solve_error();
     // Work vectors of length N available to callers between calls.
     double* scratch_n() const { return tn_.ptr; }
 
@@ -65,11 +68,14 @@ private:
     Slot<float> F32_, Linv32_;
     Slot<double> F64_, Linv64_;
     int64_t inv_size_ = 0;
-    std::vector<int> cb_level_off_, cb_level_tot_;
+    std::vector<int> fwd_task_off_, bwd_task_off_;
+    int nflags_ = 0;
     // plan arrays
-    Slot<int> sn_first_, sn_ncols_, sn_nrows_, sn_parent_, rows_, ea_map_, ch_ptr_, ch_list_, perm_;
+    Slot<int> sn_first_, sn_ncols_, sn_nrows_, sn_lda_, sn_parent_, rows_, ea_map_, ch_ptr_, ch_list_, perm_;
     Slot<int64_t> sn_F_off_, sn_f_off_, sn_rows_off_, ea_off_;
-    Slot<int> step_items_, step_prefix_, round_items_, round_prefix_, level_sn_, cb_prefix_;
+    Slot<int> step_items_, step_prefix_, round_items_, round_prefix_, level_sn_, blk_off_, flags_, counters_,
+        solve_err_;
+    Slot<int2> fwd_tasks_, bwd_tasks_;
     Slot<int64_t> inv_off_;
     Slot<int64_t> slot_pos_, w_ptr_;
     Slot<int> slot_i_, slot_j_, w_col_;

@@ -188,14 +188,17 @@ static void build_schedule(FrontPlan& p) {
 static void finish_offsets(FrontPlan& p) {
     p.sn_F_off.assign(static_cast<size_t>(p.ns), 0);
     p.sn_f_off.assign(static_cast<size_t>(p.ns), 0);
+    p.sn_lda.assign(static_cast<size_t>(p.ns), 0);
     p.F_size = 0;
     p.f_size = 0;
     p.nnz_factor = 0;
     p.flops_factor = 0.0;
     for (int s = 0; s < p.ns; ++s) {
         const int64_t N = p.sn_nrows[s], K = p.sn_ncols[s];
+        const int64_t lda = (N + 3) & ~int64_t(3);
+        p.sn_lda[s] = static_cast<Index>(lda);
         p.sn_F_off[s] = p.F_size;
-        p.F_size += (N * N + 1) & ~int64_t(1);   // keep every front 16-byte aligned in FP64
+        p.F_size += lda * N;                      // multiple of 4 entries: fronts stay 16-byte aligned
         p.sn_f_off[s] = p.f_size;
         p.f_size += N;
         p.nnz_factor += N * K - K * (K - 1) / 2;
@@ -486,7 +489,7 @@ void build_front_plan(const std::vector<LpView>& lps, const core::CSRMatrix& A, 
         const Index* e = b + p.sn_nrows[t];
         const Index* it = std::lower_bound(b + (j - p.sn_first[t]), e, i);
         if (it == e || *it != i) throw std::runtime_error("front plan: M entry outside the factor structure");
-        return p.sn_F_off[t] + (it - b) + static_cast<int64_t>(j - p.sn_first[t]) * p.sn_nrows[t];
+        return p.sn_F_off[t] + (it - b) + static_cast<int64_t>(j - p.sn_first[t]) * p.sn_lda[t];
     };
     for (Index i = 0; i < p.M; ++i) {
         p.slot_i[i] = i;

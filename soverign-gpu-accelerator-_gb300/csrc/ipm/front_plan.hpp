@@ -4,7 +4,8 @@
 // is a forest. Columns of M are grouped into supernodes; supernode s owns the
 // permuted columns [first, first+ncols) and the sorted row structure R_s
 // (|R_s| = nrows, own columns first). Its frontal matrix F_s is a dense
-// nrows x nrows column-major block (lda = nrows) in one device buffer:
+// nrows x nrows column-major block (leading dimension lda = nrows rounded up to
+// a multiple of 4, so every column starts 16-byte aligned) in one device buffer:
 //   F_s[:, :ncols]           -> the factor panel L(R_s, cols(s)) after factorisation
 //   F_s[ncols:, ncols:]      -> the update matrix passed to the parent (extend-add)
 // Levels: leaves are level 0, a parent is one above its highest child. Every
@@ -67,7 +68,7 @@ struct FrontPlan {
     std::vector<Index> perm, iperm;        // perm[k] = batch row at elimination position k
 
     int ns = 0;
-    std::vector<Index> sn_first, sn_ncols, sn_nrows, sn_parent, sn_level, sn_lp, sn_of_col;
+    std::vector<Index> sn_first, sn_ncols, sn_nrows, sn_lda, sn_parent, sn_level, sn_lp, sn_of_col;
     std::vector<int64_t> sn_rows_off, sn_F_off, sn_f_off;  // f_off: frontal vectors of the solves
     std::vector<Index> rows;               // concatenated R_s (permuted ids)
     std::vector<int64_t> ea_off;           // per supernode, into ea_map (nrows-ncols entries)

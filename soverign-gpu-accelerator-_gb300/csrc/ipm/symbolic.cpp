@@ -165,6 +165,10 @@ void compute_symbolic_factorization(const core::CSRMatrix& A, const std::vector<
 // variable touched by pivot p is bounded by
 //   min(n_live - 1, d_old + |L_p \ i|, |A_i \ i| + |L_p \ i| + sum_{e in E_i, e != p} |L_e \ L_p|).
 // Elements whose members all lie in L_p are absorbed (aggressive absorption).
+// A_i is pruned of neighbours covered by the new element only on every 16th time
+// i is touched (and always before i is eliminated): between prunings |A_i| is an
+// over-count, which keeps the degree an upper bound, and variables touched by
+// many pivots (rows linking many blocks) stop costing O(|A_i|) per pivot.
 // Ties go to the most recently inserted variable of the minimum-degree bucket.
 std::vector<Index> fill_reducing_ordering(const core::CSRMatrix& A) {
     const Index m = A.rows;
@@ -196,6 +200,7 @@ std::vector<Index> fill_reducing_ordering(const core::CSRMatrix& A) {
     };
     for (Index i = m - 1; i >= 0; --i) insert(i);
     std::vector<Index> w(static_cast<size_t>(m), -1);   // |L_e \ L_p| scratch, -1 = unset
+    std::vector<unsigned char> touches(static_cast<size_t>(m), 0);
     std::vector<Index> inLp(static_cast<size_t>(m), -1);
     std::vector<Index> touched;
     Index mindeg = 0;
@@ -212,6 +217,7 @@ std::vector<Index> fill_reducing_ordering(const core::CSRMatrix& A) {
         Lp.clear();
         inLp[p] = p;
         for (Index v : Av[p]) if (!eliminated[v] && inLp[v] != p) { inLp[v] = p; Lp.push_back(v); }
+        // (A_p may still hold covered neighbours; they are de-duplicated by inLp)
         for (Index e : Ev[p]) {
             if (dead_elem[e]) continue;
             for (Index v : Le[e]) if (!eliminated[v] && inLp[v] != p) { inLp[v] = p; Lp.push_back(v); }
@@ -234,10 +240,13 @@ std::vector<Index> fill_reducing_ordering(const core::CSRMatrix& A) {
                 w[e] -= 1;
             }
             Ei.push_back(p);
-            auto& Ai = Av[i];
-            size_t t = 0;
-            for (Index v : Ai) if (!eliminated[v] && inLp[v] != p) Ai[t++] = v;
-            Ai.resize(t);
+            if (++touches[i] >= 16) {
+                touches[i] = 0;
+                auto& Ai = Av[i];
+                size_t t = 0;
+                for (Index v : Ai) if (!eliminated[v] && inLp[v] != p) Ai[t++] = v;
+                Ai.resize(t);
+            }
         }
         // Aggressive absorption of elements entirely inside L_p.
         for (Index e : touched)

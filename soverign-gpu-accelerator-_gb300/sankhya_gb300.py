@@ -70,6 +70,7 @@ def _declare(L):
     L.sk_lp_free.argtypes = [vp]
     L.sk_compute_amd_ordering.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _i32p]
     L.sk_fill_ordering.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _i32p]
+    L.sk_plan_stats.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p, C.c_int, _f64p, C.c_int]
     L.sk_compute_symbolic.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _i32p, _i32p, _i32p, _i32p, _i32p, C.c_int]
     if hasattr(L, "sk_ipm_solve_csc"):
         L.sk_ipm_solve_csc.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p, _f64p, _f64p, C.POINTER(Options),
@@ -194,6 +195,19 @@ def fill_ordering(m, n, rp, ci):
     P = np.zeros(m, dtype=np.int32)
     check(lib().sk_fill_ordering(m, n, rp, ci, P), "sk_fill_ordering")
     return P
+
+
+PLAN_KEYS = ["supernodes", "levels", "steps", "rounds", "nnz_factor", "flops_factor", "front_entries",
+             "max_front_rows", "small_supernodes", "slots", "khatri_rao_entries", "dense_front", "ordering_used",
+             "consistent", "solve_launches", "factor_launches"]
+
+
+def plan_stats(lp, ordering=ORDER_AUTO):
+    out = np.zeros(16)
+    n = lib().sk_plan_stats(lp.m, lp.n, lp.col_ptrs, lp.row_idx, lp.vals, ordering, out, 16)
+    if n < 0:
+        raise RuntimeError("sk_plan_stats failed (%d): %s" % (n, last_error()))
+    return dict(zip(PLAN_KEYS, out.tolist()))
 
 
 def symbolic(m, n, rp, ci, P, cap=None):
