@@ -30,6 +30,8 @@ struct MehrotraOptions {
     double mu_switch = 1e-6;
     int ruiz_passes = 10;
     int strict = 0;
+    double delta32 = 1e-8;
+    double delta64 = 1e-14;
 };
 
 struct MehrotraResult {

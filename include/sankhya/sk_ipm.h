@@ -63,6 +63,8 @@ typedef struct sk_options {
                            * miss first switches a mixed-precision solve to the FP64 factor; an FP64
                            * direction is then used when it is finite with e1, e2, e3 <= 1e-6, and the
                            * merit line search plus the exact stopping test decide progress. */
+    double delta32;       /* first regularisation of FP32 fronts (default 1e-8); x10 per failed attempt */
+    double delta64;       /* first regularisation of FP64 fronts (default 1e-14; strict mode uses 1e-9) */
 } sk_options;
 
 typedef struct sk_info {

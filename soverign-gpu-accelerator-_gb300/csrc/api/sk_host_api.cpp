@@ -86,6 +86,8 @@ void sk_options_default(sk_options* opt) {
     opt->mu_switch = 1e-6;
     opt->ruiz_passes = 10;
     opt->strict = 0;
+    opt->delta32 = 1e-8;
+    opt->delta64 = 1e-14;
 }
 
 int sk_lp_generate(int family, int instance, sk_lp** out) {

@@ -757,7 +757,7 @@ void DeviceIPM::run() {
     // otherwise 1e-12 x10 for FP64 fronts (a tighter preconditioner keeps PCG short
     // once A Theta A^T is nearly singular) and 1e-7 x10 for FP32 fronts.
     auto factor = [&](bool want_fp32) -> bool {
-        double delta = want_fp32 ? 1e-7 : (o.strict ? 1e-9 : 1e-12);
+        double delta = want_fp32 ? o.delta32 : (o.strict ? 1e-9 : o.delta64);
         for (int retry = 0; retry < (o.strict ? 5 : 6); ++retry, delta *= 10.0) {
             ++I.factorizations;
             if (K.factor(I.theta.ptr, delta, want_fp32)) {

@@ -23,6 +23,8 @@ sk_options to_c(const MehrotraOptions& o) {
     c.mu_switch = o.mu_switch;
     c.ruiz_passes = o.ruiz_passes;
     c.strict = o.strict;
+    c.delta32 = o.delta32;
+    c.delta64 = o.delta64;
     return c;
 }
 

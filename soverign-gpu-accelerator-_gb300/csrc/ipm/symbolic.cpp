@@ -169,6 +169,10 @@ void compute_symbolic_factorization(const core::CSRMatrix& A, const std::vector<
 // i is touched (and always before i is eliminated): between prunings |A_i| is an
 // over-count, which keeps the degree an upper bound, and variables touched by
 // many pivots (rows linking many blocks) stop costing O(|A_i|) per pivot.
+// Variables whose degree exceeds four times the current minimum are updated
+// lazily: between refreshes (every 16th touch) they skip the |L_e \ L_p| scan and
+// keep their degree; skipped decrements only over-estimate the other degrees.
+// A lazily kept variable popped as pivot is re-scored first.
 // Ties go to the most recently inserted variable of the minimum-degree bucket.
 std::vector<Index> fill_reducing_ordering(const core::CSRMatrix& A) {
     const Index m = A.rows;
@@ -200,14 +204,32 @@ std::vector<Index> fill_reducing_ordering(const core::CSRMatrix& A) {
     };
     for (Index i = m - 1; i >= 0; --i) insert(i);
     std::vector<Index> w(static_cast<size_t>(m), -1);   // |L_e \ L_p| scratch, -1 = unset
-    std::vector<unsigned char> touches(static_cast<size_t>(m), 0);
+    std::vector<unsigned char> touches(static_cast<size_t>(m), 0), lazy_count(static_cast<size_t>(m), 0);
+    std::vector<char> lazy(static_cast<size_t>(m), 0), stale(static_cast<size_t>(m), 0);
     std::vector<Index> inLp(static_cast<size_t>(m), -1);
     std::vector<Index> touched;
     Index mindeg = 0;
     Index live = m;
     for (Index k = 0; k < m; ++k) {
-        while (mindeg <= m && head[mindeg] == -1) ++mindeg;
-        const Index p = head[mindeg];   // most recently inserted of the minimum bucket
+        Index p;
+        for (;;) {
+            while (mindeg <= m && head[mindeg] == -1) ++mindeg;
+            p = head[mindeg];   // most recently inserted of the minimum bucket
+            if (!stale[p]) break;
+            // lazily kept degree: recompute the bound |A_p| + sum_e (|L_e| - 1)
+            stale[p] = 0;
+            Index d = 0;
+            auto& Ep = Ev[p];
+            size_t o = 0;
+            for (Index e : Ep) if (!dead_elem[e]) { Ep[o++] = e; d += static_cast<Index>(Le[e].size()) - 1; }
+            Ep.resize(o);
+            d += static_cast<Index>(Av[p].size());
+            d = std::max<Index>(0, std::min<Index>(d, live - 1));
+            if (d <= mindeg) break;
+            remove(p);
+            deg[p] = d;
+            insert(p);
+        }
         remove(p);
         eliminated[p] = 1;
         order.push_back(p);
@@ -230,8 +252,11 @@ std::vector<Index> fill_reducing_ordering(const core::CSRMatrix& A) {
         const Index lp_size = static_cast<Index>(Lp.size());
         // Update E_i, prune A_i, compute |L_e \ L_p|.
         touched.clear();
+        const Index lazy_thr = std::max<Index>(64, 4 * std::max<Index>(1, mindeg));
         for (Index i : Lp) {
             auto& Ei = Ev[i];
+            lazy[i] = deg[i] > lazy_thr && (++lazy_count[i] & 15) != 0;
+            if (lazy[i]) { Ei.push_back(p); stale[i] = 1; continue; }
             size_t o = 0;
             for (Index e : Ei) if (!dead_elem[e] && e != p) Ei[o++] = e;
             Ei.resize(o);
@@ -252,6 +277,8 @@ std::vector<Index> fill_reducing_ordering(const core::CSRMatrix& A) {
         for (Index e : touched)
             if (w[e] == 0) { dead_elem[e] = 1; Le[e].clear(); }
         for (Index i : Lp) {
+            if (lazy[i]) continue;
+            stale[i] = 0;
             Index ext = 0;
             Index d = static_cast<Index>(Av[i].size()) + (lp_size - 1);
             auto& Ei = Ev[i];

@@ -27,7 +27,8 @@ _f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 class Options(C.Structure):
     _fields_ = [("precision", C.c_int), ("start", C.c_int), ("criteria", C.c_int), ("tol", C.c_double),
                 ("max_iter", C.c_int), ("ordering", C.c_int), ("verbose", C.c_int),
-                ("mu_switch", C.c_double), ("ruiz_passes", C.c_int), ("strict", C.c_int)]
+                ("mu_switch", C.c_double), ("ruiz_passes", C.c_int), ("strict", C.c_int),
+                ("delta32", C.c_double), ("delta64", C.c_double)]
 
 
 class Info(C.Structure):
