@@ -466,7 +466,7 @@ void oracle_kkt_measures(int m, int n, const int* cp, const int* ri, const doubl
 int oracle_ipm_solve(int m, int n, const int* cp, const int* ri, const double* va0,
                      const double* b0, const double* c0, const oracle_ipm_opts* o,
                      double* x_out, double* y_out, double* s_out, oracle_ipm_result* res) {
-    oracle_ipm_opts opts = {0, 1e-8, 200, 0, 0};
+    oracle_ipm_opts opts = {0, 1e-8, 200, 0, 0, 0};
     if (o) opts = *o;
     g_verbose = opts.verbose > 1;
     g_strict = opts.strict;
@@ -526,6 +526,26 @@ int oracle_ipm_solve(int m, int n, const int* cp, const int* ri, const double* v
     for (int j = 0; j < n; ++j) { x[j] = 1.0; s[j] = 1.0; }
     kkt_ctx k;
     kkt_init(&k, m);
+    if (opts.start == 1) {
+        /* Mehrotra's start (Mehrotra 1992): x~ = A^T (A A^T)^{-1} b, y = (A A^T)^{-1} A c,
+         * s~ = c - A^T y, shifted to positivity and then balanced by x^T s. */
+        for (int j = 0; j < n; ++j) w.theta[j] = 1.0;
+        form_normal_matrix(m, p.rp, p.ci, p.rv, w.theta, k.M0);
+        int dummy = 0;
+        normal_solve(&p, &k, w.theta, b, 1e-12 * (1.0 + norm_inf(m, b)), w.dy, &dummy);
+        spmv_At(&p, w.dy, x);
+        spmv_A(&p, c, w.rkkt);
+        normal_solve(&p, &k, w.theta, w.rkkt, 1e-12 * (1.0 + norm_inf(m, w.rkkt)), y, &dummy);
+        spmv_At(&p, y, s);
+        for (int j = 0; j < n; ++j) s[j] = c[j] - s[j];
+        double mx = 1e300, ms = 1e300;
+        for (int j = 0; j < n; ++j) { if (x[j] < mx) mx = x[j]; if (s[j] < ms) ms = s[j]; }
+        const double dx = fmax(-1.5 * mx, 0.0), dsv = fmax(-1.5 * ms, 0.0);
+        double xs = 0.0, sx = 0.0, ss = 0.0;
+        for (int j = 0; j < n; ++j) { x[j] += dx; s[j] += dsv; xs += x[j] * s[j]; sx += x[j]; ss += s[j]; }
+        const double hx = 0.5 * xs / ss, hs = 0.5 * xs / sx;
+        for (int j = 0; j < n; ++j) { x[j] += hx; s[j] += hs; if (!(x[j] > 0.0)) x[j] = 1.0; if (!(s[j] > 0.0)) s[j] = 1.0; }
+    }
 
     oracle_ipm_result r;
     memset(&r, 0, sizeof(r));

@@ -50,6 +50,7 @@ typedef struct oracle_ipm_opts {
     double tol;        /* tolerance of criteria 0 */
     int max_iter;      /* reference: 200 */
     int verbose;
+    int start;         /* 0: x = s = 1, y = 0 (reference :93-102); 1: Mehrotra's heuristic start */
     int strict;        /* 1: a missed solve tolerance or direction check ends the solve with
                         * IterationLimit (reference :793-797, :814-822); 0: the direction is
                         * used when finite with e1, e2, e3 <= 1e-6 (the stopping test and the

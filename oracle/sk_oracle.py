@@ -21,7 +21,7 @@ _f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 
 class IpmOpts(C.Structure):
     _fields_ = [("criteria", C.c_int), ("tol", C.c_double), ("max_iter", C.c_int), ("verbose", C.c_int),
-                ("strict", C.c_int)]
+                ("start", C.c_int), ("strict", C.c_int)]
 
 
 class IpmResult(C.Structure):
@@ -105,8 +105,8 @@ def kkt_solve(m, n, rp, ci, vals, theta, rhs, P=None, tol=1e-10, rel=True):
     return bool(ok), dy
 
 
-def ipm_solve(lp, criteria=0, tol=1e-8, max_iter=200, verbose=0, strict=0):
-    o = IpmOpts(criteria, tol, max_iter, verbose, strict)
+def ipm_solve(lp, criteria=0, tol=1e-8, max_iter=200, verbose=0, strict=0, start=0):
+    o = IpmOpts(criteria, tol, max_iter, verbose, start, strict)
     x = np.zeros(lp.n)
     y = np.zeros(lp.m)
     s = np.zeros(lp.n)

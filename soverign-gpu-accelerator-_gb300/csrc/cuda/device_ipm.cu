@@ -286,6 +286,38 @@ __global__ void k_masked_add(int n, const double* __restrict__ src, const int* _
     if (i < n && mask[lp_of[i]] != 0.0) dst[i] += src[i];
 }
 
+// s = c - t (t = A^T y); used by the heuristic start
+__global__ void k_sub(int n, const double* __restrict__ c, const double* __restrict__ t, double* __restrict__ out) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < n) out[j] = c[j] - t[j];
+}
+// v = max(v + shift[lp], tiny) with the shift per LP
+__global__ void k_shift_lp(int n, const double* __restrict__ shift, const int* __restrict__ lp_of,
+                           double* __restrict__ v) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < n) {
+        const double t = v[j] + shift[lp_of[j]];
+        v[j] = t > 1e-10 ? t : 1e-10;
+    }
+}
+struct RedMin2 {         // [min a, min b]
+    const double *a, *b;
+    __device__ static constexpr int op(int) { return OP_MIN; }
+    __device__ void operator()(int i, double* v) const {
+        v[0] = a[i];
+        v[1] = b[i];
+    }
+};
+struct RedStart {        // [sum x s, sum x, sum s]
+    const double *x, *s;
+    __device__ static constexpr int op(int) { return OP_SUM; }
+    __device__ void operator()(int j, double* v) const {
+        v[0] = x[j] * s[j];
+        v[1] = x[j];
+        v[2] = s[j];
+    }
+};
+
 // y += a[lp] * x
 __global__ void k_axpy_lp(int n, const double* __restrict__ a, const double* __restrict__ x,
                           const int* __restrict__ lp_of, double* __restrict__ y) {
@@ -354,6 +386,7 @@ struct DeviceIPM::Impl {
     int ga = 4, gt = 4;
 
     double* sc(int which) { return scal.ptr + static_cast<size_t>(which) * nlp; }
+    double* tmpn() { return crxs.ptr; }   // scratch n-vector outside the backtracking phase
     void put_scalars(int which, const std::vector<double>& v) {
         SK_CUDA(cudaMemcpyAsync(sc(which), v.data(), sizeof(double) * nlp, cudaMemcpyHostToDevice, st));
     }
@@ -609,7 +642,7 @@ void DeviceIPM::run() {
         SK_CUDA(cudaMemcpyAsync(I.s.ptr, I.hs0.data(), sizeof(double) * N, cudaMemcpyHostToDevice, st));
         for (int k = 0; k < nlp; ++k) I.res[k].learned_start = I.user_start[k];
     }
-    std::vector<double> nrp(nlp), nrd(nlp), mu(nlp), nm(nlp), nn(nlp);
+    std::vector<double> nrp(nlp, 1.0), nrd(nlp, 1.0), mu(nlp), nm(nlp), nn(nlp);
     for (int k = 0; k < nlp; ++k) {
         nm[k] = I.row_off[k + 1] - I.row_off[k];
         nn[k] = I.col_off[k + 1] - I.col_off[k];
@@ -820,6 +853,46 @@ void DeviceIPM::run() {
         for (int k = 0; k < nlp; ++k) if (I.active[k] && I.res[k].switch_iteration < 0) I.res[k].switch_iteration = it;
         return factor(false);
     };
+
+    if (o.start == SK_START_MEHROTRA) {
+        // Mehrotra's heuristic start in the scaled space: x~ = A^T (A A^T)^{-1} b,
+        // y = (A A^T)^{-1} A c, s~ = c - A^T y; x, s shifted to positivity by
+        // max(-1.5 min, 0) and then by 1/2 x^T s / sum(s), 1/2 x^T s / sum(x).
+        std::vector<double> one(nlp, 1.0);
+        I.put_scalars(0, one);
+        k_fill<<<nblk(N), 256, 0, st>>>(N, I.theta.ptr, 1.0);
+        const bool f32 = o.precision == SK_PREC_MIXED;
+        if (!factor(f32) && !(f32 && factor(false)))
+            throw api::sk_exception(SK_ERR_NUMERICAL, "heuristic start: A A^T could not be factored");
+        for (int k = 0; k < nlp; ++k) tol[k] = 1e-10;
+        std::vector<char> ok;
+        solve(I.b.ptr, I.dy.ptr, ok);
+        spmv(N, I.gt, I.t_rp.ptr, I.t_ci.ptr, I.t_v.ptr, I.dy.ptr, EpiAxpby{1.0, 0.0, I.x.ptr}, st);
+        spmv(M, I.ga, I.a_rp.ptr, I.a_ci.ptr, I.a_v.ptr, I.c.ptr, EpiAxpby{1.0, 0.0, I.rkkt.ptr}, st);
+        solve(I.rkkt.ptr, I.y.ptr, ok);
+        spmv(N, I.gt, I.t_rp.ptr, I.t_ci.ptr, I.t_v.ptr, I.y.ptr, EpiAxpby{1.0, 0.0, I.tmpn()}, st);
+        k_sub<<<nblk(N), 256, 0, st>>>(N, I.c.ptr, I.tmpn(), I.s.ptr);
+        I.reduce_cols<2>(RedMin2{I.x.ptr, I.s.ptr}, I.redout.ptr);
+        std::vector<double> h = I.fetch(static_cast<size_t>(nlp) * 2);
+        std::vector<double> sx(nlp), ss(nlp);
+        for (int k = 0; k < nlp; ++k) { sx[k] = std::max(-1.5 * h[2 * k], 0.0); ss[k] = std::max(-1.5 * h[2 * k + 1], 0.0); }
+        I.put_scalars(1, sx);
+        I.put_scalars(2, ss);
+        k_shift_lp<<<nblk(N), 256, 0, st>>>(N, d_ap, I.col_lp.ptr, I.x.ptr);
+        k_shift_lp<<<nblk(N), 256, 0, st>>>(N, d_ad, I.col_lp.ptr, I.s.ptr);
+        I.reduce_cols<3>(RedStart{I.x.ptr, I.s.ptr}, I.redout.ptr);
+        h = I.fetch(static_cast<size_t>(nlp) * 3);
+        for (int k = 0; k < nlp; ++k) {
+            const double xs = h[3 * k], sumx = h[3 * k + 1], sums = h[3 * k + 2];
+            sx[k] = std::isfinite(xs) && sums > 0 ? 0.5 * xs / sums : 1.0;
+            ss[k] = std::isfinite(xs) && sumx > 0 ? 0.5 * xs / sumx : 1.0;
+        }
+        I.put_scalars(1, sx);
+        I.put_scalars(2, ss);
+        k_shift_lp<<<nblk(N), 256, 0, st>>>(N, d_ap, I.col_lp.ptr, I.x.ptr);
+        k_shift_lp<<<nblk(N), 256, 0, st>>>(N, d_ad, I.col_lp.ptr, I.s.ptr);
+        SK_CUDA(cudaGetLastError());
+    }
 
     int iter = 0;
     std::vector<double> hm, hn;

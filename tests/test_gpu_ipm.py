@@ -140,3 +140,19 @@ def test_non_finite_input_rejected(gpu):
     bad = sk.LP(lp.m, lp.n, lp.col_ptrs, lp.row_idx, lp.vals, lp.b, c)
     with pytest.raises(RuntimeError, match="code 1"):
         sk.solve(bad)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("case", golden(), ids=lambda c: c["name"])
+def test_mehrotra_start_reaches_reference_objective(gpu, oracle, case, precision):
+    # Mehrotra's heuristic start (SK_START_MEHROTRA) changes the path, not the answer.
+    sk = gpu
+    lp = make_case(sk, case["name"])
+    info, x, y, s = sk.solve(lp, precision=precision, start=1)
+    assert info["status"] == 0, info
+    ref = case["ref_objective"]
+    assert abs(info["objective"] - ref) / (1 + abs(ref)) <= TOL
+    meas = oracle.kkt_measures(lp, x, y, s)
+    assert meas["rel_pinf"] <= TOL and meas["rel_dinf"] <= TOL and meas["rel_gap"] <= TOL
+    o, _, _, _ = oracle.ipm_solve(lp, start=1)
+    assert o["status"] == 0 and abs(info["iterations"] - o["iterations"]) <= 2

@@ -144,3 +144,15 @@ def test_oracle_objective_matches_reference_build(sk, oracle):
     r, x, y, s = oracle.ipm_solve(lp)
     assert st == 0 and r["status"] == 0
     assert abs(r["objective"] - obj) / (1 + abs(obj)) <= 1e-8
+
+
+@pytest.mark.parametrize("case", golden_cases(), ids=lambda c: c["name"])
+def test_oracle_mehrotra_start_matches_reference_simplex(sk, oracle, case):
+    lp = make_case(sk, case["name"])
+    r, x, y, s = oracle.ipm_solve(lp, start=1)
+    r0, _, _, _ = oracle.ipm_solve(lp)
+    assert r["status"] == 0
+    ref = case["ref_objective"]
+    assert abs(r["objective"] - ref) / (1 + abs(ref)) <= 1e-8
+    assert max(r["rel_pinf"], r["rel_dinf"], r["rel_gap"]) <= 1e-8
+    assert r["iterations"] <= r0["iterations"] + 2
