@@ -169,6 +169,24 @@ int sk_fill_ordering(int m, int n, const int* row_ptrs, const int* col_idx, int*
 int sk_plan_stats(int m, int n, const int* col_ptrs, const int* row_idx, const double* vals, int ordering,
                   double* out, int cap);
 
+/* ---- Allocation-free small KKT solve ----
+ * No counterpart in the reference. Solves (A diag(theta) A^T) dy = rhs in place
+ * (FP64, same regularisation ladder, refinement and return contract as
+ * sk_kkt_factorize_device + sk_kkt_solve_device) for a device CSR matrix A
+ * (m x n, column indices sorted within each row) without allocating: it is for
+ * callers that cannot call cudaMalloc / cudaFree where they need the solve
+ * (all device memory handed to their own pool, or no device-wide
+ * synchronisation allowed). All work lives in one fixed device array of
+ * 542,976 bytes, which limits m to SK_KKT_NOALLOC_MAX_ROWS; a larger m returns
+ * SK_ERR_TOO_LARGE. The first call on each device fetches that array's address
+ * (set-up), so make it before any stream capture. Every call on a device uses
+ * the same array: calls that overlap in time (two host threads, or two streams
+ * without ordering between them) race and corrupt each other's results. The
+ * call synchronises `stream` (NULL = legacy default stream) before it returns. */
+#define SK_KKT_NOALLOC_MAX_ROWS 256
+int sk_kkt_solve_noalloc(int m, int n, const int* d_row_ptrs, const int* d_col_idx, const double* d_vals,
+                         const double* d_theta, double* d_rhs, double tol, void* stream);
+
 /* ---- Device kernels exposed for parity tests (device pointers, stream may be NULL) ---- */
 /* y = alpha * A x + beta * y for CSR A (rows x ?). Replaces cusparseSpMV CSR FP64
  * (src/ipm/mehrotra_device.cu:512,603,635,936). */
