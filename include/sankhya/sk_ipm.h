@@ -37,9 +37,11 @@ extern "C" {
 #define SK_START_UNIT 0        /* x = s = 1, y = 0 (src/ipm/mehrotra_device.cu:93-102) */
 #define SK_START_MEHROTRA 1    /* Mehrotra's standard heuristic start */
 #define SK_START_USER 2        /* x, y, s given in sk_solver_set_start (scaled space of the caller's LP) */
+#define SK_START_LEARNED 3     /* bipartite network's prediction (sk_solver_set_gnn); per LP, Mehrotra's start
+                                  when the prediction is not at least twice as close to the stopping test */
 
 /* Stopping rule. */
-#define SK_CRIT_RELATIVE 0     /* rel_pinf, rel_dinf, rel_gap <= tol on the unscaled LP */
+#define SK_CRIT_RELATIVE 0     /* rel_pinf, rel_dinf, rel_gap <= tol and |c^T x - b^T y| <= tol (1 + |c^T x|), unscaled */
 #define SK_CRIT_REFERENCE 1    /* ||rp||_2, ||rd||_2, mu < 1e-6 on the scaled LP (src/ipm/mehrotra_device.cu:746-748) */
 
 /* Fill-reducing ordering of A A^T. */
@@ -65,6 +67,9 @@ typedef struct sk_options {
                            * merit line search plus the exact stopping test decide progress. */
     double delta32;       /* first regularisation of FP32 fronts (default 1e-8); x10 per failed attempt */
     double delta64;       /* first regularisation of FP64 fronts (default 1e-14; strict mode uses 1e-9) */
+    double learned_accept;/* SK_START_LEARNED: the network's start is used for an LP when its distance to
+                           * the stopping test is below learned_accept x that of Mehrotra's start
+                           * (default 0.5); otherwise that LP starts from Mehrotra's start */
 } sk_options;
 
 typedef struct sk_info {
@@ -88,6 +93,8 @@ typedef struct sk_info {
     int dense_front;          /* 1 if A A^T was treated as one dense front */
     double device_ms;         /* last sk_solver_run measured with CUDA events on the solver stream */
     double flops_factor;      /* algorithmic flops of one factorisation: sum_j c_j^2 over factor columns */
+    double start_merit;       /* max(rel pinf, rel dinf, rel gap) at the start point used */
+    double fallback_merit;    /* the same for Mehrotra's start (SK_START_LEARNED runs), else 0 */
 } sk_info;
 
 /* Fills the defaults listed above. */
@@ -126,6 +133,45 @@ void sk_solver_destroy(sk_solver* h);
  * output tile read and written once). fp32 selects the FP32 front path. Returns
  * the number of values written (16). No reference counterpart. */
 int sk_solver_profile(sk_solver* h, int fp32, double* out, int cap);
+
+/* ---- Learned start: bipartite row / column message-passing network ----
+ * No reference counterpart. 3 layers, hidden width 64, BF16 weights with FP32
+ * accumulation, FP32 master weights for Adam. Input: a Ruiz-scaled LP (column
+ * features c_j, log(1 + nnz_j), ||A_.j||_2; row features b_i, log(1 + nnz_i),
+ * ||A_i.||_2; edge weights a_ij). Output: log x_j, log s_j per column and y_i per
+ * row, in the scaled space. Loss: (1 / 2n) sum_j [(log x_j - t_j)^2 + (log s_j -
+ * u_j)^2] + (1 / m) sum_i (y_i - w_i)^2, log targets clamped to [-30, 30]. */
+typedef struct sk_gnn sk_gnn;
+typedef struct sk_gnn_batch sk_gnn_batch;
+int sk_gnn_create(unsigned long long seed, sk_gnn** out);   /* Glorot-uniform weights, biases 0 (0.01 in the input layers) */
+void sk_gnn_destroy(sk_gnn* g);
+int sk_gnn_num_params(const sk_gnn* g);
+int sk_gnn_get_params(const sk_gnn* g, float* out);         /* FP32 master weights */
+int sk_gnn_set_params(sk_gnn* g, const float* in);          /* also refreshes the BF16 copy */
+/* One graph from host CSR arrays (m x n, already scaled as the caller wants it
+ * seen); targets t_logx, t_logs (n) and t_y (m) may be NULL (inference only). */
+int sk_gnn_batch_create(int m, int n, const int* row_ptrs, const int* col_idx, const double* vals,
+                        const double* b, const double* c, const double* t_logx, const double* t_logs,
+                        const double* t_y, sk_gnn_batch** out);
+/* Device copy of a solver's scaled batch LP and of the iterate captured during its
+ * last run (sk_solver_set_capture); SK_ERR_INVALID if some LP was not captured. */
+int sk_gnn_batch_from_solver(sk_solver* h, sk_gnn_batch** out);
+int sk_gnn_batch_dims(const sk_gnn_batch* bt, int* m, int* n);
+/* Host copies of the batch's targets (log x, log s: n; y: m); any may be NULL. */
+int sk_gnn_batch_targets(const sk_gnn_batch* bt, double* logx, double* logs, double* y);
+void sk_gnn_batch_destroy(sk_gnn_batch* bt);
+/* Host outputs: logx, logs (n), y (m); any may be NULL. */
+int sk_gnn_predict(sk_gnn* g, sk_gnn_batch* bt, double* logx, double* logs, double* y);
+/* Loss on the batch's targets and its gradient w.r.t. every parameter (grad: num_params floats). */
+int sk_gnn_loss_grad(sk_gnn* g, sk_gnn_batch* bt, double* loss, float* grad);
+/* Forward + backward + one Adam step (beta1 0.9, beta2 0.999, eps 1e-8, gradient
+ * entries clipped to [-10, 10]) at learning rate lr; loss before the step. */
+int sk_gnn_train_step(sk_gnn* g, sk_gnn_batch* bt, float lr, double* loss);
+/* Network for SK_START_LEARNED (not owned: keep it alive while the solver runs). */
+int sk_solver_set_gnn(sk_solver* h, sk_gnn* g);
+/* Keep each LP's iterate the first time its mu drops below mu_threshold (or the
+ * final iterate), as training targets; 0 turns capture off. */
+int sk_solver_set_capture(sk_solver* h, double mu_threshold);
 
 /* ---- KKT normal-equation engine (device pointers) ----
  * Replaces: gpu::GPUKKTCholeskySolver (src/cuda/kkt.cuh:28-71). A is CSR (m x n).

@@ -339,7 +339,7 @@ int oracle_kkt_solve(int m, int n, const int* rp, const int* ci, const double* v
             int pi = P ? P[i] : i, pj = P ? P[j] : j;
             k.M0[(size_t)i * m + j] = M[(size_t)pi * m + pj];
         }
-    double* rp_ = (double*)malloc(sizeof(double) * ((size_t)m + 1));
+    double* rp_ = (double*)calloc((size_t)m + 1, sizeof(double));
     double* dp = (double*)malloc(sizeof(double) * ((size_t)m + 1));
     for (int i = 0; i < m; ++i) rp_[i] = rhs[P ? P[i] : i];
     double t = tol;
@@ -567,7 +567,10 @@ int oracle_ipm_solve(int m, int n, const int* cp, const int* ri, const double* v
             for (int j = 0; j < n; ++j) { double a = fabs(w.rd[j] / C[j]); if (a > dinf) dinf = a; }
             double cx = dot(n, c, x), by = dot(m, b, y);
             double gap = fabs(cx - by) / (1.0 + fabs(cx) + fabs(by));
-            converged = pinf / unscale_b <= opts.tol && dinf / unscale_c <= opts.tol && gap <= opts.tol;
+            /* the gap is also held to tol (1 + |c^T x|): with the optimum between the primal
+             * and dual objectives, c^T x is then within tol of it in relative terms */
+            converged = pinf / unscale_b <= opts.tol && dinf / unscale_c <= opts.tol && gap <= opts.tol &&
+                        fabs(cx - by) <= opts.tol * (1.0 + fabs(cx));
         }
         if (opts.verbose)
             fprintf(stderr, "oracle iter %d rp %.3e rd %.3e mu %.3e\n", iter, nrp, nrd, mu);

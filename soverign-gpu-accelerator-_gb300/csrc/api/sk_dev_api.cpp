@@ -9,6 +9,7 @@
 
 #include "api/sk_error.hpp"
 #include "cuda/device_ipm.hpp"
+#include "cuda/gnn.hpp"
 #include "cuda/kkt_engine.hpp"
 #include "ipm/front_plan.hpp"
 #include "sankhya/sk_ipm.h"
@@ -17,6 +18,24 @@ using namespace sankhya;
 
 struct sk_solver {
     std::unique_ptr<dev::DeviceIPM> ipm;
+};
+
+struct sk_gnn {
+    std::unique_ptr<dev::Gnn> net;
+    cudaStream_t st = nullptr;
+    ~sk_gnn() {
+        net.reset();
+        if (st) cudaStreamDestroy(st);
+    }
+};
+
+// One graph (or a solver's whole batch) resident on the device, with targets.
+struct sk_gnn_batch {
+    dev::Arena arena;
+    dev::Slot<int> a_rp, a_ci, t_rp, t_ci;
+    dev::Slot<double> a_v, t_v, b, c, tlx, tls, ty;
+    dev::DeviceLP lp;
+    bool has_targets = false;
 };
 
 struct sk_kkt {
@@ -44,9 +63,10 @@ sk_options opts_or_default(const sk_options* o) {
 
 void check_options(const sk_options& o) {
     if (o.precision != SK_PREC_FP64 && o.precision != SK_PREC_MIXED) throw std::invalid_argument("bad precision");
-    if (o.start < SK_START_UNIT || o.start > SK_START_USER) throw std::invalid_argument("bad start");
+    if (o.start < SK_START_UNIT || o.start > SK_START_LEARNED) throw std::invalid_argument("bad start");
     if (o.criteria != SK_CRIT_RELATIVE && o.criteria != SK_CRIT_REFERENCE) throw std::invalid_argument("bad criteria");
     if (!(o.tol > 0.0) || o.max_iter < 0 || o.ruiz_passes < 0) throw std::invalid_argument("bad tolerance / limits");
+    if (!(o.learned_accept >= 0.0)) throw std::invalid_argument("bad learned_accept");
     if (o.ordering < SK_ORDER_AUTO || o.ordering > SK_ORDER_NATURAL) throw std::invalid_argument("bad ordering");
 }
 
@@ -351,6 +371,247 @@ int sk_spmv_csr(int rows, const int* d_row_ptrs, const int* d_col_idx, const dou
     if (rows < 0 || (rows > 0 && (!d_row_ptrs || !d_col_idx || !d_vals || !d_x || !d_y))) return SK_ERR_INVALID;
     try {
         dev::spmv_csr(rows, d_row_ptrs, d_col_idx, d_vals, d_x, alpha, beta, d_y, static_cast<cudaStream_t>(stream));
+        return SK_OK;
+    } catch (...) {
+        return api::status_of_current_exception();
+    }
+}
+
+
+int sk_gnn_create(unsigned long long seed, sk_gnn** out) {
+    api::clear_error();
+    if (!out) return SK_ERR_INVALID;
+    try {
+        int ndev = 0;
+        if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+            throw api::sk_exception(SK_ERR_NO_DEVICE, "no CUDA device visible");
+        std::unique_ptr<sk_gnn> g(new sk_gnn);
+        SK_CUDA(cudaStreamCreateWithFlags(&g->st, cudaStreamNonBlocking));
+        g->net.reset(new dev::Gnn(seed));
+        *out = g.release();
+        return SK_OK;
+    } catch (...) {
+        return api::status_of_current_exception();
+    }
+}
+
+void sk_gnn_destroy(sk_gnn* g) { delete g; }
+
+int sk_gnn_num_params(const sk_gnn* g) { return g && g->net ? g->net->num_params() : -SK_ERR_INVALID; }
+
+int sk_gnn_get_params(const sk_gnn* g, float* out) {
+    api::clear_error();
+    if (!g || !out) return SK_ERR_INVALID;
+    try {
+        g->net->get_params(out);
+        return SK_OK;
+    } catch (...) {
+        return api::status_of_current_exception();
+    }
+}
+
+int sk_gnn_set_params(sk_gnn* g, const float* in) {
+    api::clear_error();
+    if (!g || !in) return SK_ERR_INVALID;
+    try {
+        g->net->set_params(in);
+        return SK_OK;
+    } catch (...) {
+        return api::status_of_current_exception();
+    }
+}
+
+int sk_gnn_batch_create(int m, int n, const int* row_ptrs, const int* col_idx, const double* vals, const double* b,
+                        const double* c, const double* t_logx, const double* t_logs, const double* t_y,
+                        sk_gnn_batch** out) {
+    api::clear_error();
+    if (!out || m <= 0 || n <= 0 || !row_ptrs || !b || !c) return SK_ERR_INVALID;
+    const bool tg = t_logx || t_logs || t_y;
+    if (tg && !(t_logx && t_logs && t_y)) {
+        api::set_error("targets: give all of t_logx, t_logs, t_y or none");
+        return SK_ERR_INVALID;
+    }
+    try {
+        core::CSRMatrix A = api::pattern_csr(m, n, row_ptrs, col_idx);
+        const int nz = row_ptrs[m];
+        if (nz > 0 && !vals) throw api::sk_exception(SK_ERR_INVALID, "vals missing");
+        A.values.assign(vals, vals + nz);
+        std::vector<int> cp(n + 1, 0), ri(nz);
+        std::vector<double> cv(nz);
+        for (int q = 0; q < nz; ++q) cp[col_idx[q] + 1]++;
+        for (int j = 0; j < n; ++j) cp[j + 1] += cp[j];
+        std::vector<int> nx(cp.begin(), cp.end() - 1);
+        for (int i = 0; i < m; ++i)
+            for (int q = row_ptrs[i]; q < row_ptrs[i + 1]; ++q) {
+                const int d = nx[col_idx[q]]++;
+                ri[d] = i;
+                cv[d] = vals[q];
+            }
+        std::unique_ptr<sk_gnn_batch> bt(new sk_gnn_batch);
+        dev::Arena& ar = bt->arena;
+        dev::reserve(ar, bt->a_rp, m + 1); dev::reserve(ar, bt->a_ci, nz); dev::reserve(ar, bt->t_rp, n + 1);
+        dev::reserve(ar, bt->t_ci, nz);
+        dev::reserve(ar, bt->a_v, nz); dev::reserve(ar, bt->t_v, nz); dev::reserve(ar, bt->b, m);
+        dev::reserve(ar, bt->c, n); dev::reserve(ar, bt->tlx, n); dev::reserve(ar, bt->tls, n);
+        dev::reserve(ar, bt->ty, m);
+        ar.commit();
+        for (auto* s : {&bt->a_rp, &bt->a_ci, &bt->t_rp, &bt->t_ci}) dev::bind(ar, *s);
+        for (auto* s : {&bt->a_v, &bt->t_v, &bt->b, &bt->c, &bt->tlx, &bt->tls, &bt->ty}) dev::bind(ar, *s);
+        cudaStream_t st = nullptr;
+        dev::upload(bt->a_rp, A.row_ptrs, st); dev::upload(bt->a_ci, A.col_indices, st);
+        dev::upload(bt->a_v, A.values, st); dev::upload(bt->t_rp, cp, st); dev::upload(bt->t_ci, ri, st);
+        dev::upload(bt->t_v, cv, st);
+        dev::upload(bt->b, std::vector<double>(b, b + m), st);
+        dev::upload(bt->c, std::vector<double>(c, c + n), st);
+        if (tg) {
+            dev::upload(bt->tlx, std::vector<double>(t_logx, t_logx + n), st);
+            dev::upload(bt->tls, std::vector<double>(t_logs, t_logs + n), st);
+            dev::upload(bt->ty, std::vector<double>(t_y, t_y + m), st);
+            bt->has_targets = true;
+        }
+        SK_CUDA(cudaStreamSynchronize(st));
+        auto& lp = bt->lp;
+        lp.nlp = 1; lp.M = m; lp.N = n; lp.nnz = nz;
+        lp.a_rp = bt->a_rp.ptr; lp.a_ci = bt->a_ci.ptr; lp.a_v = bt->a_v.ptr;
+        lp.t_rp = bt->t_rp.ptr; lp.t_ci = bt->t_ci.ptr; lp.t_v = bt->t_v.ptr;
+        lp.b = bt->b.ptr; lp.c = bt->c.ptr;
+        *out = bt.release();
+        return SK_OK;
+    } catch (...) {
+        return api::status_of_current_exception();
+    }
+}
+
+int sk_gnn_batch_from_solver(sk_solver* h, sk_gnn_batch** out) {
+    api::clear_error();
+    if (!h || !out) return SK_ERR_INVALID;
+    try {
+        dev::DeviceIPM& ipm = *h->ipm;
+        if (!ipm.capture_complete())
+            throw api::sk_exception(SK_ERR_INVALID, "no complete iterate capture (sk_solver_set_capture, then run)");
+        const dev::DeviceLP& s = ipm.device_lp();
+        const int m = s.M, n = s.N;
+        const int64_t nz = s.nnz;
+        std::unique_ptr<sk_gnn_batch> bt(new sk_gnn_batch);
+        dev::Arena& ar = bt->arena;
+        dev::reserve(ar, bt->a_rp, m + 1); dev::reserve(ar, bt->a_ci, nz); dev::reserve(ar, bt->t_rp, n + 1);
+        dev::reserve(ar, bt->t_ci, nz);
+        dev::reserve(ar, bt->a_v, nz); dev::reserve(ar, bt->t_v, nz); dev::reserve(ar, bt->b, m);
+        dev::reserve(ar, bt->c, n); dev::reserve(ar, bt->tlx, n); dev::reserve(ar, bt->tls, n);
+        dev::reserve(ar, bt->ty, m);
+        ar.commit();
+        for (auto* x : {&bt->a_rp, &bt->a_ci, &bt->t_rp, &bt->t_ci}) dev::bind(ar, *x);
+        for (auto* x : {&bt->a_v, &bt->t_v, &bt->b, &bt->c, &bt->tlx, &bt->tls, &bt->ty}) dev::bind(ar, *x);
+        auto cp = [](void* d, const void* src, size_t bytes) {
+            SK_CUDA(cudaMemcpy(d, src, bytes, cudaMemcpyDeviceToDevice));
+        };
+        cp(bt->a_rp.ptr, s.a_rp, sizeof(int) * (m + 1)); cp(bt->a_ci.ptr, s.a_ci, sizeof(int) * nz);
+        cp(bt->a_v.ptr, s.a_v, sizeof(double) * nz); cp(bt->t_rp.ptr, s.t_rp, sizeof(int) * (n + 1));
+        cp(bt->t_ci.ptr, s.t_ci, sizeof(int) * nz); cp(bt->t_v.ptr, s.t_v, sizeof(double) * nz);
+        cp(bt->b.ptr, s.b, sizeof(double) * m); cp(bt->c.ptr, s.c, sizeof(double) * n);
+        cp(bt->tlx.ptr, ipm.capture_logx(), sizeof(double) * n);
+        cp(bt->tls.ptr, ipm.capture_logs(), sizeof(double) * n);
+        cp(bt->ty.ptr, ipm.capture_y(), sizeof(double) * m);
+        bt->has_targets = true;
+        auto& lp = bt->lp;
+        lp.nlp = s.nlp; lp.M = m; lp.N = n; lp.nnz = nz;
+        lp.a_rp = bt->a_rp.ptr; lp.a_ci = bt->a_ci.ptr; lp.a_v = bt->a_v.ptr;
+        lp.t_rp = bt->t_rp.ptr; lp.t_ci = bt->t_ci.ptr; lp.t_v = bt->t_v.ptr;
+        lp.b = bt->b.ptr; lp.c = bt->c.ptr;
+        *out = bt.release();
+        return SK_OK;
+    } catch (...) {
+        return api::status_of_current_exception();
+    }
+}
+
+int sk_gnn_batch_dims(const sk_gnn_batch* bt, int* m, int* n) {
+    if (!bt) return SK_ERR_INVALID;
+    if (m) *m = bt->lp.M;
+    if (n) *n = bt->lp.N;
+    return SK_OK;
+}
+
+int sk_gnn_batch_targets(const sk_gnn_batch* bt, double* logx, double* logs, double* y) {
+    api::clear_error();
+    if (!bt) return SK_ERR_INVALID;
+    if (!bt->has_targets) { api::set_error("batch has no targets"); return SK_ERR_INVALID; }
+    try {
+        const int m = bt->lp.M, n = bt->lp.N;
+        if (logx) SK_CUDA(cudaMemcpy(logx, bt->tlx.ptr, sizeof(double) * n, cudaMemcpyDeviceToHost));
+        if (logs) SK_CUDA(cudaMemcpy(logs, bt->tls.ptr, sizeof(double) * n, cudaMemcpyDeviceToHost));
+        if (y) SK_CUDA(cudaMemcpy(y, bt->ty.ptr, sizeof(double) * m, cudaMemcpyDeviceToHost));
+        return SK_OK;
+    } catch (...) {
+        return api::status_of_current_exception();
+    }
+}
+
+void sk_gnn_batch_destroy(sk_gnn_batch* bt) { delete bt; }
+
+int sk_gnn_predict(sk_gnn* g, sk_gnn_batch* bt, double* logx, double* logs, double* y) {
+    api::clear_error();
+    if (!g || !bt) return SK_ERR_INVALID;
+    try {
+        const int m = bt->lp.M, n = bt->lp.N;
+        dev::Arena tmp;
+        dev::Slot<double> ox, os, oy;
+        dev::reserve(tmp, ox, n); dev::reserve(tmp, os, n); dev::reserve(tmp, oy, m);
+        tmp.commit();
+        dev::bind(tmp, ox); dev::bind(tmp, os); dev::bind(tmp, oy);
+        g->net->forward(bt->lp, g->st, ox.ptr, os.ptr, oy.ptr);
+        if (logx) SK_CUDA(cudaMemcpyAsync(logx, ox.ptr, sizeof(double) * n, cudaMemcpyDeviceToHost, g->st));
+        if (logs) SK_CUDA(cudaMemcpyAsync(logs, os.ptr, sizeof(double) * n, cudaMemcpyDeviceToHost, g->st));
+        if (y) SK_CUDA(cudaMemcpyAsync(y, oy.ptr, sizeof(double) * m, cudaMemcpyDeviceToHost, g->st));
+        SK_CUDA(cudaStreamSynchronize(g->st));
+        return SK_OK;
+    } catch (...) {
+        return api::status_of_current_exception();
+    }
+}
+
+int sk_gnn_loss_grad(sk_gnn* g, sk_gnn_batch* bt, double* loss, float* grad) {
+    api::clear_error();
+    if (!g || !bt) return SK_ERR_INVALID;
+    if (!bt->has_targets) { api::set_error("batch has no targets"); return SK_ERR_INVALID; }
+    try {
+        const double l = g->net->forward(bt->lp, g->st, nullptr, nullptr, nullptr, bt->tlx.ptr, bt->tls.ptr, bt->ty.ptr);
+        if (loss) *loss = l;
+        g->net->backward(bt->lp, g->st, grad);
+        SK_CUDA(cudaStreamSynchronize(g->st));
+        return SK_OK;
+    } catch (...) {
+        return api::status_of_current_exception();
+    }
+}
+
+int sk_gnn_train_step(sk_gnn* g, sk_gnn_batch* bt, float lr, double* loss) {
+    api::clear_error();
+    if (!g || !bt || !(lr > 0.f)) return SK_ERR_INVALID;
+    if (!bt->has_targets) { api::set_error("batch has no targets"); return SK_ERR_INVALID; }
+    try {
+        const double l = g->net->forward(bt->lp, g->st, nullptr, nullptr, nullptr, bt->tlx.ptr, bt->tls.ptr, bt->ty.ptr);
+        if (loss) *loss = l;
+        g->net->backward(bt->lp, g->st, nullptr);
+        g->net->adam_step(g->st, lr);
+        return SK_OK;
+    } catch (...) {
+        return api::status_of_current_exception();
+    }
+}
+
+int sk_solver_set_gnn(sk_solver* h, sk_gnn* g) {
+    api::clear_error();
+    if (!h) return SK_ERR_INVALID;
+    h->ipm->set_gnn(g ? g->net.get() : nullptr);
+    return SK_OK;
+}
+
+int sk_solver_set_capture(sk_solver* h, double mu_threshold) {
+    api::clear_error();
+    if (!h) return SK_ERR_INVALID;
+    try {
+        h->ipm->set_capture(mu_threshold);
         return SK_OK;
     } catch (...) {
         return api::status_of_current_exception();

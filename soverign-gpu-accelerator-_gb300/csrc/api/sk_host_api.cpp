@@ -88,6 +88,7 @@ void sk_options_default(sk_options* opt) {
     opt->strict = 0;
     opt->delta32 = 1e-8;
     opt->delta64 = 1e-14;
+    opt->learned_accept = 0.5;
 }
 
 int sk_lp_generate(int family, int instance, sk_lp** out) {

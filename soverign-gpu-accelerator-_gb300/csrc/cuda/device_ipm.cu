@@ -19,6 +19,7 @@
 // deterministic per LP, and in mixed precision the factor is FP32 until mu drops
 // below the switch threshold or an FP32 solve misses its tolerance.
 #include "cuda/device_ipm.hpp"
+#include "cuda/gnn.hpp"
 
 #include <algorithm>
 #include <chrono>
@@ -34,6 +35,8 @@ namespace {
 
 constexpr int kChunk = 4096;
 constexpr int kMaxR = 10;
+constexpr double kLearnedSaturated = 0.99;   // learned start: upper bound on its distance to the stopping test
+
 enum { OP_SUM = 0, OP_MAX = 1, OP_MIN = 2 };
 
 inline int nblk(int64_t n, int t = 256) { return static_cast<int>((n + t - 1) / t); }
@@ -318,6 +321,54 @@ struct RedStart {        // [sum x s, sum x, sum s]
     }
 };
 
+// learned start: x = exp(lx), s = exp(ls), exponents clamped to [-20, 20]
+__global__ void k_learned_point(int n, const double* __restrict__ lx, const double* __restrict__ ls,
+                                double* __restrict__ x, double* __restrict__ s) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < n) {
+        const double a = lx[j], b = ls[j];
+        x[j] = exp(isfinite(a) ? fmin(fmax(a, -20.0), 20.0) : 0.0);
+        s[j] = exp(isfinite(b) ? fmin(fmax(b, -20.0), 20.0) : 0.0);
+    }
+}
+// pairs with x_j s_j below floor[lp] are scaled up (both by the same factor) to the floor
+__global__ void k_center_floor(int n, const double* __restrict__ floor_lp, const int* __restrict__ lp_of,
+                               double* __restrict__ x, double* __restrict__ s) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < n) {
+        const double f = floor_lp[lp_of[j]], p = x[j] * s[j];
+        if (p < f && p > 0.0) {
+            const double g = sqrt(f / p);
+            x[j] *= g;
+            s[j] *= g;
+        }
+    }
+}
+struct RedRatioNeg {     // [max a with x - a dx >= 0, same for s - a ds]
+    const double *x, *dx, *s, *ds;
+    __device__ static constexpr int op(int) { return OP_MIN; }
+    __device__ void operator()(int j, double* v) const {
+        v[0] = dx[j] > 0.0 ? x[j] / dx[j] : 1.0e30;
+        v[1] = ds[j] > 0.0 ? s[j] / ds[j] : 1.0e30;
+    }
+};
+// out = a * b
+__global__ void k_hadamard(int n, const double* __restrict__ a, const double* __restrict__ b, double* __restrict__ out) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < n) out[j] = a[j] * b[j];
+}
+// a = keep[lp] != 0 ? a : b
+__global__ void k_pick_lp(int n, const double* __restrict__ keep, const int* __restrict__ lp_of,
+                          double* __restrict__ a, const double* __restrict__ b) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < n && keep[lp_of[j]] == 0.0) a[j] = b[j];
+}
+// out = log(max(v, 1e-300))
+__global__ void k_log_floor(int n, const double* __restrict__ v, double* __restrict__ out) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < n) out[j] = log(fmax(v[j], 1e-300));
+}
+
 // y += a[lp] * x
 __global__ void k_axpy_lp(int n, const double* __restrict__ a, const double* __restrict__ x,
                           const int* __restrict__ lp_of, double* __restrict__ y) {
@@ -384,6 +435,10 @@ struct DeviceIPM::Impl {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::vector<double> hx0, hy0, hs0;      // user start (scaled)
     int ga = 4, gt = 4;
+    Gnn* gnn = nullptr;                     // network of SK_START_LEARNED (not owned)
+    double capture_mu = 0.0;                // iterate capture for training targets
+    std::vector<char> captured;
+    double *cap_lx = nullptr, *cap_ls = nullptr, *cap_y = nullptr;
 
     double* sc(int which) { return scal.ptr + static_cast<size_t>(which) * nlp; }
     double* tmpn() { return crxs.ptr; }   // scratch n-vector outside the backtracking phase
@@ -595,6 +650,7 @@ void DeviceIPM::profile(bool fp32, double* out16) {
 
 DeviceIPM::~DeviceIPM() {
     if (im_ && im_->ev0) { cudaEventDestroy(im_->ev0); cudaEventDestroy(im_->ev1); }
+    if (im_) for (double* p : {im_->cap_lx, im_->cap_ls, im_->cap_y}) if (p) cudaFree(p);
     kkt_.reset();
     if (im_ && im_->st) cudaStreamDestroy(im_->st);
 }
@@ -612,6 +668,30 @@ void DeviceIPM::set_start(int lp, const double* x, const double* y, const double
     I.user_start[lp] = 1;
 }
 
+void DeviceIPM::set_gnn(Gnn* g) { im_->gnn = g; }
+
+void DeviceIPM::set_capture(double mu) {
+    Impl& I = *im_;
+    if (!(mu >= 0.0)) throw api::sk_exception(SK_ERR_INVALID, "set_capture: mu must be >= 0");
+    I.capture_mu = mu;
+    if (mu > 0.0 && !I.cap_lx) {
+        SK_CUDA(cudaMalloc(&I.cap_lx, sizeof(double) * I.N));
+        SK_CUDA(cudaMalloc(&I.cap_ls, sizeof(double) * I.N));
+        SK_CUDA(cudaMalloc(&I.cap_y, sizeof(double) * I.M));
+    }
+    I.captured.assign(I.nlp, 0);
+}
+
+bool DeviceIPM::capture_complete() const {
+    const Impl& I = *im_;
+    if (!(I.capture_mu > 0.0) || static_cast<int>(I.captured.size()) != I.nlp) return false;
+    for (char c : I.captured) if (!c) return false;
+    return true;
+}
+const double* DeviceIPM::capture_logx() const { return im_->cap_lx; }
+const double* DeviceIPM::capture_logs() const { return im_->cap_ls; }
+const double* DeviceIPM::capture_y() const { return im_->cap_y; }
+
 void DeviceIPM::run() {
     Impl& I = *im_;
     KktEngine& K = *kkt_;
@@ -624,6 +704,9 @@ void DeviceIPM::run() {
     }
     SK_CUDA(cudaEventRecord(I.ev0, st));
     const auto& o = I.opt;
+    if (o.start == SK_START_LEARNED && !I.gnn)
+        throw api::sk_exception(SK_ERR_INVALID, "SK_START_LEARNED needs a network (sk_solver_set_gnn)");
+    if (I.capture_mu > 0.0) I.captured.assign(nlp, 0);
     I.factorizations = I.solves = I.refine_steps = 0;
     I.switched = false;
     I.used_fp32 = false;
@@ -854,7 +937,7 @@ void DeviceIPM::run() {
         return factor(false);
     };
 
-    if (o.start == SK_START_MEHROTRA) {
+    if (o.start == SK_START_MEHROTRA || o.start == SK_START_LEARNED) {
         // Mehrotra's heuristic start in the scaled space: x~ = A^T (A A^T)^{-1} b,
         // y = (A A^T)^{-1} A c, s~ = c - A^T y; x, s shifted to positivity by
         // max(-1.5 min, 0) and then by 1/2 x^T s / sum(s), 1/2 x^T s / sum(x).
@@ -894,6 +977,87 @@ void DeviceIPM::run() {
         SK_CUDA(cudaGetLastError());
     }
 
+    if (o.start == SK_START_LEARNED) {
+        // Mehrotra's start (just computed) is the fallback; keep it in (dxa, dya, dsa).
+        SK_CUDA(cudaMemcpyAsync(I.dxa.ptr, I.x.ptr, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
+        SK_CUDA(cudaMemcpyAsync(I.dya.ptr, I.y.ptr, sizeof(double) * M, cudaMemcpyDeviceToDevice, st));
+        SK_CUDA(cudaMemcpyAsync(I.dsa.ptr, I.s.ptr, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
+        // the network's point in the scaled space: x = exp(log x), s = exp(log s), y
+        I.gnn->forward(lp_, st, I.dx.ptr, I.ds.ptr, I.dy.ptr);
+        k_learned_point<<<nblk(N), 256, 0, st>>>(N, I.dx.ptr, I.ds.ptr, I.x.ptr, I.s.ptr);
+        SK_CUDA(cudaMemcpyAsync(I.y.ptr, I.dy.ptr, sizeof(double) * M, cudaMemcpyDeviceToDevice, st));
+        // Weighted projection towards Ax = b and A^T y + s = c with the predicted
+        // Theta = x / s (rp = Ax - b, rd = A^T y + s - c): x -= a_p Theta A^T w with
+        // (A Theta A^T) w = rp; y -= a_d v, s -= a_d (rd - A^T v) with (A Theta A^T) v =
+        // A Theta rd; a_p, a_d the longest steps (at most 1) that keep 10% of x and s.
+        {
+            std::vector<double> one(nlp, 1.0);
+            I.put_scalars(0, one);
+            k_theta<<<nblk(N), 256, 0, st>>>(N, I.x.ptr, I.s.ptr, I.col_lp.ptr, d_mask, I.theta.ptr);
+            const bool f32 = o.precision == SK_PREC_MIXED;
+            if (!factor(f32) && !(f32 && factor(false)))
+                throw api::sk_exception(SK_ERR_NUMERICAL, "learned start: A Theta A^T could not be factored");
+            for (int k = 0; k < nlp; ++k) tol[k] = 1e-8;
+            std::vector<char> ok;
+            residuals(I.x.ptr, I.y.ptr, I.s.ptr, I.rp.ptr, I.rd.ptr);
+            solve(I.rp.ptr, I.dy.ptr, ok);
+            spmv(N, I.gt, I.t_rp.ptr, I.t_ci.ptr, I.t_v.ptr, I.dy.ptr, EpiTheta{I.theta.ptr, I.dx.ptr}, st);
+            k_hadamard<<<nblk(N), 256, 0, st>>>(N, I.theta.ptr, I.rd.ptr, I.tmpn());
+            spmv(M, I.ga, I.a_rp.ptr, I.a_ci.ptr, I.a_v.ptr, I.tmpn(), EpiAxpby{1.0, 0.0, I.rkkt.ptr}, st);
+            solve(I.rkkt.ptr, I.dy.ptr, ok);
+            spmv(N, I.gt, I.t_rp.ptr, I.t_ci.ptr, I.t_v.ptr, I.dy.ptr, EpiAxpby{1.0, 0.0, I.tmpn()}, st);
+            k_sub<<<nblk(N), 256, 0, st>>>(N, I.rd.ptr, I.tmpn(), I.ds.ptr);
+            I.reduce_cols<2>(RedRatioNeg{I.x.ptr, I.dx.ptr, I.s.ptr, I.ds.ptr}, I.redout.ptr);
+            std::vector<double> h = I.fetch(static_cast<size_t>(nlp) * 2), apv(nlp), adv(nlp);
+            for (int k = 0; k < nlp; ++k) {
+                apv[k] = std::isfinite(h[2 * k]) ? -std::min(1.0, 0.9 * h[2 * k]) : 0.0;
+                adv[k] = std::isfinite(h[2 * k + 1]) ? -std::min(1.0, 0.9 * h[2 * k + 1]) : 0.0;
+            }
+            I.put_scalars(1, apv);
+            k_axpy_lp<<<nblk(N), 256, 0, st>>>(N, d_ap, I.dx.ptr, I.col_lp.ptr, I.x.ptr);
+            I.put_scalars(1, adv);
+            k_axpy_lp<<<nblk(N), 256, 0, st>>>(N, d_ap, I.ds.ptr, I.col_lp.ptr, I.s.ptr);
+            k_axpy_lp<<<nblk(M), 256, 0, st>>>(M, d_ap, I.dy.ptr, I.row_lp.ptr, I.y.ptr);
+        }
+        // centrality floor: x_j s_j >= 0.1 mean(x s) within each LP
+        I.reduce_cols<3>(RedStart{I.x.ptr, I.s.ptr}, I.redout.ptr);
+        std::vector<double> h = I.fetch(static_cast<size_t>(nlp) * 3), fl(nlp);
+        for (int k = 0; k < nlp; ++k) fl[k] = std::isfinite(h[3 * k]) ? 0.1 * h[3 * k] / nn[k] : 0.0;
+        I.put_scalars(1, fl);
+        k_center_floor<<<nblk(N), 256, 0, st>>>(N, d_ap, I.col_lp.ptr, I.x.ptr, I.s.ptr);
+        // distance to the stopping test, max(rel pinf, rel dinf, rel gap), of both candidates
+        auto merit = [&](const double* xx, const double* yy, const double* ss) {
+            residuals(xx, yy, ss, I.rp.ptr, I.rd.ptr);
+            I.reduce_rows<3>(RedResidM{I.rp.ptr, I.R.ptr, I.b.ptr, yy}, I.redout.ptr);
+            I.reduce_cols<4>(RedResidN{I.rd.ptr, I.C.ptr, xx, ss, I.c.ptr}, I.redout.ptr + nlp * 3);
+            std::vector<double> hh = I.fetch(static_cast<size_t>(nlp) * 7), phi(nlp);
+            const double* a = hh.data();
+            const double* b = hh.data() + nlp * 3;
+            for (int k = 0; k < nlp; ++k) {
+                const double obj = b[k * 4 + 3], by = a[k * 3 + 2];
+                const double v = std::max({a[k * 3 + 1] / (1.0 + I.binf[k]), b[k * 4 + 1] / (1.0 + I.cinf[k]),
+                                           std::fabs(obj - by) / (1.0 + std::fabs(obj) + std::fabs(by))});
+                phi[k] = std::isfinite(v) ? v : HUGE_VAL;
+            }
+            return phi;
+        };
+        const std::vector<double> phiL = merit(I.x.ptr, I.y.ptr, I.s.ptr);
+        const std::vector<double> phiM = merit(I.dxa.ptr, I.dya.ptr, I.dsa.ptr);
+        std::vector<double> keep(nlp);
+        for (int k = 0; k < nlp; ++k) {
+            // phi near 1 means c^T x and b^T y differ by orders of magnitude: not a usable start
+            keep[k] = phiL[k] < o.learned_accept * phiM[k] && phiL[k] < kLearnedSaturated ? 1.0 : 0.0;
+            I.res[k].learned_start = keep[k] != 0.0;
+            I.res[k].start_merit = keep[k] != 0.0 ? phiL[k] : phiM[k];
+            I.res[k].fallback_merit = phiM[k];
+        }
+        I.put_scalars(0, keep);
+        k_pick_lp<<<nblk(N), 256, 0, st>>>(N, d_mask, I.col_lp.ptr, I.x.ptr, I.dxa.ptr);
+        k_pick_lp<<<nblk(N), 256, 0, st>>>(N, d_mask, I.col_lp.ptr, I.s.ptr, I.dsa.ptr);
+        k_pick_lp<<<nblk(M), 256, 0, st>>>(M, d_mask, I.row_lp.ptr, I.y.ptr, I.dya.ptr);
+        SK_CUDA(cudaGetLastError());
+    }
+
     int iter = 0;
     std::vector<double> hm, hn;
     for (iter = 0; iter < o.max_iter; ++iter) {
@@ -920,10 +1084,20 @@ void DeviceIPM::run() {
             r.iterations = iter;
             bool conv;
             if (o.criteria == SK_CRIT_REFERENCE) conv = nrp[k] < 1e-6 && nrd[k] < 1e-6 && mu[k] < 1e-6;
-            else conv = r.rel_pinf <= o.tol && r.rel_dinf <= o.tol && r.rel_gap <= o.tol;
+            else   // the gap also within tol (1 + |c^T x|): the objective is then within tol of the optimum
+                conv = r.rel_pinf <= o.tol && r.rel_dinf <= o.tol && r.rel_gap <= o.tol &&
+                       std::fabs(r.objective - hm[k * 3 + 2]) <= o.tol * (1.0 + std::fabs(r.objective));
             if (o.verbose)
                 std::fprintf(stderr, "[sk] lp %d iter %d rp %.3e rd %.3e mu %.3e gap %.3e %s\n", k, iter, nrp[k],
                              nrd[k], mu[k], r.rel_gap, I.switched || o.precision == SK_PREC_FP64 ? "fp64" : "fp32");
+            if (I.capture_mu > 0.0 && !I.captured[k] && (conv || mu[k] < I.capture_mu)) {
+                const int co = I.col_off[k], nk = I.col_off[k + 1] - co;
+                const int ro = I.row_off[k], mk = I.row_off[k + 1] - ro;
+                k_log_floor<<<nblk(nk), 256, 0, st>>>(nk, I.x.ptr + co, I.cap_lx + co);
+                k_log_floor<<<nblk(nk), 256, 0, st>>>(nk, I.s.ptr + co, I.cap_ls + co);
+                SK_CUDA(cudaMemcpyAsync(I.cap_y + ro, I.y.ptr + ro, sizeof(double) * mk, cudaMemcpyDeviceToDevice, st));
+                I.captured[k] = 1;
+            }
             if (conv) { r.status = SK_STATUS_OPTIMAL; I.active[k] = 0; continue; }
             any = true;
             mumax = std::max(mumax, mu[k]);
@@ -935,11 +1109,13 @@ void DeviceIPM::run() {
         // precision for this iteration
         bool fp32 = o.precision == SK_PREC_MIXED && !I.switched && mumax >= o.mu_switch;
         if (o.precision == SK_PREC_MIXED && !I.switched && !fp32) {
+            if (o.verbose) std::fprintf(stderr, "[sk] FP64 fronts from iter %d: mu below mu_switch\n", iter);
             I.switched = true;
             for (int k = 0; k < nlp; ++k) if (I.active[k]) I.res[k].switch_iteration = iter;
         }
         bool ok_fac = factor(fp32);
         if (!ok_fac && fp32) {
+            if (o.verbose) std::fprintf(stderr, "[sk] FP64 fronts from iter %d: FP32 factorisation failed\n", iter);
             I.switched = true;
             for (int k = 0; k < nlp; ++k) if (I.active[k]) I.res[k].switch_iteration = iter;
             fp32 = false;
@@ -953,14 +1129,26 @@ void DeviceIPM::run() {
         // ---------------- predictor
         DirStats pd;
         std::vector<char> acc_p, use_p;
-        bool fac_ok = true;
-        for (int attempt = 0; attempt < 2; ++attempt) {
+        bool fac_ok = true, tightened = false;
+        // An FP32 direction that misses the check is first recomputed with the same
+        // factor and a 100x tighter PCG target; only a second miss moves to FP64 fronts.
+        auto tighten = [&](const std::vector<char>& acc) {
+            if (tightened) return false;
+            tightened = true;
+            for (int k = 0; k < nlp; ++k) if (I.active[k] && !acc[k]) tol[k] *= 0.01;
+            return true;
+        };
+        for (int attempt = 0; attempt < 3; ++attempt) {
             k_rhs<<<nblk(N), 256, 0, st>>>(N, I.x.ptr, I.s.ptr, I.theta.ptr, I.rd.ptr, nullptr, nullptr, nullptr,
                                           I.col_lp.ptr, I.rxs.ptr, I.v.ptr);
             direction(I.dxa.ptr, I.dya.ptr, I.dsa.ptr, I.rxs.ptr, acc_p, use_p, pd);
-            I.max_pcg_iter = I.last_pcg;
+            I.max_pcg_iter = std::max(tightened ? I.max_pcg_iter : 0, I.last_pcg);
             if (!fp32 || !any_active_missing(acc_p)) break;
+            if (tighten(acc_p)) continue;
             // an FP32 direction missed the reference accuracy: FP64 factor from here on
+            if (o.verbose)
+                std::fprintf(stderr, "[sk] FP64 fronts from iter %d: FP32 predictor missed the accuracy (pcg %d)\n",
+                             iter, I.last_pcg);
             fp32 = false;
             if (!(fac_ok = switch_to_fp64(iter))) break;
         }
@@ -981,17 +1169,23 @@ void DeviceIPM::run() {
         I.put_scalars(3, sigmu);
         DirStats cd;
         std::vector<char> acc_c, okc;
-        for (int attempt = 0; attempt < 2; ++attempt) {
+        for (int attempt = 0; attempt < 3; ++attempt) {
             k_rhs<<<nblk(N), 256, 0, st>>>(N, I.x.ptr, I.s.ptr, I.theta.ptr, I.rd.ptr, I.dxa.ptr, I.dsa.ptr, d_tgt,
                                           I.col_lp.ptr, I.rxs.ptr, I.v.ptr);
             direction(I.dx.ptr, I.dy.ptr, I.ds.ptr, I.rxs.ptr, acc_c, okc, cd);
             I.max_pcg_iter = std::max(I.max_pcg_iter, I.last_pcg);
             if (!fp32 || !any_active_missing(acc_c)) break;
+            if (tighten(acc_c)) continue;
+            if (o.verbose)
+                std::fprintf(stderr, "[sk] FP64 fronts from iter %d: FP32 corrector missed the accuracy (pcg %d)\n",
+                             iter, I.last_pcg);
             fp32 = false;
             if (!switch_to_fp64(iter)) { okc.assign(nlp, 0); break; }
         }
         // FP32 fronts that needed many PCG steps are not worth keeping: FP64 from the next iteration
         if (fp32 && I.max_pcg_iter > 20) {
+            if (o.verbose)
+                std::fprintf(stderr, "[sk] FP64 fronts from iter %d: %d PCG steps\n", iter + 1, I.max_pcg_iter);
             I.switched = true;
             for (int k = 0; k < nlp; ++k) if (I.active[k] && I.res[k].switch_iteration < 0) I.res[k].switch_iteration = iter + 1;
         }
@@ -1162,6 +1356,8 @@ void DeviceIPM::result(int lp, double* x, double* y, double* s, sk_info* info) c
         info->dense_front = p.dense_mode ? 1 : 0;
         info->device_ms = I.device_ms;
         info->flops_factor = p.flops_factor;
+        info->start_merit = r.start_merit;
+        info->fallback_merit = r.fallback_merit;
     }
 }
 

@@ -17,6 +17,8 @@
 namespace sankhya {
 namespace dev {
 
+class Gnn;
+
 struct LpResult {
     int status = SK_STATUS_ITERATION_LIMIT;
     int iterations = 0;
@@ -25,6 +27,8 @@ struct LpResult {
     double rel_pinf = 0.0, rel_dinf = 0.0, rel_gap = 0.0;
     int switch_iteration = -1;
     int learned_start = 0;
+    double start_merit = 0.0;      // max(rel pinf, rel dinf, rel gap) at the start point used
+    double fallback_merit = 0.0;   // same for Mehrotra's start (learned-start runs only)
 };
 
 class DeviceIPM {
@@ -34,6 +38,16 @@ public:
     ~DeviceIPM();
 
     void set_start(int lp, const double* x, const double* y, const double* s);
+    // Network used by SK_START_LEARNED (not owned).
+    void set_gnn(Gnn* g);
+    // Keep each LP's iterate (scaled space) at the first iteration whose mu is
+    // below `mu` (or the final iterate if mu never gets there); 0 disables.
+    void set_capture(double mu);
+    // Captured iterate as training targets: log x, log s (N) and y (M), device.
+    bool capture_complete() const;
+    const double* capture_logx() const;
+    const double* capture_logs() const;
+    const double* capture_y() const;
     void run();
     // Kernel-class breakdown at the current iterate (see sk_solver_profile).
     void profile(bool fp32, double* out16);

@@ -16,7 +16,7 @@ SK_ERR_NUMERICAL = 3
 SK_ERR_TOO_LARGE = 7
 STATUS = {0: "Optimal", 1: "Infeasible", 2: "Unbounded", 3: "IterationLimit"}
 PREC_FP64, PREC_MIXED = 0, 1
-START_UNIT, START_MEHROTRA, START_USER = 0, 1, 2
+START_UNIT, START_MEHROTRA, START_USER, START_LEARNED = 0, 1, 2, 3
 CRIT_RELATIVE, CRIT_REFERENCE = 0, 1
 ORDER_AUTO, ORDER_REFERENCE, ORDER_NATURAL = 0, 1, 2
 
@@ -28,7 +28,7 @@ class Options(C.Structure):
     _fields_ = [("precision", C.c_int), ("start", C.c_int), ("criteria", C.c_int), ("tol", C.c_double),
                 ("max_iter", C.c_int), ("ordering", C.c_int), ("verbose", C.c_int),
                 ("mu_switch", C.c_double), ("ruiz_passes", C.c_int), ("strict", C.c_int),
-                ("delta32", C.c_double), ("delta64", C.c_double)]
+                ("delta32", C.c_double), ("delta64", C.c_double), ("learned_accept", C.c_double)]
 
 
 class Info(C.Structure):
@@ -39,7 +39,7 @@ class Info(C.Structure):
                 ("solves", C.c_int), ("refine_steps", C.c_int), ("learned_start", C.c_int),
                 ("setup_ms", C.c_double), ("solve_ms", C.c_double), ("nnz_factor", C.c_longlong),
                 ("num_supernodes", C.c_int), ("dense_front", C.c_int), ("device_ms", C.c_double),
-                ("flops_factor", C.c_double)]
+                ("flops_factor", C.c_double), ("start_merit", C.c_double), ("fallback_merit", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -90,6 +90,23 @@ def _declare(L):
         L.sk_kkt_get_factor.argtypes = [vp, _f64p, _f64p]
         L.sk_kkt_destroy.argtypes = [vp]
         L.sk_spmv_csr.argtypes = [C.c_int, vp, vp, vp, vp, C.c_double, C.c_double, vp, vp]
+        _f32p = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
+        L.sk_gnn_create.argtypes = [C.c_ulonglong, C.POINTER(vp)]
+        L.sk_gnn_destroy.argtypes = [vp]
+        L.sk_gnn_num_params.argtypes = [vp]
+        L.sk_gnn_get_params.argtypes = [vp, _f32p]
+        L.sk_gnn_set_params.argtypes = [vp, _f32p]
+        L.sk_gnn_batch_create.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p, _f64p, _f64p, vp, vp, vp,
+                                          C.POINTER(vp)]
+        L.sk_gnn_batch_from_solver.argtypes = [vp, C.POINTER(vp)]
+        L.sk_gnn_batch_dims.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        L.sk_gnn_batch_destroy.argtypes = [vp]
+        L.sk_gnn_batch_targets.argtypes = [vp, vp, vp, vp]
+        L.sk_gnn_predict.argtypes = [vp, vp, vp, vp, vp]
+        L.sk_gnn_loss_grad.argtypes = [vp, vp, C.POINTER(C.c_double), vp]
+        L.sk_gnn_train_step.argtypes = [vp, vp, C.c_float, C.POINTER(C.c_double)]
+        L.sk_solver_set_gnn.argtypes = [vp, vp]
+        L.sk_solver_set_capture.argtypes = [vp, C.c_double]
 
 
 def last_error():
@@ -270,6 +287,15 @@ class Solver:
     def run(self):
         check(lib().sk_solver_run(self.h), "sk_solver_run")
 
+    def set_gnn(self, net):
+        """Network used when the solver was created with start=START_LEARNED."""
+        self._gnn = net
+        check(lib().sk_solver_set_gnn(self.h, net.h if net is not None else None), "sk_solver_set_gnn")
+
+    def set_capture(self, mu):
+        """Keep each LP's iterate the first time its mu < `mu` (training targets)."""
+        check(lib().sk_solver_set_capture(self.h, float(mu)), "sk_solver_set_capture")
+
     def result(self, k, want_vectors=True):
         lp = self.lps[k]
         info = Info()
@@ -331,6 +357,103 @@ class Kkt:
     def close(self):
         if self.h:
             lib().sk_kkt_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class GnnBatch:
+    """Graph(s) resident on the device for the learned-start network, with optional
+    targets (log x, log s, y in the LP's scaled space)."""
+
+    def __init__(self, handle):
+        self.h = handle
+        m, n = C.c_int(), C.c_int()
+        check(lib().sk_gnn_batch_dims(self.h, C.byref(m), C.byref(n)), "sk_gnn_batch_dims")
+        self.m, self.n = m.value, n.value
+
+    @classmethod
+    def from_arrays(cls, m, n, rp, ci, vals, b, c, targets=None):
+        rp, ci = (np.ascontiguousarray(a, dtype=np.int32) for a in (rp, ci))
+        vals, b, c = (np.ascontiguousarray(a, dtype=np.float64) for a in (vals, b, c))
+        keep = [None, None, None]
+        if targets is not None:
+            keep = [np.ascontiguousarray(a, dtype=np.float64) for a in targets]
+        h = C.c_void_p()
+        check(lib().sk_gnn_batch_create(m, n, rp, ci, vals, b, c, _ptr(keep[0]), _ptr(keep[1]), _ptr(keep[2]),
+                                        C.byref(h)), "sk_gnn_batch_create")
+        return cls(h)
+
+    @classmethod
+    def from_solver(cls, solver):
+        h = C.c_void_p()
+        check(lib().sk_gnn_batch_from_solver(solver.h, C.byref(h)), "sk_gnn_batch_from_solver")
+        return cls(h)
+
+    def targets(self):
+        lx, ls, y = np.zeros(self.n), np.zeros(self.n), np.zeros(self.m)
+        check(lib().sk_gnn_batch_targets(self.h, _ptr(lx), _ptr(ls), _ptr(y)), "sk_gnn_batch_targets")
+        return lx, ls, y
+
+    def close(self):
+        if self.h:
+            lib().sk_gnn_batch_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Gnn:
+    """Learned-start network (sk_gnn_*): BF16 weights on the device, FP32 master copy."""
+
+    def __init__(self, seed=1):
+        self.h = C.c_void_p()
+        check(lib().sk_gnn_create(seed, C.byref(self.h)), "sk_gnn_create")
+        self.num_params = lib().sk_gnn_num_params(self.h)
+
+    def get_params(self):
+        p = np.zeros(self.num_params, dtype=np.float32)
+        check(lib().sk_gnn_get_params(self.h, p), "sk_gnn_get_params")
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.size == self.num_params
+        check(lib().sk_gnn_set_params(self.h, p), "sk_gnn_set_params")
+
+    def predict(self, batch):
+        lx, ls, y = np.zeros(batch.n), np.zeros(batch.n), np.zeros(batch.m)
+        check(lib().sk_gnn_predict(self.h, batch.h, _ptr(lx), _ptr(ls), _ptr(y)), "sk_gnn_predict")
+        return lx, ls, y
+
+    def loss_grad(self, batch):
+        g = np.zeros(self.num_params, dtype=np.float32)
+        loss = C.c_double()
+        check(lib().sk_gnn_loss_grad(self.h, batch.h, C.byref(loss), g.ctypes.data), "sk_gnn_loss_grad")
+        return loss.value, g
+
+    def train_step(self, batch, lr):
+        loss = C.c_double()
+        check(lib().sk_gnn_train_step(self.h, batch.h, lr, C.byref(loss)), "sk_gnn_train_step")
+        return loss.value
+
+    def save(self, path):
+        np.save(path, self.get_params())
+
+    def load(self, path):
+        self.set_params(np.load(path))
+
+    def close(self):
+        if self.h:
+            lib().sk_gnn_destroy(self.h)
             self.h = C.c_void_p()
 
     def __del__(self):

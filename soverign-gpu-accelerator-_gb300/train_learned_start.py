@@ -1,0 +1,136 @@
+"""Trains the learned-start network on the uneven-batch LP family and evaluates
+it on held-out seeds.
+
+Family: family 3 of the generator (m ~ logUniform[200, 5000], n = ceil(m U[2, 3]),
+density U[0.5%, 2%], feasible and bounded by construction). Training targets are
+iterates of the plain FP64 IPM (Mehrotra's start): each LP's (log x, log s, y)
+in its Ruiz-scaled space the first time mu drops below --capture-mu. Training
+runs on the GPU through the engine's own BF16 forward / backward kernels and
+Adam (sk_gnn_train_step). Evaluation solves held-out LPs in mixed precision from
+Mehrotra's start and from the learned start (which falls back per LP to
+Mehrotra's start) and reports iterations, fallback rate and device time.
+
+usage: python train_learned_start.py [--train 1024] [--heldout 128] [--batch 16]
+           [--epochs 30] [--lr 2e-3] [--capture-mu 1e-2] [--out weights/learned_start_family3.npy]
+Writes the FP32 master weights (.npy) and a JSON report next to them.
+"""
+import argparse
+import json
+import math
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+import sankhya_gb300 as sk  # noqa: E402
+
+TRAIN_BASE = 100000     # family-3 instance numbers of the training set
+HELDOUT_BASE = 200000   # ... and of the held-out set (the benchmark batch uses 0..511)
+
+
+def solve_for_targets(instances, batch, capture_mu):
+    """Plain FP64 IPM over the instances in batches; returns device-resident
+    training batches (scaled LP + captured iterate) and per-LP iteration counts."""
+    out, iters, t0 = [], [], time.perf_counter()
+    for i in range(0, len(instances), batch):
+        lps = [sk.generate(3, k) for k in instances[i:i + batch]]
+        s = sk.Solver(lps, precision=sk.PREC_FP64, start=sk.START_MEHROTRA)
+        s.set_capture(capture_mu)
+        s.run()
+        infos = [s.result(k, want_vectors=False)[0] for k in range(len(lps))]
+        if all(inf["status"] == 0 for inf in infos):
+            out.append(sk.GnnBatch.from_solver(s))
+        iters += [inf["iterations"] for inf in infos]
+        s.close()
+    return out, iters, time.perf_counter() - t0
+
+
+def run_batch(lps, start, net=None, precision=sk.PREC_MIXED):
+    s = sk.Solver(lps, precision=precision, start=start)
+    if net is not None:
+        s.set_gnn(net)
+    s.run()                                  # first run builds the CUDA graphs
+    s.run()
+    infos = [s.result(k, want_vectors=False)[0] for k in range(len(lps))]
+    s.close()
+    return infos
+
+
+def evaluate(net, instances, batch):
+    rows = []
+    for i in range(0, len(instances), batch):
+        lps = [sk.generate(3, k) for k in instances[i:i + batch]]
+        base = run_batch(lps, sk.START_MEHROTRA)
+        lrn = run_batch(lps, sk.START_LEARNED, net)
+        for k in range(len(lps)):
+            b, l = base[k], lrn[k]
+            rows.append({"m": lps[k].m, "n": lps[k].n, "it_mehrotra": b["iterations"], "it_learned": l["iterations"],
+                         "learned_used": l["learned_start"], "ok": b["status"] == 0 and l["status"] == 0,
+                         "obj_rel_diff": abs(b["objective"] - l["objective"]) / (1 + abs(b["objective"])),
+                         "batch": i // batch, "ms_mehrotra": b["device_ms"], "ms_learned": l["device_ms"]})
+    nb = max(r["batch"] for r in rows) + 1
+    ms_b = sum(next(r["ms_mehrotra"] for r in rows if r["batch"] == q) for q in range(nb))
+    ms_l = sum(next(r["ms_learned"] for r in rows if r["batch"] == q) for q in range(nb))
+    n = len(rows)
+    return {"lps": n, "all_optimal": all(r["ok"] for r in rows),
+            "max_obj_rel_diff": max(r["obj_rel_diff"] for r in rows),
+            "mean_iterations_mehrotra": sum(r["it_mehrotra"] for r in rows) / n,
+            "mean_iterations_learned": sum(r["it_learned"] for r in rows) / n,
+            "fallback_rate": 1.0 - sum(r["learned_used"] for r in rows) / n,
+            "device_ms_mehrotra": ms_b, "device_ms_learned": ms_l,
+            "lps_per_s_mehrotra": 1000.0 * n / ms_b, "lps_per_s_learned": 1000.0 * n / ms_l}, rows
+
+
+def train(net, batches, epochs, lr0, seed, log_every=5):
+    rng = np.random.default_rng(seed)
+    steps = epochs * len(batches)
+    hist, step, t0 = [], 0, time.perf_counter()
+    for ep in range(epochs):
+        tot = 0.0
+        for q in rng.permutation(len(batches)):
+            lr = lr0 * 0.5 * (1.0 + math.cos(math.pi * step / steps))   # cosine decay
+            tot += net.train_step(batches[q], lr)
+            step += 1
+        hist.append(tot / len(batches))
+        if ep % log_every == 0 or ep == epochs - 1:
+            print("[train] epoch %d loss %.5f (%.1f s)" % (ep, hist[-1], time.perf_counter() - t0), flush=True)
+    return hist, time.perf_counter() - t0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--train", type=int, default=1024)
+    ap.add_argument("--heldout", type=int, default=128)
+    ap.add_argument("--batch", type=int, default=16)
+    ap.add_argument("--epochs", type=int, default=30)
+    ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--capture-mu", type=float, default=1e-2)
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--out", default=os.path.join(HERE, "weights", "learned_start_family3.npy"))
+    args = ap.parse_args()
+    tr, it_tr, t_solve = solve_for_targets(list(range(TRAIN_BASE, TRAIN_BASE + args.train)), args.batch,
+                                           args.capture_mu)
+    print("[data] %d training batches, plain FP64 solves %.1f s, mean iterations %.2f" %
+          (len(tr), t_solve, float(np.mean(it_tr))), flush=True)
+    net = sk.Gnn(args.seed)
+    hist, t_train = train(net, tr, args.epochs, args.lr, args.seed)
+    for b in tr:
+        b.close()
+    summary, rows = evaluate(net, list(range(HELDOUT_BASE, HELDOUT_BASE + args.heldout)), args.batch)
+    print(json.dumps(summary), flush=True)
+    os.makedirs(os.path.dirname(os.path.abspath(args.out)), exist_ok=True)
+    net.save(args.out)
+    rep = {"family": 3, "train_instances": [TRAIN_BASE, TRAIN_BASE + args.train],
+           "heldout_instances": [HELDOUT_BASE, HELDOUT_BASE + args.heldout], "batch": args.batch,
+           "epochs": args.epochs, "lr": args.lr, "capture_mu": args.capture_mu, "seed": args.seed,
+           "target_solve_s": t_solve, "train_s": t_train, "loss_history": hist, "heldout": summary,
+           "per_lp": rows}
+    with open(os.path.splitext(args.out)[0] + ".json", "w") as f:
+        json.dump(rep, f, indent=1)
+
+
+if __name__ == "__main__":
+    main()
