@@ -101,6 +101,32 @@ class Clocks:
                 "samples": len(sm)}
 
 
+def count_kernel_launches(fn):
+    """Kernels launched by one call of fn() (which launches only this library's
+    kernels), counted from a CUPTI trace (torch.profiler); graph-launched kernels
+    are included. Returns None if the profiler is unavailable."""
+    import tempfile
+    try:
+        import torch
+        from torch.profiler import ProfilerActivity, profile
+        acts = [ProfilerActivity.CPU, ProfilerActivity.CUDA]
+        with profile(activities=acts):       # the first session of a process records no kernels
+            torch.zeros(1, device="cuda").add_(1)
+            torch.cuda.synchronize()
+        with profile(activities=acts) as prof:
+            fn()
+            torch.cuda.synchronize()
+        with tempfile.NamedTemporaryFile(suffix=".json", delete=False) as f:
+            path = f.name
+        prof.export_chrome_trace(path)
+        with open(path) as f:
+            trace = json.load(f)
+        os.unlink(path)
+        return sum(1 for e in trace.get("traceEvents", []) if e.get("cat") == "kernel")
+    except Exception:
+        return None
+
+
 def dist_setup(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -157,6 +183,9 @@ def run_ours(args):
     clk = clocks.stop()
     total_ms = barrier_max(dist, sum(dev_ms))
     value = world * args.steps / (total_ms / 1000.0)
+    # kernels per solve, counted on one more (untimed) run of the same solve
+    per_run = count_kernel_launches(solver.run)
+    launches = per_run * args.steps if per_run is not None else None
     # kernel-class breakdown (instrumented replay of one factorisation + solve at the final iterate)
     prof = solver.profile(fp32=True)
     solver.close()
@@ -209,7 +238,8 @@ def run_ours(args):
             "kernel_breakdown_ms": {"mixed": {k: v for k, v in prof.items() if isinstance(v, dict)},
                                     "fp64": {k: v for k, v in prof64.items() if isinstance(v, dict)}},
             "wall_s_timed_region": wall,
-            "gpu_launches": None,
+            "gpu_launches": launches,
+            "gpu_launches_note": "kernels of libsankhya_gb300 per solve (CUPTI trace of one extra run) x steps",
             "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
             "e2e": {"value": e2e_value, "unit": "LPs/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": 1000.0 * e2e_total / len(e2e_t)}}

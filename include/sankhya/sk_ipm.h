@@ -41,7 +41,8 @@ extern "C" {
                                   when the prediction is not at least twice as close to the stopping test */
 
 /* Stopping rule. */
-#define SK_CRIT_RELATIVE 0     /* rel_pinf, rel_dinf, rel_gap <= tol and |c^T x - b^T y| <= tol (1 + |c^T x|), unscaled */
+#define SK_CRIT_RELATIVE 0     /* rel_pinf, rel_dinf, rel_gap <= tol and |c^T x - b^T y| <= tol (1 + |c^T x|), unscaled;
+                                  the first three alone for 3 iterations in a row also stop */
 #define SK_CRIT_REFERENCE 1    /* ||rp||_2, ||rd||_2, mu < 1e-6 on the scaled LP (src/ipm/mehrotra_device.cu:746-748) */
 
 /* Fill-reducing ordering of A A^T. */

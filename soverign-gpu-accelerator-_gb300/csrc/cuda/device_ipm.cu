@@ -33,9 +33,15 @@ namespace dev {
 
 namespace {
 
-constexpr int kChunk = 4096;
+constexpr int kChunk = 1024;   // entries per block of the segmented reductions
 constexpr int kMaxR = 10;
 constexpr double kLearnedSaturated = 0.99;   // learned start: upper bound on its distance to the stopping test
+constexpr double kShortStep = 0.1;           // learned-start restart: a step shorter than this ...
+constexpr int kShortSteps = 3;               // ... this many times ...
+constexpr int kRestartWindow = 10;           // ... within the first iterations
+constexpr int kLooseIters = 3;               // stall acceptance of the relative tests (see the stopping rule)
+constexpr int kProgressIter = 12;            // learned-start restart: by this iteration the distance to the
+constexpr double kProgress = 1e-3;           // stopping test must have fallen by this factor
 
 enum { OP_SUM = 0, OP_MAX = 1, OP_MIN = 2 };
 
@@ -439,6 +445,9 @@ struct DeviceIPM::Impl {
     double capture_mu = 0.0;                // iterate capture for training targets
     std::vector<char> captured;
     double *cap_lx = nullptr, *cap_ls = nullptr, *cap_y = nullptr;
+    double *mx0 = nullptr, *my0 = nullptr, *ms0 = nullptr;   // Mehrotra's start kept for learned-start restarts
+    std::vector<int> short_steps, loose_count;
+    std::vector<char> reinit;
 
     double* sc(int which) { return scal.ptr + static_cast<size_t>(which) * nlp; }
     double* tmpn() { return crxs.ptr; }   // scratch n-vector outside the backtracking phase
@@ -650,7 +659,7 @@ void DeviceIPM::profile(bool fp32, double* out16) {
 
 DeviceIPM::~DeviceIPM() {
     if (im_ && im_->ev0) { cudaEventDestroy(im_->ev0); cudaEventDestroy(im_->ev1); }
-    if (im_) for (double* p : {im_->cap_lx, im_->cap_ls, im_->cap_y}) if (p) cudaFree(p);
+    if (im_) for (double* p : {im_->cap_lx, im_->cap_ls, im_->cap_y, im_->mx0, im_->my0, im_->ms0}) if (p) cudaFree(p);
     kkt_.reset();
     if (im_ && im_->st) cudaStreamDestroy(im_->st);
 }
@@ -1051,6 +1060,14 @@ void DeviceIPM::run() {
             I.res[k].start_merit = keep[k] != 0.0 ? phiL[k] : phiM[k];
             I.res[k].fallback_merit = phiM[k];
         }
+        if (!I.mx0) {
+            SK_CUDA(cudaMalloc(&I.mx0, sizeof(double) * N));
+            SK_CUDA(cudaMalloc(&I.ms0, sizeof(double) * N));
+            SK_CUDA(cudaMalloc(&I.my0, sizeof(double) * M));
+        }
+        SK_CUDA(cudaMemcpyAsync(I.mx0, I.dxa.ptr, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
+        SK_CUDA(cudaMemcpyAsync(I.ms0, I.dsa.ptr, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
+        SK_CUDA(cudaMemcpyAsync(I.my0, I.dya.ptr, sizeof(double) * M, cudaMemcpyDeviceToDevice, st));
         I.put_scalars(0, keep);
         k_pick_lp<<<nblk(N), 256, 0, st>>>(N, d_mask, I.col_lp.ptr, I.x.ptr, I.dxa.ptr);
         k_pick_lp<<<nblk(N), 256, 0, st>>>(N, d_mask, I.col_lp.ptr, I.s.ptr, I.dsa.ptr);
@@ -1058,6 +1075,18 @@ void DeviceIPM::run() {
         SK_CUDA(cudaGetLastError());
     }
 
+    I.short_steps.assign(nlp, 0);
+    I.loose_count.assign(nlp, 0);
+    I.reinit.assign(nlp, 0);
+    // An LP started from the network's point goes back to Mehrotra's start (once)
+    // instead of stopping on a numerical failure.
+    std::vector<char> back_req(nlp, 0);
+    auto learned_rescue = [&](int k) {
+        if (o.start != SK_START_LEARNED || !I.res[k].learned_start) return false;
+        back_req[k] = 1;
+        I.active[k] = 0;    // sits out the rest of this iteration
+        return true;
+    };
     int iter = 0;
     std::vector<double> hm, hn;
     for (iter = 0; iter < o.max_iter; ++iter) {
@@ -1074,7 +1103,8 @@ void DeviceIPM::run() {
             nrp[k] = std::sqrt(hm[k * 3]);
             nrd[k] = std::sqrt(hn[k * 4]);
             mu[k] = hn[k * 4 + 2] / nn[k];
-            if (iter == 0) {
+            if (iter == 0 || I.reinit[k]) {
+                I.reinit[k] = 0;
                 I.rp0[k] = std::max(1.0, nrp[k]);
                 I.rd0[k] = std::max(1.0, nrd[k]);
                 I.mu0[k] = std::max(1.0, mu[k]);
@@ -1084,9 +1114,14 @@ void DeviceIPM::run() {
             r.iterations = iter;
             bool conv;
             if (o.criteria == SK_CRIT_REFERENCE) conv = nrp[k] < 1e-6 && nrd[k] < 1e-6 && mu[k] < 1e-6;
-            else   // the gap also within tol (1 + |c^T x|): the objective is then within tol of the optimum
-                conv = r.rel_pinf <= o.tol && r.rel_dinf <= o.tol && r.rel_gap <= o.tol &&
-                       std::fabs(r.objective - hm[k * 3 + 2]) <= o.tol * (1.0 + std::fabs(r.objective));
+            else {   // the gap also within tol (1 + |c^T x|): the objective is then within tol of the optimum
+                const bool loose = r.rel_pinf <= o.tol && r.rel_dinf <= o.tol && r.rel_gap <= o.tol;
+                conv = loose && std::fabs(r.objective - hm[k * 3 + 2]) <= o.tol * (1.0 + std::fabs(r.objective));
+                // an iterate that meets the three relative tests but cannot close the gap
+                // further (numerical stall) is accepted after kLooseIters iterations
+                I.loose_count[k] = loose && !conv ? I.loose_count[k] + 1 : 0;
+                if (I.loose_count[k] >= kLooseIters) conv = true;
+            }
             if (o.verbose)
                 std::fprintf(stderr, "[sk] lp %d iter %d rp %.3e rd %.3e mu %.3e gap %.3e %s\n", k, iter, nrp[k],
                              nrd[k], mu[k], r.rel_gap, I.switched || o.precision == SK_PREC_FP64 ? "fp64" : "fp32");
@@ -1159,7 +1194,10 @@ void DeviceIPM::run() {
         std::vector<double> sigmu(nlp, 0.0);
         for (int k = 0; k < nlp; ++k) {
             if (!I.active[k]) continue;
-            if (!use_p[k]) { I.res[k].status = SK_STATUS_ITERATION_LIMIT; I.active[k] = 0; continue; }
+            if (!use_p[k]) {
+                if (!learned_rescue(k)) { I.res[k].status = SK_STATUS_ITERATION_LIMIT; I.active[k] = 0; }
+                continue;
+            }
             const double apa = std::min(1.0, pd.rx[k]), ada = std::min(1.0, pd.rs[k]);
             const double mua = (pd.xs[k] + ada * pd.xds[k] + apa * pd.dxs[k] + apa * ada * pd.dxds[k]) / nn[k];
             const double sigma = std::min(1.0, std::pow(std::max(0.0, mua) / std::max(1e-16, mu[k]), 3.0));
@@ -1291,7 +1329,45 @@ void DeviceIPM::run() {
             k_masked_copy<<<nblk(M), 256, 0, st>>>(M, I.yt.ptr, I.row_lp.ptr, d_rmask, I.y.ptr);
         }
         for (int k = 0; k < nlp; ++k)
-            if (I.active[k] && !accepted[k]) { I.res[k].status = SK_STATUS_ITERATION_LIMIT; I.active[k] = 0; }
+            if (I.active[k] && !accepted[k] && !learned_rescue(k)) {
+                I.res[k].status = SK_STATUS_ITERATION_LIMIT;
+                I.active[k] = 0;
+            }
+        // Learned-start safeguard: an LP started from the network's point that takes a
+        // short step (min(a_p, a_d) < kShortStep) in kShortSteps of its first
+        // kRestartWindow iterations, or that hit a numerical failure, goes back to
+        // Mehrotra's start.
+        if (o.start == SK_START_LEARNED) {
+            std::vector<double> back(nlp, 0.0);
+            bool any_back = false;
+            for (int k = 0; k < nlp; ++k) {
+                if (!I.res[k].learned_start) continue;
+                bool go = back_req[k] != 0;
+                if (!go && iter < kRestartWindow && I.active[k] && accepted[k] &&
+                    std::min(ap[k], ad[k]) < kShortStep && ++I.short_steps[k] >= kShortSteps)
+                    go = true;
+                // too little progress: the distance to the stopping test has not fallen by
+                // kProgress since the start after kProgressIter iterations
+                const LpResult& rk = I.res[k];
+                if (!go && iter == kProgressIter && I.active[k] &&
+                    std::max({rk.rel_pinf, rk.rel_dinf, rk.rel_gap}) > kProgress * rk.start_merit)
+                    go = true;
+                if (!go) continue;
+                back[k] = 1.0;
+                any_back = true;
+                back_req[k] = 0;
+                I.active[k] = 1;
+                I.res[k].learned_start = 0;
+                I.reinit[k] = 1;
+                if (o.verbose) std::fprintf(stderr, "[sk] lp %d: learned start abandoned, Mehrotra's start\n", k);
+            }
+            if (any_back) {
+                I.put_scalars(4, back);
+                k_masked_copy<<<nblk(N), 256, 0, st>>>(N, I.mx0, I.col_lp.ptr, d_rmask, I.x.ptr);
+                k_masked_copy<<<nblk(N), 256, 0, st>>>(N, I.ms0, I.col_lp.ptr, d_rmask, I.s.ptr);
+                k_masked_copy<<<nblk(M), 256, 0, st>>>(M, I.my0, I.row_lp.ptr, d_rmask, I.y.ptr);
+            }
+        }
     }
     // LPs still running at the iteration cap: final residuals (mehrotra_device.cu:1026-1035)
     bool any_left = false;

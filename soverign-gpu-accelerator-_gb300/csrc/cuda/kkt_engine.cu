@@ -6,9 +6,10 @@
 //               k_trsm           panel rows below the tile: X L^T = B
 //               k_update         trailing update C -= L_i L_j^T (tiles of 64x64)
 //               k_extend_add     child update matrix into the parent front
-//   solve       k_fwd_init / k_fwd_diag / k_fwd_gemv      L z = r, multifrontal
-//               k_bwd_init / k_bwd_partial / k_bwd_diag   L^T x = z
-// Every kernel's grid is a list of (front, tile) work items of one level / step,
+//   solve       k_fwd_gather     frontal right-hand sides of one level
+//               k_fwd_tasks      L z = r, dependency-driven 64-row block tasks
+//               k_bwd_tasks      L^T x = z, same scheme in reverse
+// Factorisation grids are lists of (front, tile) work items of one level / step,
 // decoded with a binary search over a prefix of per-front tile counts.
 #include "cuda/kkt_engine.hpp"
 
@@ -145,25 +146,24 @@ __global__ void k_asm_cols_dense(int M, const int* __restrict__ rp, const int* _
 // Cholesky of the 64x64 diagonal tile of step k of one front, in the front's
 // precision T, plus the explicit inverse of the factored tile (used by the panel
 // solve and by both triangular solves), stored column-major in Linv.
-// 256 threads on a shared tile: four threads per row share each rank-1 update,
-// four threads per column share each inverse substitution (shuffle-reduced);
-// loops stay rolled so the code is small. A partial tile is padded with the identity.
+// Blocked by 16 columns so that the block-wide barriers are few: warp 0 factors
+// each 16x16 diagonal block (warp-synchronous), one thread per row solves the
+// panel below it, and all threads apply the trailing update. The inverse: four
+// warps invert the four diagonal blocks, then block rows of L^{-1} follow as
+// X_ij = -X_ii (sum_k L_ik X_kj). A partial tile is padded with the identity.
 template <class T>
-__global__ void __launch_bounds__(256) k_potrf(StepArgs a, const int* __restrict__ items, PlanDev pd, T* F,
-                                               T* __restrict__ Linv, const int64_t* __restrict__ inv_off,
-                                               int* err) {
-    extern __shared__ __align__(16) unsigned char smraw[];
-    T* A = reinterpret_cast<T*>(smraw);
-    T* X = A + T64 * LDS;
-    T* rdiag = X + T64 * LDS;
-    T* col = rdiag + T64;                 // scaled column c, read by all rows
-    const int s = items[a.item_off + blockIdx.x];
+__device__ __noinline__ void potrf_tile(int s, int kstep, PlanDev pd, T* F, T* __restrict__ Linv,
+                           const int64_t* __restrict__ inv_off, int* err, unsigned char* smraw) {
+    constexpr int B = 16;
+    T* A = reinterpret_cast<T*>(smraw);   // A[r * LDS + c], lower triangle
+    T* X = A + T64 * LDS;                 // L^{-1}, same layout
+    T* rdiag = X + T64 * LDS;             // 1 / L(c, c)
     const int K = pd.sn_ncols[s];
     const int LD = pd.sn_lda[s];
-    const int k0 = a.k * T64;
+    const int k0 = kstep * T64;
     const int w = min(T64, K - k0);
     T* Fs = F + pd.F_off[s];
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
 #pragma unroll 4
     for (int it = 0; it < 16; ++it) {
         const int idx = tid + it * 256;
@@ -172,35 +172,58 @@ __global__ void __launch_bounds__(256) k_potrf(StepArgs a, const int* __restrict
         if (r < w && c < w && c <= r) x = Fs[(k0 + r) + static_cast<int64_t>(k0 + c) * LD];
         else if (r == c) x = T(1);
         A[r * LDS + c] = x;
+        X[r * LDS + c] = T(0);
     }
-    auto pivot = [&](int c) {
-        T p = A[c * LDS + c];
-        if (!(p > T(0))) {
-            if (atomicCAS(err, 0, 1) == 0) err[1] = s;
-            p = T(1);
-        }
-        const T d = sqrt(p);
-        A[c * LDS + c] = d;
-        rdiag[c] = T(1) / d;
-    };
     __syncthreads();
-    if (tid == 0) pivot(0);
-    __syncthreads();
-    const int rr = tid >> 2, part = tid & 3;
-    for (int c = 0; c < T64; ++c) {
-        if (tid < T64 && tid > c) {
-            const T l = A[tid * LDS + c] * rdiag[c];
-            A[tid * LDS + c] = l;
-            col[tid] = l;
+    for (int c0 = 0; c0 < T64; c0 += B) {
+        if (wid == 0) {            // 16x16 diagonal block, lanes 0..15 own its rows
+            const int rr = c0 + (lane & 15);
+            for (int jj = 0; jj < B; ++jj) {
+                const int c = c0 + jj;
+                if (lane == 0) {
+                    T p = A[c * LDS + c];
+                    if (!(p > T(0))) {
+                        if (atomicCAS(err, 0, 1) == 0) err[1] = s;
+                        p = T(1);
+                    }
+                    const T d = sqrt(p);
+                    A[c * LDS + c] = d;
+                    rdiag[c] = T(1) / d;
+                }
+                __syncwarp();
+                if (lane < B && rr > c) A[rr * LDS + c] *= rdiag[c];
+                __syncwarp();
+                if (rr > c) {
+                    const T l = A[rr * LDS + c];
+                    for (int cc = c + 1 + (lane >> 4); cc <= rr; cc += 2) A[rr * LDS + cc] -= l * A[cc * LDS + c];
+                }
+                __syncwarp();
+            }
         }
         __syncthreads();
-        if (rr > c) {
-            const T l = col[rr];
-            T* Ar = A + rr * LDS;
-            for (int cc = c + 1 + part; cc <= rr; cc += 4) Ar[cc] -= l * col[cc];
+        const int t0 = c0 + B, nt = T64 - t0;
+        if (tid < nt) {            // panel row r: X L_kk^T = A_r
+            const int r = t0 + tid;
+            T x[B];
+#pragma unroll
+            for (int jj = 0; jj < B; ++jj) {
+                T v = A[r * LDS + c0 + jj];
+#pragma unroll
+                for (int q = 0; q < jj; ++q) v -= x[q] * A[(c0 + jj) * LDS + c0 + q];
+                x[jj] = v * rdiag[c0 + jj];
+            }
+#pragma unroll
+            for (int jj = 0; jj < B; ++jj) A[r * LDS + c0 + jj] = x[jj];
         }
         __syncthreads();
-        if (tid == 0 && c + 1 < T64) pivot(c + 1);
+        for (int e = tid; e < nt * nt; e += 256) {   // trailing lower triangle
+            const int r = t0 + e / nt, cc = t0 + e % nt;
+            if (cc > r) continue;
+            T v = A[r * LDS + cc];
+#pragma unroll
+            for (int q = 0; q < B; ++q) v -= A[r * LDS + c0 + q] * A[cc * LDS + c0 + q];
+            A[r * LDS + cc] = v;
+        }
         __syncthreads();
     }
 #pragma unroll 4
@@ -209,25 +232,68 @@ __global__ void __launch_bounds__(256) k_potrf(StepArgs a, const int* __restrict
         const int r = idx & 63, c = idx >> 6;
         if (r < w && c < w && c <= r) Fs[(k0 + r) + static_cast<int64_t>(k0 + c) * LD] = A[r * LDS + c];
     }
-    // X = L^{-1}, column j by four threads: X(i,j) = (delta_ij - sum_{q=j}^{i-1} L(i,q) X(q,j)) / L(i,i)
-    const int j = tid >> 2;
-    for (int i = 0; i < T64; ++i) {
-        T acc = T(0);
-        if (i > j)
-            for (int q = j + part; q < i; q += 4) acc += A[i * LDS + q] * X[q * LDS + j];
-        acc += __shfl_xor_sync(0xffffffffu, acc, 1);
-        acc += __shfl_xor_sync(0xffffffffu, acc, 2);
-        if (part == 0) X[i * LDS + j] = (i < j) ? T(0) : (((i == j) ? T(1) : T(0)) - acc) * rdiag[i];
-        __syncwarp();
+    // inverse of the diagonal blocks: warp b, lane = column of block b
+    if (wid < T64 / B && lane < B) {
+        const int c0 = wid * B, j = c0 + lane;
+        for (int i = j; i < c0 + B; ++i) {
+            T acc = (i == j) ? T(1) : T(0);
+            for (int q = j; q < i; ++q) acc -= A[i * LDS + q] * X[q * LDS + j];
+            X[i * LDS + j] = acc * rdiag[i];
+        }
     }
     __syncthreads();
-    T* Li = Linv + inv_off[s] + static_cast<int64_t>(a.k) * T64 * T64;
+    // block rows 1..3: T_ij = sum_{q < r0} L(i, q) X(q, j), then X_ij = -X_ii T_ij
+    for (int r0 = B; r0 < T64; r0 += B) {
+        const int cnt = r0 * B;            // (r0 / B) blocks of 16x16
+        for (int e = tid; e < cnt; e += 256) {
+            const int i = r0 + (e % (B * B)) / B, j = (e / (B * B)) * B + e % B;
+            T acc = T(0);
+            for (int q = (e / (B * B)) * B; q < r0; ++q) acc += A[i * LDS + q] * X[q * LDS + j];
+            X[i * LDS + j] = acc;
+        }
+        __syncthreads();
+        T out[3];
+#pragma unroll
+        for (int u = 0; u < 3; ++u) {
+            const int e = tid + u * 256;
+            out[u] = T(0);
+            if (e < cnt) {
+                const int rr = (e % (B * B)) / B, i = r0 + rr, j = (e / (B * B)) * B + e % B;
+                T acc = T(0);
+                for (int q = 0; q <= rr; ++q) acc += X[i * LDS + r0 + q] * X[(r0 + q) * LDS + j];
+                out[u] = -acc;
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int u = 0; u < 3; ++u) {
+            const int e = tid + u * 256;
+            if (e < cnt) {
+                const int i = r0 + (e % (B * B)) / B, j = (e / (B * B)) * B + e % B;
+                X[i * LDS + j] = out[u];
+            }
+        }
+        __syncthreads();
+    }
+    T* Li = Linv + inv_off[s] + static_cast<int64_t>(kstep) * T64 * T64;
 #pragma unroll 4
     for (int it = 0; it < 16; ++it) {
         const int idx = tid + it * 256;
         const int i = idx & 63, jj = idx >> 6;
         Li[i + jj * T64] = (i < w && jj < w) ? X[i * LDS + jj] : T(0);
     }
+}
+
+constexpr size_t potrf_smem(size_t elem) { return (2 * T64 * LDS + 2 * T64) * elem; }
+
+// Diagonal-tile Cholesky of the first step of each front of a level (later steps
+// are factored at the end of the previous step's update, see k_update).
+template <class T>
+__global__ void __launch_bounds__(256) k_potrf(StepArgs a, const int* __restrict__ items, PlanDev pd, T* F,
+                                               T* __restrict__ Linv, const int64_t* __restrict__ inv_off,
+                                               int* err) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    potrf_tile<T>(items[a.item_off + blockIdx.x], a.k, pd, F, Linv, inv_off, err, smraw);
 }
 
 // Panel rows below the diagonal tile: X = B L_kk^{-T} = B Linv^T (a small GEMM).
@@ -279,7 +345,9 @@ __global__ void __launch_bounds__(256) k_trsm(StepArgs a, const int* __restrict_
 // before any arithmetic, so every global load of a thread is in flight at once.
 template <class T>
 __global__ void __launch_bounds__(256) k_update(StepArgs a, const int* __restrict__ items,
-                                                const int* __restrict__ prefix, PlanDev pd, T* F) {
+                                                const int* __restrict__ prefix, PlanDev pd, T* F,
+                                                T* __restrict__ Linv, const int64_t* __restrict__ inv_off,
+                                                int* err) {
     extern __shared__ __align__(16) unsigned char smraw[];
     T* As = reinterpret_cast<T*>(smraw);     // [kk][r]
     T* Bs = As + T64 * T64;                  // [kk][c]
@@ -346,6 +414,12 @@ __global__ void __launch_bounds__(256) k_update(StepArgs a, const int* __restric
             if (r < nri && c < ncj && (ti != tj || r >= c))
                 Fs[(ri0 + r) + static_cast<int64_t>(cj0 + c) * LD] = cv[q][p] - acc[q][p];
         }
+    // The block that finished the first trailing diagonal tile factors it right away
+    // (step k + 1's diagonal tile), overlapping the rest of this step's update.
+    if (lt == 0 && t0 < K) {
+        __syncthreads();
+        potrf_tile<T>(s, a.k + 1, pd, F, Linv, inv_off, err, smraw);
+    }
 }
 
 template <class T>
@@ -390,25 +464,19 @@ __global__ void k_unpermute_scale(int M, const int* __restrict__ perm, const dou
     if (q < M) dst[perm[q]] = D[q] * static_cast<double>(xp[q]);
 }
 
-// Frontal right-hand side: own entries of the permuted rhs, then the children's
-// update vectors added in a fixed order.
+// Frontal right-hand sides of one level: one thread per front row, the row's own
+// entry of the permuted rhs (or 0 outside the front's columns) plus the children's
+// update-vector entries that map to it, added in child order.
 template <class T>
-__global__ void k_fwd_init(const int* __restrict__ level_sn, PlanDev pd, const T* __restrict__ zp,
-                           T* __restrict__ fv) {
-    const int s = level_sn[blockIdx.x];
-    const int N = pd.sn_nrows[s], K = pd.sn_ncols[s], first = pd.sn_first[s];
-    const int LD = pd.sn_lda[s];
-    T* f = fv + pd.f_off[s];
-    for (int q = threadIdx.x; q < N; q += blockDim.x) f[q] = q < K ? zp[first + q] : T(0);
-    __syncthreads();
-    for (int e = pd.ch_ptr[s]; e < pd.ch_ptr[s + 1]; ++e) {
-        const int c = pd.ch_list[e];
-        const int Kc = pd.sn_ncols[c], u = pd.sn_nrows[c] - Kc;
-        const T* uc = fv + pd.f_off[c] + Kc;
-        const int* map = pd.ea_map + pd.ea_off[c];
-        for (int t = threadIdx.x; t < u; t += blockDim.x) f[map[t]] += uc[t];
-        __syncthreads();
-    }
+__global__ void k_fwd_gather(int n, const int* __restrict__ dst, const int* __restrict__ zpi,
+                             const int* __restrict__ ptr, const int* __restrict__ src, const T* __restrict__ zp,
+                             T* __restrict__ fv) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int z = zpi[t];
+    T acc = z >= 0 ? zp[z] : T(0);
+    for (int q = ptr[t]; q < ptr[t + 1]; ++q) acc += fv[src[q]];
+    fv[dst[t]] = acc;
 }
 
 // ---- dependency-driven triangular solves -------------------------------------
@@ -437,19 +505,26 @@ __device__ __forceinline__ bool wait_flag(const int* flag, int target, int* err,
 template <class T>
 __device__ __forceinline__ T ld_cg(const T* p) { return __ldcg(p); }
 
+constexpr int kReadyBlocks = 16;   // column blocks taken per pass once their flags are set
+
+__device__ __forceinline__ int flag_now(const int* flag) { return *reinterpret_cast<const volatile int*>(flag); }
+
 // Forward: task (s, i). Own block i < nb covers rows [64 i, min(64 i + 64, K));
 // external block i >= nb covers rows [K + 64 (i - nb), ...) < N. The task forms
 // f_rows - sum_{j < min(i, nb)} L(rows, block j) z_j; an own block then stores
 // z_i = Linv_i (..) in zsol and flags 1, an external block stores the parent's
-// update vector in f.
+// update vector in f. Column blocks whose flags are already set are taken
+// together (up to kReadyBlocks per pass); the first block of each pass has its L
+// values loaded before the wait, so the latency-critical last dependency only
+// waits for its flag and z values.
 template <class T>
 __global__ void __launch_bounds__(256) k_fwd_tasks(const int2* __restrict__ tasks, int ntasks, int* counter,
                                                    PlanDev pd, const T* __restrict__ F, const T* __restrict__ Linv,
                                                    const int64_t* __restrict__ inv_off,
                                                    const int* __restrict__ blk_off, int* flags, T* fv, T* zsol,
                                                    int* err) {
-    __shared__ int task_sh, abort_sh;
-    __shared__ T zj[T64];
+    __shared__ int task_sh, abort_sh, ready_sh;
+    __shared__ T zs[kReadyBlocks * T64];
     __shared__ T red[4][T64];
     __shared__ T fb[T64];
     const int tid = threadIdx.x;
@@ -473,21 +548,55 @@ __global__ void __launch_bounds__(256) k_fwd_tasks(const int2* __restrict__ task
     const int rend = own ? K : N;
     const int row = row0 + r;
     const bool rv = row < rend;
+    // this thread's entries of the diagonal-tile inverse (own blocks), loaded up front
+    const int w = own ? min(T64, K - i * T64) : 0;
+    const int zc = tid >> 2, zpart = tid & 3;
+    T li[16];
+    if (own) {
+        const T* Li = Linv + inv_off[s] + static_cast<int64_t>(i) * T64 * T64;
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+            const int q = zpart + 4 * k;
+            li[k] = (zc < w && q <= zc) ? Li[zc + q * T64] : T(0);
+        }
+    }
     T acc = T(0);
     const int jmax = own ? i : nb;
-    for (int j = 0; j < jmax; ++j) {
-        if (tid == 0) wait_flag(fl + j, 1, err, &abort_sh);
-        __syncthreads();
-        if (abort_sh) return;
-        if (tid < T64) zj[tid] = (j * T64 + tid < K) ? ld_cg(zsol + first + j * T64 + tid) : T(0);
-        __syncthreads();
-        if (rv) {
-            const T* Lc = Fs + row + static_cast<int64_t>(j * T64 + cg * 16) * LD;
+    for (int j = 0; j < jmax;) {
+        T pre[16];
+        const int colp = j * T64 + cg * 16;
 #pragma unroll
-            for (int c = 0; c < 16; ++c)
-                if (j * T64 + cg * 16 + c < K) acc += Lc[static_cast<int64_t>(c) * LD] * zj[cg * 16 + c];
+        for (int c = 0; c < 16; ++c)
+            pre[c] = (rv && colp + c < K) ? Fs[row + static_cast<int64_t>(colp + c) * LD] : T(0);
+        if (tid == 0) {
+            if (wait_flag(fl + j, 1, err, &abort_sh)) {
+                int e = j + 1;
+                while (e < jmax && e < j + kReadyBlocks && flag_now(fl + e) >= 1) ++e;
+                __threadfence();
+                ready_sh = e;
+            }
         }
         __syncthreads();
+        if (abort_sh) return;
+        const int e = ready_sh;
+        for (int q = tid; q < (e - j) * T64; q += 256) {
+            const int col = j * T64 + q;
+            zs[q] = col < K ? ld_cg(zsol + first + col) : T(0);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int c = 0; c < 16; ++c) acc += pre[c] * zs[cg * 16 + c];
+        if (rv) {
+            for (int jj = j + 1; jj < e; ++jj) {
+                const T* Lc = Fs + row + static_cast<int64_t>(jj * T64 + cg * 16) * LD;
+                const T* zz = zs + (jj - j) * T64 + cg * 16;
+#pragma unroll
+                for (int c = 0; c < 16; ++c)
+                    if (jj * T64 + cg * 16 + c < K) acc += Lc[static_cast<int64_t>(c) * LD] * zz[c];
+            }
+        }
+        __syncthreads();
+        j = e;
     }
     red[cg][r] = acc;
     __syncthreads();
@@ -497,15 +606,15 @@ __global__ void __launch_bounds__(256) k_fwd_tasks(const int2* __restrict__ task
     }
     __syncthreads();
     if (own) {
-        const int w = min(T64, K - i * T64);
-        const T* Li = Linv + inv_off[s] + static_cast<int64_t>(i) * T64 * T64;
-        const int c = tid >> 2, part = tid & 3;
         T z = T(0);
-        if (c < w)
-            for (int q = part; q <= c; q += 4) z += Li[c + q * T64] * fb[q];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+            const int q = zpart + 4 * k;
+            if (q <= zc) z += li[k] * fb[q];
+        }
         z += __shfl_xor_sync(0xffffffffu, z, 1);
         z += __shfl_xor_sync(0xffffffffu, z, 2);
-        if (part == 0 && c < w) zsol[first + i * T64 + c] = z;
+        if (zpart == 0 && zc < w) zsol[first + i * T64 + zc] = z;
         __threadfence();
         __syncthreads();
         if (tid == 0) atomicExch(fl + i, 1);
@@ -516,15 +625,17 @@ __global__ void __launch_bounds__(256) k_fwd_tasks(const int2* __restrict__ task
 
 // Backward: task (s, i), i descending: x_i = Linv_i^T (z_i - sum_{rows r below
 // block i} L(r, block i)^T x_r); rows of own later blocks wait for their flag (2),
-// rows outside the front's columns come from ancestors (earlier levels).
+// rows outside the front's columns come from ancestors (earlier levels). Later
+// blocks are taken oldest first (nb - 1 downwards), ready ones together, and the
+// L values of the first block of each pass are loaded before its wait.
 template <class T>
 __global__ void __launch_bounds__(256) k_bwd_tasks(const int2* __restrict__ tasks, int ntasks, int* counter,
                                                    PlanDev pd, const T* __restrict__ F, const T* __restrict__ Linv,
                                                    const int64_t* __restrict__ inv_off,
                                                    const int* __restrict__ blk_off, int* flags, T* xp,
                                                    const T* __restrict__ zsol, int* err) {
-    __shared__ int task_sh, abort_sh;
-    __shared__ T xb[T64];
+    __shared__ int task_sh, abort_sh, ready_sh;
+    __shared__ T xb[kReadyBlocks * T64];   // x of ready own blocks, or of a chunk of outside rows
     __shared__ T tb[T64];
     const int tid = threadIdx.x;
     if (tid == 0) {
@@ -547,30 +658,78 @@ __global__ void __launch_bounds__(256) k_bwd_tasks(const int2* __restrict__ task
 #pragma unroll
     for (int q = 0; q < 8; ++q) part[q] = T(0);
     const int c0 = i * T64 + wid * 8;
-    // rows outside the front's own columns (solved by ancestors)
-    for (int r = K + lane; r < N; r += 32) {
-        const T xr = xp[R[r]];
-#pragma unroll
-        for (int q = 0; q < 8; ++q)
-            if (c0 + q < K) part[q] += Fs[r + static_cast<int64_t>(c0 + q) * LD] * xr;
-    }
-    // rows of own later blocks: the oldest (already solved) first, the newest
-    // dependency (block i + 1) last, so the wavefront does not serialise
-    for (int j = nb - 1; j > i; --j) {
-        if (tid == 0) wait_flag(fl + j, 2, err, &abort_sh);
+    // rows outside the front's own columns (solved by ancestors): their x values are
+    // gathered into shared memory a chunk at a time, then each warp runs down the rows
+    constexpr int kOut = kReadyBlocks * T64;
+    for (int r0 = K; r0 < N; r0 += kOut) {
+        const int nr = min(kOut, N - r0);
+        for (int q = tid; q < nr; q += 256) xb[q] = xp[R[r0 + q]];
         __syncthreads();
-        if (abort_sh) return;
-        if (tid < T64) xb[tid] = (j * T64 + tid < K) ? ld_cg(xp + first + j * T64 + tid) : T(0);
-        __syncthreads();
-        for (int rr = lane; rr < T64; rr += 32) {
-            const int r = j * T64 + rr;
-            if (r >= K) break;
-            const T xr = xb[rr];
+        for (int q = lane; q < nr; q += 32) {
+            const T xr = xb[q];
+            const T* Fr = Fs + (r0 + q);
 #pragma unroll
-            for (int q = 0; q < 8; ++q)
-                if (c0 + q < K) part[q] += Fs[r + static_cast<int64_t>(c0 + q) * LD] * xr;
+            for (int u = 0; u < 8; ++u)
+                if (c0 + u < K) part[u] += Fr[static_cast<int64_t>(c0 + u) * LD] * xr;
         }
         __syncthreads();
+    }
+    // this thread's entries of the diagonal-tile inverse
+    const int xc = tid >> 2, xpq = tid & 3;
+    T li[16];
+    {
+        const T* Li = Linv + inv_off[s] + static_cast<int64_t>(i) * T64 * T64;
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+            const int q = xc + xpq + 4 * k;
+            li[k] = (xc < w && q < w) ? Li[q + xc * T64] : T(0);
+        }
+    }
+    // rows of own later blocks
+    for (int j = nb - 1; j > i;) {
+        T pre[16];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int rr = j * T64 + lane + 32 * h;
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+                pre[h * 8 + q] = (rr < K && c0 + q < K) ? Fs[rr + static_cast<int64_t>(c0 + q) * LD] : T(0);
+        }
+        if (tid == 0) {
+            if (wait_flag(fl + j, 2, err, &abort_sh)) {
+                int e = j - 1;
+                while (e > i && e > j - kReadyBlocks && flag_now(fl + e) >= 2) --e;
+                __threadfence();
+                ready_sh = e;
+            }
+        }
+        __syncthreads();
+        if (abort_sh) return;
+        const int e = ready_sh;   // blocks j, j - 1, ..., e + 1 are ready
+        for (int q = tid; q < (j - e) * T64; q += 256) {
+            const int blk = j - q / T64, rr = blk * T64 + q % T64;
+            xb[q] = rr < K ? ld_cg(xp + first + rr) : T(0);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const T xr = xb[lane + 32 * h];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) part[q] += pre[h * 8 + q] * xr;
+        }
+        for (int blk = j - 1; blk > e; --blk) {
+            const T* xx = xb + (j - blk) * T64;
+            for (int rr = lane; rr < T64; rr += 32) {
+                const int r = blk * T64 + rr;
+                if (r >= K) break;
+                const T xr = xx[rr];
+#pragma unroll
+                for (int q = 0; q < 8; ++q)
+                    if (c0 + q < K) part[q] += Fs[r + static_cast<int64_t>(c0 + q) * LD] * xr;
+            }
+        }
+        __syncthreads();
+        j = e;
     }
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
@@ -583,14 +742,15 @@ __global__ void __launch_bounds__(256) k_bwd_tasks(const int2* __restrict__ task
     }
     __syncthreads();
     {
-        const T* Li = Linv + inv_off[s] + static_cast<int64_t>(i) * T64 * T64;
-        const int c = tid >> 2, pq = tid & 3;
         T x = T(0);
-        if (c < w)
-            for (int q = c + pq; q < w; q += 4) x += Li[q + c * T64] * tb[q];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+            const int q = xc + xpq + 4 * k;
+            if (q < w) x += li[k] * tb[q];
+        }
         x += __shfl_xor_sync(0xffffffffu, x, 1);
         x += __shfl_xor_sync(0xffffffffu, x, 2);
-        if (pq == 0 && c < w) xp[first + i * T64 + c] = x;
+        if (xpq == 0 && xc < w) xp[first + i * T64 + xc] = x;
     }
     __threadfence();
     __syncthreads();
@@ -634,11 +794,11 @@ struct KktEngine::Prof {
 template <class T>
 static void set_smem_attrs() {
     SK_CUDA(cudaFuncSetAttribute(k_potrf<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 static_cast<int>((2 * T64 * LDS + 2 * T64) * sizeof(T))));
+                                 static_cast<int>(potrf_smem(sizeof(T)))));
     SK_CUDA(cudaFuncSetAttribute(k_trsm<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  static_cast<int>(2 * T64 * T64 * sizeof(T))));
     SK_CUDA(cudaFuncSetAttribute(k_update<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 static_cast<int>(2 * T64 * T64 * sizeof(T))));
+                                 static_cast<int>(potrf_smem(sizeof(T)))));
 }
 
 KktEngine::KktEngine(const ipm::FrontPlan& plan, const DeviceLP& lp, cudaStream_t stream)
@@ -675,6 +835,36 @@ KktEngine::KktEngine(const ipm::FrontPlan& plan, const DeviceLP& lp, cudaStream_
     }
     fwd_task_off_[p.nlevels] = static_cast<int>(ftask.size());
     bwd_task_off_[p.nlevels] = static_cast<int>(btask.size());
+    // forward right-hand-side gather lists (one item per front row, level by level)
+    if (p.f_size >= (int64_t(1) << 31)) throw std::runtime_error("front vectors exceed 2^31 entries");
+    std::vector<int> g_dst, g_zp, g_ptr(1, 0), g_src;
+    gather_off_.assign(static_cast<size_t>(p.nlevels) + 1, 0);
+    for (int l = 0; l < p.nlevels; ++l) {
+        gather_off_[l] = static_cast<int>(g_dst.size());
+        for (int q = p.level_ptr[l]; q < p.level_ptr[l + 1]; ++q) {
+            const int s = p.level_sn[q];
+            const int N = p.sn_nrows[s], K = p.sn_ncols[s];
+            std::vector<int> cnt(static_cast<size_t>(N) + 1, 0);
+            for (int e = p.ch_ptr[s]; e < p.ch_ptr[s + 1]; ++e) {
+                const int c = p.ch_list[e], u = p.sn_nrows[c] - p.sn_ncols[c];
+                for (int r = 0; r < u; ++r) cnt[p.ea_map[p.ea_off[c] + r] + 1]++;
+            }
+            for (int r = 0; r < N; ++r) cnt[r + 1] += cnt[r];
+            std::vector<int> src(static_cast<size_t>(cnt[N])), pos(cnt.begin(), cnt.end() - 1);
+            for (int e = p.ch_ptr[s]; e < p.ch_ptr[s + 1]; ++e) {
+                const int c = p.ch_list[e], Kc = p.sn_ncols[c], u = p.sn_nrows[c] - Kc;
+                for (int r = 0; r < u; ++r)
+                    src[pos[p.ea_map[p.ea_off[c] + r]]++] = static_cast<int>(p.sn_f_off[c] + Kc + r);
+            }
+            for (int r = 0; r < N; ++r) {
+                g_dst.push_back(static_cast<int>(p.sn_f_off[s] + r));
+                g_zp.push_back(r < K ? p.sn_first[s] + r : -1);
+                g_ptr.push_back(g_ptr.back() + cnt[r + 1] - cnt[r]);
+            }
+            g_src.insert(g_src.end(), src.begin(), src.end());
+        }
+    }
+    gather_off_[p.nlevels] = static_cast<int>(g_dst.size());
     auto rsv = [&](auto& slot, const auto& vec) { reserve(arena_, slot, vec.size()); };
     rsv(sn_first_, p.sn_first); rsv(sn_ncols_, p.sn_ncols); rsv(sn_nrows_, p.sn_nrows); rsv(sn_lda_, p.sn_lda); rsv(sn_parent_, p.sn_parent);
     rsv(rows_, p.rows); rsv(ea_map_, p.ea_map); rsv(ch_ptr_, p.ch_ptr); rsv(ch_list_, p.ch_list);
@@ -684,6 +874,7 @@ KktEngine::KktEngine(const ipm::FrontPlan& plan, const DeviceLP& lp, cudaStream_
     rsv(slot_pos_, p.slot_pos); rsv(w_ptr_, p.w_ptr); rsv(slot_i_, p.slot_i); rsv(slot_j_, p.slot_j);
     rsv(w_col_, p.w_col); rsv(w_val_, p.w_val); rsv(inv_off_, inv_off); rsv(blk_off_, blk_off);
     rsv(fwd_tasks_, ftask); rsv(bwd_tasks_, btask);
+    rsv(g_dst_, g_dst); rsv(g_zp_, g_zp); rsv(g_ptr_, g_ptr); rsv(g_src_, g_src);
     reserve(arena_, flags_, static_cast<size_t>(std::max(1, nflags_)));
     reserve(arena_, counters_, static_cast<size_t>(2 * std::max(1, p.nlevels)));
     reserve(arena_, solve_err_, 1);
@@ -702,7 +893,7 @@ KktEngine::KktEngine(const ipm::FrontPlan& plan, const DeviceLP& lp, cudaStream_
     bnd(ch_list_); bnd(perm_); bnd(sn_F_off_); bnd(sn_f_off_); bnd(sn_rows_off_); bnd(ea_off_); bnd(step_items_);
     bnd(step_prefix_); bnd(round_items_); bnd(round_prefix_); bnd(level_sn_); bnd(slot_pos_); bnd(w_ptr_);
     bnd(slot_i_); bnd(slot_j_); bnd(w_col_); bnd(w_val_); bnd(inv_off_); bnd(blk_off_); bnd(fwd_tasks_);
-    bnd(bwd_tasks_); bnd(flags_); bnd(counters_); bnd(solve_err_); bnd(D_); bnd(Mdiag_);
+    bnd(bwd_tasks_); bnd(g_dst_); bnd(g_zp_); bnd(g_ptr_); bnd(g_src_); bnd(flags_); bnd(counters_); bnd(solve_err_); bnd(D_); bnd(Mdiag_);
     bnd(zp_); bnd(xp_); bnd(zsol_); bnd(fvec_); bnd(tn_); bnd(params_); bnd(err_);
     upload(sn_first_, p.sn_first, st_); upload(sn_ncols_, p.sn_ncols, st_); upload(sn_nrows_, p.sn_nrows, st_);
     upload(sn_lda_, p.sn_lda, st_);
@@ -715,6 +906,7 @@ KktEngine::KktEngine(const ipm::FrontPlan& plan, const DeviceLP& lp, cudaStream_
     upload(slot_i_, p.slot_i, st_); upload(slot_j_, p.slot_j, st_); upload(w_col_, p.w_col, st_);
     upload(w_val_, p.w_val, st_); upload(inv_off_, inv_off, st_); upload(blk_off_, blk_off, st_);
     upload(fwd_tasks_, ftask, st_); upload(bwd_tasks_, btask, st_);
+    upload(g_dst_, g_dst, st_); upload(g_zp_, g_zp, st_); upload(g_ptr_, g_ptr, st_); upload(g_src_, g_src, st_);
     SK_CUDA(cudaMemsetAsync(solve_err_.ptr, 0, sizeof(int), st_));
     SK_CUDA(cudaStreamSynchronize(st_));
     set_smem_attrs<float>();
@@ -762,10 +954,11 @@ void KktEngine::launch_factor(T* F, T* Linv, Prof* prof) {
         for (int q = p.step_level_ptr[l]; q < p.step_level_ptr[l + 1]; ++q) {
             const auto& st = p.steps[q];
             StepArgs a{st.k, st.item_off, st.nitems, st.trsm_prefix_off, st.upd_prefix_off};
-            run(1, [&] {
-                k_potrf<T><<<st.nitems, 256, (2 * T64 * LDS + 2 * T64) * sizeof(T), st_>>>(a, step_items_.ptr, pdv, F,
-                                                                                    Linv, inv_off_.ptr, err_.ptr);
-            });
+            if (st.k == 0)   // later diagonal tiles are factored by the previous step's update
+                run(1, [&] {
+                    k_potrf<T><<<st.nitems, 256, potrf_smem(sizeof(T)), st_>>>(a, step_items_.ptr, pdv, F, Linv,
+                                                                               inv_off_.ptr, err_.ptr);
+                });
             if (st.trsm_tiles > 0)
                 run(2, [&] {
                     k_trsm<T><<<static_cast<int>(st.trsm_tiles), 256, 2 * T64 * T64 * sizeof(T), st_>>>(
@@ -773,8 +966,8 @@ void KktEngine::launch_factor(T* F, T* Linv, Prof* prof) {
                 });
             if (st.upd_tiles > 0) {
                 run(3, [&] {
-                    k_update<T><<<static_cast<int>(st.upd_tiles), 256, 2 * T64 * T64 * sizeof(T), st_>>>(
-                        a, step_items_.ptr, step_prefix_.ptr, pdv, F);
+                    k_update<T><<<static_cast<int>(st.upd_tiles), 256, potrf_smem(sizeof(T)), st_>>>(
+                        a, step_items_.ptr, step_prefix_.ptr, pdv, F, Linv, inv_off_.ptr, err_.ptr);
                 });
                 if (prof) {
                     for (int it = 0; it < st.nitems; ++it) {
@@ -812,10 +1005,12 @@ void KktEngine::launch_solve(const T* F, const T* Linv, Prof* prof) {
     SK_CUDA(cudaMemsetAsync(flags_.ptr, 0, sizeof(int) * static_cast<size_t>(std::max(1, nflags_)), st_));
     SK_CUDA(cudaMemsetAsync(counters_.ptr, 0, sizeof(int) * 2 * static_cast<size_t>(std::max(1, p.nlevels)), st_));
     for (int l = 0; l < p.nlevels; ++l) {
-        const int nl = p.level_ptr[l + 1] - p.level_ptr[l];
         const int nt = fwd_task_off_[l + 1] - fwd_task_off_[l];
+        const int g0 = gather_off_[l], ng = gather_off_[l + 1] - g0;
         run(5, [&] {
-            k_fwd_init<T><<<nl, 256, 0, st_>>>(level_sn_.ptr + p.level_ptr[l], pdv, zp, fv);
+            if (ng > 0)
+                k_fwd_gather<T><<<blocks_for(ng, 256), 256, 0, st_>>>(ng, g_dst_.ptr + g0, g_zp_.ptr + g0,
+                                                                      g_ptr_.ptr + g0, g_src_.ptr, zp, fv);
             k_fwd_tasks<T><<<nt, 256, 0, st_>>>(fwd_tasks_.ptr + fwd_task_off_[l], nt, counters_.ptr + l, pdv, F,
                                                 Linv, inv_off_.ptr, blk_off_.ptr, flags_.ptr, fv, zs,
                                                 solve_err_.ptr);

@@ -68,7 +68,7 @@ private:
     Slot<float> F32_, Linv32_;
     Slot<double> F64_, Linv64_;
     int64_t inv_size_ = 0;
-    std::vector<int> fwd_task_off_, bwd_task_off_;
+    std::vector<int> fwd_task_off_, bwd_task_off_, gather_off_;
     int nflags_ = 0;
     // plan arrays
     Slot<int> sn_first_, sn_ncols_, sn_nrows_, sn_lda_, sn_parent_, rows_, ea_map_, ch_ptr_, ch_list_, perm_;
@@ -76,6 +76,7 @@ private:
     Slot<int> step_items_, step_prefix_, round_items_, round_prefix_, level_sn_, blk_off_, flags_, counters_,
         solve_err_;
     Slot<int2> fwd_tasks_, bwd_tasks_;
+    Slot<int> g_dst_, g_zp_, g_ptr_, g_src_;   // forward right-hand-side gather lists
     Slot<int64_t> inv_off_;
     Slot<int64_t> slot_pos_, w_ptr_;
     Slot<int> slot_i_, slot_j_, w_col_;

@@ -112,25 +112,27 @@ def test_solver_rejects_learned_start_without_network(gpu):
 @pytest.mark.skipif(not os.path.exists(WEIGHTS), reason="trained weights not present")
 def test_trained_network_cuts_iterations_on_heldout_seeds(gpu):
     # What the trained network gains: held-out members of the family (never seen in
-    # training), solved from Mehrotra's start and from the learned start.
+    # training or in choosing the acceptance rule), each solved alone from Mehrotra's
+    # start and from the learned start (which falls back to Mehrotra's per LP).
     sk = gpu
     net = sk.Gnn(1)
     net.load(WEIGHTS)
-    lps = [sk.generate(3, 200000 + 64 + k) for k in range(16)]
-    its = {}
+    its = {sk.START_MEHROTRA: 0, sk.START_LEARNED: 0}
     used = 0
-    for start in (sk.START_MEHROTRA, sk.START_LEARNED):
-        s = sk.Solver(lps, precision=sk.PREC_MIXED, start=start)
-        if start == sk.START_LEARNED:
-            s.set_gnn(net)
-        s.run()
-        infos = [s.result(k, want_vectors=False)[0] for k in range(len(lps))]
-        assert all(i["status"] == 0 for i in infos)
-        its[start] = sum(i["iterations"] for i in infos)
-        if start == sk.START_LEARNED:
-            used = sum(i["learned_start"] for i in infos)
-        s.close()
-    print("iterations: mehrotra %d learned %d, learned start used on %d/16" %
+    for k in range(12):
+        lp = sk.generate(3, 200300 + k)
+        for start in (sk.START_MEHROTRA, sk.START_LEARNED):
+            s = sk.Solver([lp], precision=sk.PREC_MIXED, start=start)
+            if start == sk.START_LEARNED:
+                s.set_gnn(net)
+            s.run()
+            info = s.result(0, want_vectors=False)[0]
+            assert info["status"] == 0
+            its[start] += info["iterations"]
+            if start == sk.START_LEARNED:
+                used += info["learned_start"]
+            s.close()
+    print("iterations: mehrotra %d learned %d, learned start used on %d/12" %
           (its[sk.START_MEHROTRA], its[sk.START_LEARNED], used))
     assert used > 0
     assert its[sk.START_LEARNED] < its[sk.START_MEHROTRA]
