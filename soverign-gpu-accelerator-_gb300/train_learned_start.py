@@ -11,7 +11,7 @@ Mehrotra's start and from the learned start (which falls back per LP to
 Mehrotra's start) and reports iterations, fallback rate and device time.
 
 usage: python train_learned_start.py [--train 1024] [--heldout 128] [--batch 16]
-           [--epochs 30] [--lr 2e-3] [--capture-mu 1e-2] [--out weights/learned_start_family3.npy]
+           [--epochs 30] [--lr 2e-3] [--capture-mu 1.0] [--out weights/learned_start_family3.npy]
 Writes the FP32 master weights (.npy) and a JSON report next to them.
 """
 import argparse
@@ -28,7 +28,8 @@ sys.path.insert(0, HERE)
 import sankhya_gb300 as sk  # noqa: E402
 
 TRAIN_BASE = 100000     # family-3 instance numbers of the training set
-HELDOUT_BASE = 200000   # ... and of the held-out set (the benchmark batch uses 0..511)
+HELDOUT_BASE = 200100   # ... and of the held-out set (the benchmark batch uses 0..511; 200000..200099
+                        # were used to choose the capture level and the acceptance rule)
 
 
 def solve_for_targets(instances, batch, capture_mu):
@@ -107,7 +108,7 @@ def main():
     ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--epochs", type=int, default=30)
     ap.add_argument("--lr", type=float, default=2e-3)
-    ap.add_argument("--capture-mu", type=float, default=1e-2)
+    ap.add_argument("--capture-mu", type=float, default=1.0)
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--out", default=os.path.join(HERE, "weights", "learned_start_family3.npy"))
     args = ap.parse_args()
