@@ -127,6 +127,47 @@ def count_kernel_launches(fn):
         return None
 
 
+WEIGHTS = os.path.join(ROOT, "soverign-gpu-accelerator-_gb300", "weights", "learned_start_family3.npy")
+
+
+def batch_comparison(sk, nlps):
+    """LPs/s on the first `nlps` members of the 512-LP uneven batch (family 3),
+    solved as one batch: mixed precision + learned start (falling back per LP to
+    Mehrotra's start), mixed precision + Mehrotra's start, and the plain FP64 IPM
+    (unit start). Device time of the second of two runs of each."""
+    lps = [sk.generate(3, k) for k in range(nlps)]
+    net = None
+    if os.path.exists(WEIGHTS):
+        net = sk.Gnn(1)
+        net.load(WEIGHTS)
+    out = {"lps": nlps, "members": "family-3 instances 0..%d (m %d..%d)" % (
+        nlps - 1, min(lp.m for lp in lps), max(lp.m for lp in lps))}
+    arms = [("mixed_learned", sk.PREC_MIXED, sk.START_LEARNED), ("mixed_mehrotra", sk.PREC_MIXED, sk.START_MEHROTRA),
+            ("plain_fp64", sk.PREC_FP64, sk.START_UNIT)]
+    for name, prec, start in arms:
+        if start == sk.START_LEARNED and net is None:
+            continue
+        s = sk.Solver(lps, precision=prec, start=start)
+        if start == sk.START_LEARNED:
+            s.set_gnn(net)
+        s.run()
+        s.run()
+        infos = [s.result(k, want_vectors=False)[0] for k in range(nlps)]
+        s.close()
+        ms = infos[0]["device_ms"]
+        out[name] = {"ms": ms, "lps_per_s": 1000.0 * nlps / ms, "all_optimal": all(i["status"] == 0 for i in infos),
+                     "mean_iterations": sum(i["iterations"] for i in infos) / nlps}
+        if start == sk.START_LEARNED:
+            out[name]["learned_used"] = sum(i["learned_start"] for i in infos)
+    if net is not None:
+        net.close()
+    base = out["plain_fp64"]["lps_per_s"]
+    for name in ("mixed_learned", "mixed_mehrotra"):
+        if name in out:
+            out[name]["speedup_vs_plain_fp64"] = out[name]["lps_per_s"] / base
+    return out
+
+
 def dist_setup(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -197,6 +238,7 @@ def run_ours(args):
     info64b, *_ = fp64.result(0, want_vectors=False)
     prof64 = fp64.profile(fp32=False)
     fp64.close()
+    batch = batch_comparison(sk, args.batch_lps) if args.batch_lps > 0 else None
     # end to end through the C ABI (host arrays in, host solution out)
     e2e_t = []
     for _ in range(max(1, args.steps)):
@@ -211,13 +253,35 @@ def run_ours(args):
     h2d = lp.nbytes()
     d2h = (2 * lp.n + lp.m) * 8
     hbm, bf16, src = peaks()
-    upd = prof["update"]
-    achieved_tflops = prof["update_flops"] / (upd["ms"] / 1000.0) / 1e12 if upd["ms"] > 0 else 0.0
-    roof = {"kernel": "k_update<float> (FP32 frontal trailing update, SIMT)", "bound": "tensor",
-            "achieved": achieved_tflops, "peak": bf16, "unit": "TFLOP/s", "frac": achieved_tflops / bf16,
-            "peak_source": "%s bf16 dense tensor peak (MEASURED_PEAKS.json bf16_tflops)" % src,
-            "traffic": None, "launches": upd["launches"], "ms_total": upd["ms"],
-            "note": "timed by an event-instrumented replay of one factorisation at the final iterate"}
+    fp64_peak = 1.25   # TFLOP/s, nominal dense FP64 of a GB300 (no FP64 entry in MEASURED_PEAKS.json)
+    note = ("event-timed replay of one factorisation and one triangular solve at the final iterate; "
+            "the update class includes the diagonal-tile Cholesky fused into it")
+
+    def upd_roof(p, kernel, peak, peak_src, bound):
+        u = p["update"]
+        a = p["update_flops"] / (u["ms"] / 1000.0) / 1e12 if u["ms"] > 0 else 0.0
+        return {"kernel": kernel, "bound": bound, "achieved": a, "peak": peak, "unit": "TFLOP/s", "frac": a / peak,
+                "peak_source": peak_src, "traffic": None, "launches": u["launches"], "ms_total": u["ms"],
+                "algorithmic_flops": p["update_flops"], "note": note}
+
+    def solve_roof(p, kernel, elem):
+        ms = p["fwd_solve"]["ms"] + p["bwd_solve"]["ms"]
+        nbytes = 2.0 * elem * info["nnz_factor"]          # each factor entry read once per direction
+        a = nbytes / (ms / 1000.0) / 1e9 if ms > 0 else 0.0
+        return {"kernel": kernel, "bound": "hbm", "achieved": a, "peak": hbm, "unit": "GB/s", "frac": a / hbm,
+                "peak_source": "%s copy bandwidth (MEASURED_PEAKS.json hbm_gbs)" % src, "traffic": None,
+                "ms_total": ms, "algorithmic_bytes": nbytes, "note": note}
+
+    # The dominant kernel of the mixed solve (launch list in profiles/): the FP64 trailing update of
+    # the last factorisations, an FP64-pipe-bound SIMT kernel.
+    roof = upd_roof(prof64, "k_update<double> (FP64 frontal trailing update)", fp64_peak,
+                    "nominal GB300 dense FP64 1.25 TFLOP/s (of nominal; MEASURED_PEAKS.json has no FP64 entry)",
+                    "fp64")
+    rooflines = [roof,
+                 upd_roof(prof, "k_update<float> (FP32 frontal trailing update, SIMT)", bf16,
+                          "%s bf16 dense tensor peak (MEASURED_PEAKS.json bf16_tflops)" % src, "tensor"),
+                 solve_roof(prof, "k_fwd_tasks<float> + k_bwd_tasks<float> (one triangular solve pair)", 4),
+                 solve_roof(prof64, "k_fwd_tasks<double> + k_bwd_tasks<double> (one triangular solve pair)", 8)]
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(sk, cores=1)
@@ -232,6 +296,7 @@ def run_ours(args):
                        "switch_iteration": info["switch_iteration"], "factorizations": info["factorizations"],
                        "solves": info["solves"], "nnz_factor": info["nnz_factor"],
                        "supernodes": info["num_supernodes"], "flops_per_factorization": info["flops_factor"]},
+            "batch_family3": batch,
             "plain_fp64": {"ms_per_solve": info64b["device_ms"], "iterations": info64b["iterations"],
                            "lps_per_s": 1000.0 / info64b["device_ms"] if info64b["device_ms"] > 0 else None,
                            "speedup_mixed_vs_fp64": info64b["device_ms"] / (total_ms / args.steps)},
@@ -240,7 +305,7 @@ def run_ours(args):
             "wall_s_timed_region": wall,
             "gpu_launches": launches,
             "gpu_launches_note": "kernels of libsankhya_gb300 per solve (CUPTI trace of one extra run) x steps",
-            "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
+            "roofline": roof, "kernel_rooflines": rooflines, "cpu_baseline": cpu, "clocks": clk,
             "e2e": {"value": e2e_value, "unit": "LPs/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": 1000.0 * e2e_total / len(e2e_t)}}
     if rank == 0:
@@ -317,6 +382,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batch-lps", type=int, default=32,
+                    help="family-3 batch members for the mixed+learned vs plain FP64 batch comparison (0: skip)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -654,6 +654,7 @@ void DeviceIPM::profile(bool fp32, double* out16) {
     I.put_scalars(0, ones);
     k_theta<<<nblk(I.N), 256, 0, I.st>>>(I.N, I.x.ptr, I.s.ptr, I.col_lp.ptr, I.sc(0), I.theta.ptr);
     k_fill<<<nblk(I.M), 256, 0, I.st>>>(I.M, I.r.ptr, 1.0);
+    kkt_->set_active(std::vector<char>(I.nlp, 1));   // every front, whatever the last run left on
     kkt_->profile(I.theta.ptr, fp32 ? 1e-7 : 1e-9, fp32, I.r.ptr, I.corr.ptr, out16);
 }
 
@@ -721,6 +722,7 @@ void DeviceIPM::run() {
     I.used_fp32 = false;
     I.res.assign(nlp, LpResult());
     I.active.assign(nlp, 1);
+    K.set_active(I.active);
     I.rp0.assign(nlp, 1.0);
     I.rd0.assign(nlp, 1.0);
     I.mu0.assign(nlp, 1.0);
@@ -1140,6 +1142,7 @@ void DeviceIPM::run() {
         if (!any) break;
         for (int k = 0; k < nlp; ++k) mask[k] = I.active[k] ? 1.0 : 0.0;
         I.put_scalars(0, mask);
+        K.set_active(I.active);   // converged LPs' fronts are no longer factored or solved
         k_theta<<<nblk(N), 256, 0, st>>>(N, I.x.ptr, I.s.ptr, I.col_lp.ptr, d_mask, I.theta.ptr);
         // precision for this iteration
         bool fp32 = o.precision == SK_PREC_MIXED && !I.switched && mumax >= o.mu_switch;

@@ -33,6 +33,8 @@ struct PlanDev {
     const int* ch_ptr;
     const int* ch_list;
     const int* sn_parent;
+    const int* sn_lp;      // LP of each front (fronts never span LPs)
+    const int* lp_on;      // 1 while an LP of the batch is still being solved; 0 skips its fronts
 };
 
 namespace {
@@ -293,7 +295,9 @@ __global__ void __launch_bounds__(256) k_potrf(StepArgs a, const int* __restrict
                                                T* __restrict__ Linv, const int64_t* __restrict__ inv_off,
                                                int* err) {
     extern __shared__ __align__(16) unsigned char smraw[];
-    potrf_tile<T>(items[a.item_off + blockIdx.x], a.k, pd, F, Linv, inv_off, err, smraw);
+    const int s = items[a.item_off + blockIdx.x];
+    if (!pd.lp_on[pd.sn_lp[s]]) return;
+    potrf_tile<T>(s, a.k, pd, F, Linv, inv_off, err, smraw);
 }
 
 // Panel rows below the diagonal tile: X = B L_kk^{-T} = B Linv^T (a small GEMM).
@@ -306,6 +310,7 @@ __global__ void __launch_bounds__(256) k_trsm(StepArgs a, const int* __restrict_
     T* B = Iv + T64 * T64;                   // B[c][r] (column-major)
     const int i = find_item(prefix + a.tp_off, a.nitems, blockIdx.x);
     const int s = items[a.item_off + i];
+    if (!pd.lp_on[pd.sn_lp[s]]) return;
     const int lt = blockIdx.x - prefix[a.tp_off + i];
     const int N = pd.sn_nrows[s], K = pd.sn_ncols[s];
     const int LD = pd.sn_lda[s];
@@ -353,6 +358,7 @@ __global__ void __launch_bounds__(256) k_update(StepArgs a, const int* __restric
     T* Bs = As + T64 * T64;                  // [kk][c]
     const int i = find_item(prefix + a.up_off, a.nitems, blockIdx.x);
     const int s = items[a.item_off + i];
+    if (!pd.lp_on[pd.sn_lp[s]]) return;
     const int lt = blockIdx.x - prefix[a.up_off + i];
     int ti, tj;
     tri_index(lt, ti, tj);
@@ -427,6 +433,7 @@ __global__ void k_extend_add(int item_off, int nitems, int prefix_off, const int
                              const int* __restrict__ prefix, PlanDev pd, T* F) {
     const int i = find_item(prefix + prefix_off, nitems, blockIdx.x);
     const int c = items[item_off + i];
+    if (!pd.lp_on[pd.sn_lp[c]]) return;
     const int lt = blockIdx.x - prefix[prefix_off + i];
     int ti, tj;
     tri_index(lt, ti, tj);
@@ -457,11 +464,16 @@ __global__ void k_permute_scale(int M, const int* __restrict__ perm, const doubl
     if (q < M) zp[q] = static_cast<T>(D[q] * src[perm[q]]);
 }
 
+// Rows of LPs whose fronts were skipped get 0.
 template <class T>
 __global__ void k_unpermute_scale(int M, const int* __restrict__ perm, const double* __restrict__ D,
-                                  const T* __restrict__ xp, double* __restrict__ dst) {
+                                  const T* __restrict__ xp, const int* __restrict__ row_lp,
+                                  const int* __restrict__ lp_on, double* __restrict__ dst) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q < M) dst[perm[q]] = D[q] * static_cast<double>(xp[q]);
+    if (q < M) {
+        const int r = perm[q];
+        dst[r] = lp_on[row_lp[r]] ? D[q] * static_cast<double>(xp[q]) : 0.0;
+    }
 }
 
 // Frontal right-hand sides of one level: one thread per front row, the row's own
@@ -518,7 +530,7 @@ __device__ __forceinline__ int flag_now(const int* flag) { return *reinterpret_c
 // values loaded before the wait, so the latency-critical last dependency only
 // waits for its flag and z values.
 template <class T>
-__global__ void __launch_bounds__(256) k_fwd_tasks(const int2* __restrict__ tasks, int ntasks, int* counter,
+__global__ void __launch_bounds__(256, 1) k_fwd_tasks(const int2* __restrict__ tasks, int ntasks, int* counter,
                                                    PlanDev pd, const T* __restrict__ F, const T* __restrict__ Linv,
                                                    const int64_t* __restrict__ inv_off,
                                                    const int* __restrict__ blk_off, int* flags, T* fv, T* zsol,
@@ -536,6 +548,7 @@ __global__ void __launch_bounds__(256) k_fwd_tasks(const int2* __restrict__ task
     const int t = task_sh;
     if (t >= ntasks) return;
     const int s = tasks[t].x, i = tasks[t].y;
+    if (!pd.lp_on[pd.sn_lp[s]]) return;   // every task of the front's LP is skipped alike
     const int N = pd.sn_nrows[s], K = pd.sn_ncols[s], first = pd.sn_first[s];
     const int LD = pd.sn_lda[s];
     const int nb = (K + T64 - 1) / T64;
@@ -629,7 +642,7 @@ __global__ void __launch_bounds__(256) k_fwd_tasks(const int2* __restrict__ task
 // blocks are taken oldest first (nb - 1 downwards), ready ones together, and the
 // L values of the first block of each pass are loaded before its wait.
 template <class T>
-__global__ void __launch_bounds__(256) k_bwd_tasks(const int2* __restrict__ tasks, int ntasks, int* counter,
+__global__ void __launch_bounds__(256, 1) k_bwd_tasks(const int2* __restrict__ tasks, int ntasks, int* counter,
                                                    PlanDev pd, const T* __restrict__ F, const T* __restrict__ Linv,
                                                    const int64_t* __restrict__ inv_off,
                                                    const int* __restrict__ blk_off, int* flags, T* xp,
@@ -646,6 +659,7 @@ __global__ void __launch_bounds__(256) k_bwd_tasks(const int2* __restrict__ task
     const int t = task_sh;
     if (t >= ntasks) return;
     const int s = tasks[t].x, i = tasks[t].y;
+    if (!pd.lp_on[pd.sn_lp[s]]) return;   // every task of the front's LP is skipped alike
     const int N = pd.sn_nrows[s], K = pd.sn_ncols[s], first = pd.sn_first[s];
     const int LD = pd.sn_lda[s];
     const int nb = (K + T64 - 1) / T64;
@@ -665,7 +679,23 @@ __global__ void __launch_bounds__(256) k_bwd_tasks(const int2* __restrict__ task
         const int nr = min(kOut, N - r0);
         for (int q = tid; q < nr; q += 256) xb[q] = xp[R[r0 + q]];
         __syncthreads();
-        for (int q = lane; q < nr; q += 32) {
+        // four rows per lane per pass: 32 independent loads in flight
+        int q = lane;
+        for (; q + 96 < nr; q += 128) {
+            T fr[4][8];
+#pragma unroll
+            for (int h = 0; h < 4; ++h)
+#pragma unroll
+                for (int u = 0; u < 8; ++u)
+                    fr[h][u] = c0 + u < K ? Fs[(r0 + q + 32 * h) + static_cast<int64_t>(c0 + u) * LD] : T(0);
+#pragma unroll
+            for (int h = 0; h < 4; ++h) {
+                const T xr = xb[q + 32 * h];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) part[u] += fr[h][u] * xr;
+            }
+        }
+        for (; q < nr; q += 32) {
             const T xr = xb[q];
             const T* Fr = Fs + (r0 + q);
 #pragma unroll
@@ -865,6 +895,13 @@ KktEngine::KktEngine(const ipm::FrontPlan& plan, const DeviceLP& lp, cudaStream_
         }
     }
     gather_off_[p.nlevels] = static_cast<int>(g_dst.size());
+    // LP of each front (from the batch row of its first column) and the all-on LP mask
+    std::vector<int> sn_lp(static_cast<size_t>(p.ns), 0);
+    for (int s = 0; s < p.ns; ++s) {
+        const Index r = p.perm[p.sn_first[s]];
+        sn_lp[s] = static_cast<int>(std::upper_bound(p.row_off.begin(), p.row_off.end(), r) - p.row_off.begin()) - 1;
+    }
+    lp_on_h_.assign(static_cast<size_t>(std::max(1, p.nlp)), 1);
     auto rsv = [&](auto& slot, const auto& vec) { reserve(arena_, slot, vec.size()); };
     rsv(sn_first_, p.sn_first); rsv(sn_ncols_, p.sn_ncols); rsv(sn_nrows_, p.sn_nrows); rsv(sn_lda_, p.sn_lda); rsv(sn_parent_, p.sn_parent);
     rsv(rows_, p.rows); rsv(ea_map_, p.ea_map); rsv(ch_ptr_, p.ch_ptr); rsv(ch_list_, p.ch_list);
@@ -875,6 +912,7 @@ KktEngine::KktEngine(const ipm::FrontPlan& plan, const DeviceLP& lp, cudaStream_
     rsv(w_col_, p.w_col); rsv(w_val_, p.w_val); rsv(inv_off_, inv_off); rsv(blk_off_, blk_off);
     rsv(fwd_tasks_, ftask); rsv(bwd_tasks_, btask);
     rsv(g_dst_, g_dst); rsv(g_zp_, g_zp); rsv(g_ptr_, g_ptr); rsv(g_src_, g_src);
+    rsv(sn_lp_, sn_lp); rsv(lp_on_, lp_on_h_);
     reserve(arena_, flags_, static_cast<size_t>(std::max(1, nflags_)));
     reserve(arena_, counters_, static_cast<size_t>(2 * std::max(1, p.nlevels)));
     reserve(arena_, solve_err_, 1);
@@ -893,7 +931,7 @@ KktEngine::KktEngine(const ipm::FrontPlan& plan, const DeviceLP& lp, cudaStream_
     bnd(ch_list_); bnd(perm_); bnd(sn_F_off_); bnd(sn_f_off_); bnd(sn_rows_off_); bnd(ea_off_); bnd(step_items_);
     bnd(step_prefix_); bnd(round_items_); bnd(round_prefix_); bnd(level_sn_); bnd(slot_pos_); bnd(w_ptr_);
     bnd(slot_i_); bnd(slot_j_); bnd(w_col_); bnd(w_val_); bnd(inv_off_); bnd(blk_off_); bnd(fwd_tasks_);
-    bnd(bwd_tasks_); bnd(g_dst_); bnd(g_zp_); bnd(g_ptr_); bnd(g_src_); bnd(flags_); bnd(counters_); bnd(solve_err_); bnd(D_); bnd(Mdiag_);
+    bnd(bwd_tasks_); bnd(g_dst_); bnd(g_zp_); bnd(g_ptr_); bnd(g_src_); bnd(sn_lp_); bnd(lp_on_); bnd(flags_); bnd(counters_); bnd(solve_err_); bnd(D_); bnd(Mdiag_);
     bnd(zp_); bnd(xp_); bnd(zsol_); bnd(fvec_); bnd(tn_); bnd(params_); bnd(err_);
     upload(sn_first_, p.sn_first, st_); upload(sn_ncols_, p.sn_ncols, st_); upload(sn_nrows_, p.sn_nrows, st_);
     upload(sn_lda_, p.sn_lda, st_);
@@ -907,6 +945,7 @@ KktEngine::KktEngine(const ipm::FrontPlan& plan, const DeviceLP& lp, cudaStream_
     upload(w_val_, p.w_val, st_); upload(inv_off_, inv_off, st_); upload(blk_off_, blk_off, st_);
     upload(fwd_tasks_, ftask, st_); upload(bwd_tasks_, btask, st_);
     upload(g_dst_, g_dst, st_); upload(g_zp_, g_zp, st_); upload(g_ptr_, g_ptr, st_); upload(g_src_, g_src, st_);
+    upload(sn_lp_, sn_lp, st_); upload(lp_on_, lp_on_h_, st_);
     SK_CUDA(cudaMemsetAsync(solve_err_.ptr, 0, sizeof(int), st_));
     SK_CUDA(cudaStreamSynchronize(st_));
     set_smem_attrs<float>();
@@ -922,7 +961,8 @@ KktEngine::~KktEngine() {
 
 PlanDev KktEngine::pd() const {
     return PlanDev{sn_first_.ptr, sn_ncols_.ptr, sn_nrows_.ptr, sn_lda_.ptr, sn_F_off_.ptr, sn_f_off_.ptr, sn_rows_off_.ptr,
-                   rows_.ptr, ea_off_.ptr, ea_map_.ptr, ch_ptr_.ptr, ch_list_.ptr, sn_parent_.ptr};
+                   rows_.ptr, ea_off_.ptr, ea_map_.ptr, ch_ptr_.ptr, ch_list_.ptr, sn_parent_.ptr, sn_lp_.ptr,
+                   lp_on_.ptr};
 }
 
 template <class T>
@@ -1094,9 +1134,19 @@ void KktEngine::apply_inverse(const double* d_src, double* d_dst) {
     }
     SK_CUDA(cudaGraphLaunch(gsol_[q], st_));
     if (fp32_) k_unpermute_scale<float><<<blocks_for(p.M, 256), 256, 0, st_>>>(
-        p.M, perm_.ptr, D_.ptr, reinterpret_cast<const float*>(xp_.ptr), d_dst);
-    else k_unpermute_scale<double><<<blocks_for(p.M, 256), 256, 0, st_>>>(p.M, perm_.ptr, D_.ptr, xp_.ptr, d_dst);
+        p.M, perm_.ptr, D_.ptr, reinterpret_cast<const float*>(xp_.ptr), lp_.row_lp, lp_on_.ptr, d_dst);
+    else k_unpermute_scale<double><<<blocks_for(p.M, 256), 256, 0, st_>>>(p.M, perm_.ptr, D_.ptr, xp_.ptr,
+                                                                           lp_.row_lp, lp_on_.ptr, d_dst);
     SK_CUDA(cudaGetLastError());
+}
+
+void KktEngine::set_active(const std::vector<char>& on) {
+    bool same = on.size() == lp_on_h_.size();
+    for (size_t k = 0; same && k < on.size(); ++k) same = (on[k] != 0) == (lp_on_h_[k] != 0);
+    if (same) return;
+    if (on.size() != lp_on_h_.size()) throw std::invalid_argument("set_active: one flag per LP");
+    for (size_t k = 0; k < on.size(); ++k) lp_on_h_[k] = on[k] ? 1 : 0;
+    SK_CUDA(cudaMemcpyAsync(lp_on_.ptr, lp_on_h_.data(), sizeof(int) * lp_on_h_.size(), cudaMemcpyHostToDevice, st_));
 }
 
 void KktEngine::apply_normal(const double* d_theta, const double* d_src, double* d_dst) {
@@ -1121,12 +1171,12 @@ void KktEngine::profile(const double* d_theta, double delta, bool fp32, const do
                                                                           reinterpret_cast<float*>(zp_.ptr));
         launch_solve<float>(F32_.ptr, Linv32_.ptr, &pr);
         k_unpermute_scale<float><<<blocks_for(plan_.M, 256), 256, 0, st_>>>(
-            plan_.M, perm_.ptr, D_.ptr, reinterpret_cast<const float*>(xp_.ptr), d_out);
+            plan_.M, perm_.ptr, D_.ptr, reinterpret_cast<const float*>(xp_.ptr), lp_.row_lp, lp_on_.ptr, d_out);
     } else {
         k_permute_scale<double><<<blocks_for(plan_.M, 256), 256, 0, st_>>>(plan_.M, perm_.ptr, D_.ptr, d_rhs, zp_.ptr);
         launch_solve<double>(F64_.ptr, Linv64_.ptr, &pr);
         k_unpermute_scale<double><<<blocks_for(plan_.M, 256), 256, 0, st_>>>(plan_.M, perm_.ptr, D_.ptr, xp_.ptr,
-                                                                             d_out);
+                                                                             lp_.row_lp, lp_on_.ptr, d_out);
     }
     SK_CUDA(cudaStreamSynchronize(st_));
     for (int q = 0; q < 16; ++q) out[q] = 0.0;

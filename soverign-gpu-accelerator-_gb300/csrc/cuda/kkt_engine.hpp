@@ -33,6 +33,9 @@ public:
     void apply_inverse(const double* d_src, double* d_dst);
     // dst = A diag(theta) A^T src (FP64, matrix-free).
     void apply_normal(const double* d_theta, const double* d_src, double* d_dst);
+    // Which LPs of the batch are still being solved: factorisation and solves skip
+    // the fronts of the others (their solve output rows are 0). All on initially.
+    void set_active(const std::vector<char>& on);
 
     // Diagnostics: one factorisation + one solve (of d_rhs) without graphs, with
     // CUDA events around every launch; fills out[16] as sk_solver_profile documents.
@@ -77,6 +80,8 @@ private:
         solve_err_;
     Slot<int2> fwd_tasks_, bwd_tasks_;
     Slot<int> g_dst_, g_zp_, g_ptr_, g_src_;   // forward right-hand-side gather lists
+    Slot<int> sn_lp_, lp_on_;
+    std::vector<int> lp_on_h_;
     Slot<int64_t> inv_off_;
     Slot<int64_t> slot_pos_, w_ptr_;
     Slot<int> slot_i_, slot_j_, w_col_;
