@@ -228,7 +228,8 @@ def run_ours(args):
     per_run = count_kernel_launches(solver.run)
     launches = per_run * args.steps if per_run is not None else None
     # kernel-class breakdown (instrumented replay of one factorisation + solve at the final iterate)
-    prof = solver.profile(fp32=True)
+    prof = solver.profile(fp32=True)                 # tensor-core FP32 updates
+    prof_simt = solver.profile(fp32=True, tensor=False)
     solver.close()
     # plain FP64 solve of the same LP for the comparison the metric names
     fp64 = sk.Solver([lp], precision=sk.PREC_FP64)
@@ -278,7 +279,9 @@ def run_ours(args):
                     "nominal GB300 dense FP64 1.25 TFLOP/s (of nominal; MEASURED_PEAKS.json has no FP64 entry)",
                     "fp64")
     rooflines = [roof,
-                 upd_roof(prof, "k_update<float> (FP32 frontal trailing update, SIMT)", bf16,
+                 upd_roof(prof, "k_update_tc (FP32 frontal trailing update, tcgen05 TF32 x3; flops counted once)",
+                          bf16, "%s bf16 dense tensor peak (MEASURED_PEAKS.json bf16_tflops)" % src, "tensor"),
+                 upd_roof(prof_simt, "k_update<float> (FP32 frontal trailing update, SIMT)", bf16,
                           "%s bf16 dense tensor peak (MEASURED_PEAKS.json bf16_tflops)" % src, "tensor"),
                  solve_roof(prof, "k_fwd_tasks<float> + k_bwd_tasks<float> (one triangular solve pair)", 4),
                  solve_roof(prof64, "k_fwd_tasks<double> + k_bwd_tasks<double> (one triangular solve pair)", 8)]
@@ -301,6 +304,7 @@ def run_ours(args):
                            "lps_per_s": 1000.0 / info64b["device_ms"] if info64b["device_ms"] > 0 else None,
                            "speedup_mixed_vs_fp64": info64b["device_ms"] / (total_ms / args.steps)},
             "kernel_breakdown_ms": {"mixed": {k: v for k, v in prof.items() if isinstance(v, dict)},
+                                    "mixed_simt_update": {k: v for k, v in prof_simt.items() if isinstance(v, dict)},
                                     "fp64": {k: v for k, v in prof64.items() if isinstance(v, dict)}},
             "wall_s_timed_region": wall,
             "gpu_launches": launches,

@@ -131,8 +131,9 @@ void sk_solver_destroy(sk_solver* h);
  * c = 0 assembly, 1 potrf, 2 trsm, 3 update, 4 extend-add, 5 forward solve,
  * 6 backward solve; out[14] = algorithmic flops of the update launches, out[15] =
  * bytes the update launches must move at least (each input tile read once, each
- * output tile read and written once). fp32 selects the FP32 front path. Returns
- * the number of values written (16). No reference counterpart. */
+ * output tile read and written once). fp32: 0 = FP64 fronts, 1 = FP32 fronts with
+ * tensor-core (tcgen05) updates, 2 = FP32 fronts with SIMT updates. Returns the
+ * number of values written (16). No reference counterpart. */
 int sk_solver_profile(sk_solver* h, int fp32, double* out, int cap);
 
 /* ---- Learned start: bipartite row / column message-passing network ----

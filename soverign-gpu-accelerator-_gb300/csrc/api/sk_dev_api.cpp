@@ -169,7 +169,7 @@ int sk_solver_profile(sk_solver* h, int fp32, double* out, int cap) {
     api::clear_error();
     if (!h || !out || cap < 16) return -SK_ERR_INVALID;
     try {
-        h->ipm->profile(fp32 != 0, out);
+        h->ipm->profile(fp32 != 0, fp32 == 1, out);
         return 16;
     } catch (...) {
         return -api::status_of_current_exception();

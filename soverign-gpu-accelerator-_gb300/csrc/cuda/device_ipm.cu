@@ -39,6 +39,7 @@ constexpr double kLearnedSaturated = 0.99;   // learned start: upper bound on it
 constexpr double kShortStep = 0.1;           // learned-start restart: a step shorter than this ...
 constexpr int kShortSteps = 3;               // ... this many times ...
 constexpr int kRestartWindow = 10;           // ... within the first iterations
+constexpr double kTensorMu = 1e-4;           // FP32 fronts: tensor-core updates while mu >= this
 constexpr int kLooseIters = 3;               // stall acceptance of the relative tests (see the stopping rule)
 constexpr int kProgressIter = 12;            // learned-start restart: by this iteration the distance to the
 constexpr double kProgress = 1e-3;           // stopping test must have fallen by this factor
@@ -648,13 +649,14 @@ DeviceIPM::DeviceIPM(const std::vector<ipm::LpView>& lps, const std::vector<cons
     setup_ms_ = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }
 
-void DeviceIPM::profile(bool fp32, double* out16) {
+void DeviceIPM::profile(bool fp32, bool tensor, double* out16) {
     Impl& I = *im_;
     std::vector<double> ones(I.nlp, 1.0);
     I.put_scalars(0, ones);
     k_theta<<<nblk(I.N), 256, 0, I.st>>>(I.N, I.x.ptr, I.s.ptr, I.col_lp.ptr, I.sc(0), I.theta.ptr);
     k_fill<<<nblk(I.M), 256, 0, I.st>>>(I.M, I.r.ptr, 1.0);
     kkt_->set_active(std::vector<char>(I.nlp, 1));   // every front, whatever the last run left on
+    kkt_->set_tensor_update(tensor);
     kkt_->profile(I.theta.ptr, fp32 ? 1e-7 : 1e-9, fp32, I.r.ptr, I.corr.ptr, out16);
 }
 
@@ -883,7 +885,11 @@ void DeviceIPM::run() {
     // delta: the reference's 1e-9 x10 ladder in strict mode (src/cuda/kkt.cu:35, 665-669);
     // otherwise 1e-12 x10 for FP64 fronts (a tighter preconditioner keeps PCG short
     // once A Theta A^T is nearly singular) and 1e-7 x10 for FP32 fronts.
+    // FP32 trailing updates run on the tensor cores (TF32 x3) while mu >= kTensorMu; the
+    // last FP32 iterations, whose directions decide the FP64 switch, use exact FP32.
+    bool tensor_now = true;
     auto factor = [&](bool want_fp32) -> bool {
+        K.set_tensor_update(tensor_now);
         double delta = want_fp32 ? o.delta32 : (o.strict ? 1e-9 : o.delta64);
         for (int retry = 0; retry < (o.strict ? 5 : 6); ++retry, delta *= 10.0) {
             ++I.factorizations;
@@ -1145,6 +1151,7 @@ void DeviceIPM::run() {
         K.set_active(I.active);   // converged LPs' fronts are no longer factored or solved
         k_theta<<<nblk(N), 256, 0, st>>>(N, I.x.ptr, I.s.ptr, I.col_lp.ptr, d_mask, I.theta.ptr);
         // precision for this iteration
+        tensor_now = mumax >= kTensorMu;
         bool fp32 = o.precision == SK_PREC_MIXED && !I.switched && mumax >= o.mu_switch;
         if (o.precision == SK_PREC_MIXED && !I.switched && !fp32) {
             if (o.verbose) std::fprintf(stderr, "[sk] FP64 fronts from iter %d: mu below mu_switch\n", iter);

@@ -15,6 +15,8 @@
 
 #include <algorithm>
 #include <cmath>
+#include <stdexcept>
+#include <type_traits>
 
 namespace sankhya {
 namespace dev {
@@ -47,7 +49,8 @@ struct StepArgs {
     int item_off;
     int nitems;
     int tp_off;   // trsm prefix offset
-    int up_off;   // update prefix offset
+    int up_off;   // update prefix offset (64x64 tiles)
+    int up2_off;  // update prefix offset (128x128 blocks, tensor-core path)
 };
 
 
@@ -425,6 +428,183 @@ __global__ void __launch_bounds__(256) k_update(StepArgs a, const int* __restric
     if (lt == 0 && t0 < K) {
         __syncthreads();
         potrf_tile<T>(s, a.k + 1, pd, F, Linv, inv_off, err, smraw);
+    }
+}
+
+// ---- tensor-core trailing update of FP32 fronts (tcgen05, TF32 x3) ---------
+// One block of 256 threads updates a 128x128 block of the trailing lower triangle
+// (four 64x64 tiles): C -= A_i A_j^T with A_i, A_j the 128 x w panel rows, as
+// D = A_lo B_hi^T + A_hi B_lo^T + A_hi B_hi^T on the 5th-generation tensor cores.
+// Each FP32 operand x is split into TF32 parts hi = tf32(x), lo = tf32(x - hi),
+// so the three products recover close to FP32 accuracy. Operands are staged in
+// shared memory in the canonical K-major no-swizzle layout (8-row x 16-byte core
+// matrices; K-adjacent core matrices 128 B apart, 8-row groups 2048 B apart); the
+// MMA shape is M=128, N=128, K=8, accumulating in 128 TMEM columns. One elected
+// thread issues the 24 MMAs and commits them to an mbarrier while every thread
+// loads its C values; all eight warps then read D (warp w: TMEM lanes of quarter
+// w % 4, columns 64 (w / 4) ..) and write C. Every wait is bounded: on a time-out
+// the block records err[2], frees its TMEM and leaves C untouched.
+
+constexpr int kTcRows = 128;                         // operand rows per block (two 64-row tiles)
+constexpr uint32_t kTcLbo = 128;                     // bytes between K-adjacent core matrices
+constexpr uint32_t kTcSbo = 2048;                    // bytes between 8-row groups (64 fp32 per row)
+constexpr size_t kTcOp = kTcRows * T64 * 4;          // one operand part: 32 KB
+constexpr size_t kTcSmem = 4 * kTcOp + 64;           // + mbarrier and TMEM address
+constexpr int kTcSpin = 1 << 22;
+// instruction descriptor: D = F32 (bits 4-5 = 1), A = B = TF32 (bits 7-9, 10-12 = 2), both
+// K-major, N >> 3 at bits 17-22, M >> 4 at bits 24-28
+constexpr uint32_t kTcIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((128u >> 3) << 17) | ((128u >> 4) << 24);
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ uint64_t tc_sdesc(uint32_t saddr) {
+    uint64_t d = static_cast<uint64_t>((saddr & 0x3FFFFu) >> 4);
+    d |= static_cast<uint64_t>(kTcLbo >> 4) << 16;
+    d |= static_cast<uint64_t>(kTcSbo >> 4) << 32;
+    d |= static_cast<uint64_t>(1) << 46;             // descriptor version bits 46-48 = 0b001
+    return d;                                        // base offset 0, no swizzle
+}
+__device__ __forceinline__ uint32_t tc_off(int r, int k) {   // byte offset of (row r, col k)
+    return static_cast<uint32_t>((r >> 3) * kTcSbo + (k >> 2) * kTcLbo + (r & 7) * 16 + (k & 3) * 4);
+}
+__device__ __forceinline__ uint32_t to_tf32(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return r;
+}
+
+__global__ void __launch_bounds__(256, 1) k_update_tc(StepArgs a, const int* __restrict__ items,
+                                                      const int* __restrict__ prefix, PlanDev pd, float* F,
+                                                      float* __restrict__ Linv,
+                                                      const int64_t* __restrict__ inv_off, int* err) {
+    extern __shared__ __align__(1024) unsigned char smraw[];
+    unsigned char* Ahi = smraw;
+    unsigned char* Alo = Ahi + kTcOp;
+    unsigned char* Bhi = Alo + kTcOp;
+    unsigned char* Blo = Bhi + kTcOp;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(Blo + kTcOp);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(Blo + kTcOp + 16);
+    int* fail = reinterpret_cast<int*>(Blo + kTcOp + 32);
+    const int i = find_item(prefix + a.up2_off, a.nitems, blockIdx.x);
+    const int s = items[a.item_off + i];
+    if (!pd.lp_on[pd.sn_lp[s]]) return;
+    const int lb = blockIdx.x - prefix[a.up2_off + i];
+    int bi, bj;
+    tri_index(lb, bi, bj);
+    const int N = pd.sn_nrows[s], K = pd.sn_ncols[s];
+    const int LD = pd.sn_lda[s];
+    const int k0 = a.k * T64;
+    const int w = min(T64, K - k0);
+    const int t0 = k0 + w;
+    const int r0 = t0 + bi * kTcRows, c0 = t0 + bj * kTcRows;
+    const int nra = min(kTcRows, N - r0), ncb = min(kTcRows, N - c0);
+    float* Fs = F + pd.F_off[s];
+    const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_addr(bar)));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        *fail = 0;
+    }
+    if (wid == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;" :: "r"(smem_addr(tslot)));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    // operands: rows r0.. (A) and c0.. (B), columns k0..k0+w of the panel, in TF32 parts
+#pragma unroll 4
+    for (int it = 0; it < 32; ++it) {
+        const int idx = tid + it * 256;
+        const int r = idx & (kTcRows - 1), kk = idx >> 7;
+        const int64_t cofs = static_cast<int64_t>(k0 + kk) * LD;
+        const float av = (kk < w && r < nra) ? Fs[r0 + r + cofs] : 0.f;
+        const float bv = (kk < w && r < ncb) ? Fs[c0 + r + cofs] : 0.f;
+        const uint32_t ah = to_tf32(av), bh = to_tf32(bv);
+        const uint32_t o = tc_off(r, kk);
+        *reinterpret_cast<uint32_t*>(Ahi + o) = ah;
+        *reinterpret_cast<uint32_t*>(Alo + o) = to_tf32(av - __uint_as_float(ah));
+        *reinterpret_cast<uint32_t*>(Bhi + o) = bh;
+        *reinterpret_cast<uint32_t*>(Blo + o) = to_tf32(bv - __uint_as_float(bh));
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tslot;
+    if (tid == 0) {
+        const uint32_t ahi = smem_addr(Ahi), alo = smem_addr(Alo), bhi = smem_addr(Bhi), blo = smem_addr(Blo);
+        const int nk = (w + 7) / 8;
+        uint32_t acc = 0;
+        for (int ks = 0; ks < nk; ++ks) {
+            const uint32_t ko = static_cast<uint32_t>(ks) * 2 * kTcLbo;
+            const uint64_t da[3] = {tc_sdesc(alo + ko), tc_sdesc(ahi + ko), tc_sdesc(ahi + ko)};
+            const uint64_t db[3] = {tc_sdesc(bhi + ko), tc_sdesc(blo + ko), tc_sdesc(bhi + ko)};
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                             " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n"
+                             :: "r"(tmem), "l"(da[q]), "l"(db[q]), "r"(kTcIdesc), "r"(acc));
+                acc = 1;
+            }
+        }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                     :: "r"(smem_addr(bar)) : "memory");
+    }
+    // this thread's row of D (TMEM lane) and 64 columns, and its C values, loaded while the MMAs run
+    const int row = 32 * (wid & 3) + lane, ch = 64 * (wid >> 2);
+    const bool rok = row < nra;
+    float cv[64];
+#pragma unroll
+    for (int j = 0; j < 64; ++j) {
+        const int col = ch + j;
+        const bool in = rok && col < ncb && (bi != bj || row >= col);
+        cv[j] = in ? Fs[(r0 + row) + static_cast<int64_t>(c0 + col) * LD] : 0.f;
+    }
+    if (tid == 0) {
+        uint32_t done = 0;
+        for (int spin = 0; spin < kTcSpin && !done; ++spin) {
+            asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n"
+                         " selp.u32 %0, 1, 0, p;\n}\n" : "=r"(done) : "r"(smem_addr(bar)) : "memory");
+            if (!done) __nanosleep(20);
+        }
+        if (!done) {
+            *fail = 1;
+            atomicExch(err + 2, 1);
+        }
+    }
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const bool ok = *fail == 0;
+    if (ok) {
+#pragma unroll
+        for (int c16 = 0; c16 < 4; ++c16) {
+            uint32_t v[16];
+            const uint32_t taddr = tmem + (static_cast<uint32_t>(32 * (wid & 3)) << 16) +
+                                   static_cast<uint32_t>(ch + 16 * c16);
+            asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                         : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+                           "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+                           "=r"(v[14]), "=r"(v[15])
+                         : "r"(taddr));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+                const int j = 16 * c16 + q, col = ch + j;
+                if (rok && col < ncb && (bi != bj || row >= col))
+                    Fs[(r0 + row) + static_cast<int64_t>(c0 + col) * LD] = cv[j] - __uint_as_float(v[q]);
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (wid == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;" :: "r"(tmem));
+    }
+    if (!ok) return;
+    // the block holding the first trailing diagonal tile factors it (as in k_update)
+    if (lb == 0 && t0 < K) {
+        __syncthreads();
+        potrf_tile<float>(s, a.k + 1, pd, F, Linv, inv_off, err, smraw);
     }
 }
 
@@ -823,6 +1003,9 @@ struct KktEngine::Prof {
 
 template <class T>
 static void set_smem_attrs() {
+    if (std::is_same<T, float>::value)
+        SK_CUDA(cudaFuncSetAttribute(k_update_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     static_cast<int>(kTcSmem)));
     SK_CUDA(cudaFuncSetAttribute(k_potrf<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  static_cast<int>(potrf_smem(sizeof(T)))));
     SK_CUDA(cudaFuncSetAttribute(k_trsm<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -924,7 +1107,7 @@ KktEngine::KktEngine(const ipm::FrontPlan& plan, const DeviceLP& lp, cudaStream_
     reserve(arena_, fvec_, static_cast<size_t>(p.f_size));
     reserve(arena_, tn_, static_cast<size_t>(std::max(1, p.N)));
     reserve(arena_, params_, 4);
-    reserve(arena_, err_, 2);
+    reserve(arena_, err_, 4);
     arena_.commit();
     auto bnd = [&](auto& slot) { bind(arena_, slot); };
     bnd(sn_first_); bnd(sn_ncols_); bnd(sn_nrows_); bnd(sn_lda_); bnd(sn_parent_); bnd(rows_); bnd(ea_map_); bnd(ch_ptr_);
@@ -953,10 +1136,10 @@ KktEngine::KktEngine(const ipm::FrontPlan& plan, const DeviceLP& lp, cudaStream_
 }
 
 KktEngine::~KktEngine() {
-    for (int q = 0; q < 2; ++q) {
+    for (int q = 0; q < 3; ++q)
         if (gfac_[q]) cudaGraphExecDestroy(gfac_[q]);
+    for (int q = 0; q < 2; ++q)
         if (gsol_[q]) cudaGraphExecDestroy(gsol_[q]);
-    }
 }
 
 PlanDev KktEngine::pd() const {
@@ -973,7 +1156,7 @@ void KktEngine::launch_factor(T* F, T* Linv, Prof* prof) {
     const auto& p = plan_;
     const PlanDev pdv = pd();
     SK_CUDA(cudaMemsetAsync(F, 0, sizeof(T) * static_cast<size_t>(p.F_size), st_));
-    SK_CUDA(cudaMemsetAsync(err_.ptr, 0, 2 * sizeof(int), st_));
+    SK_CUDA(cudaMemsetAsync(err_.ptr, 0, 4 * sizeof(int), st_));
     const double* theta = theta_bound_;
     run(0, [&] {
         if (p.dense_mode) {
@@ -993,7 +1176,7 @@ void KktEngine::launch_factor(T* F, T* Linv, Prof* prof) {
     for (int l = 0; l < p.nlevels; ++l) {
         for (int q = p.step_level_ptr[l]; q < p.step_level_ptr[l + 1]; ++q) {
             const auto& st = p.steps[q];
-            StepArgs a{st.k, st.item_off, st.nitems, st.trsm_prefix_off, st.upd_prefix_off};
+            StepArgs a{st.k, st.item_off, st.nitems, st.trsm_prefix_off, st.upd_prefix_off, st.upd2_prefix_off};
             if (st.k == 0)   // later diagonal tiles are factored by the previous step's update
                 run(1, [&] {
                     k_potrf<T><<<st.nitems, 256, potrf_smem(sizeof(T)), st_>>>(a, step_items_.ptr, pdv, F, Linv,
@@ -1006,8 +1189,17 @@ void KktEngine::launch_factor(T* F, T* Linv, Prof* prof) {
                 });
             if (st.upd_tiles > 0) {
                 run(3, [&] {
-                    k_update<T><<<static_cast<int>(st.upd_tiles), 256, potrf_smem(sizeof(T)), st_>>>(
-                        a, step_items_.ptr, step_prefix_.ptr, pdv, F, Linv, inv_off_.ptr, err_.ptr);
+                    bool tc = false;
+                    if constexpr (std::is_same<T, float>::value) {
+                        if (tensor_) {
+                            tc = true;
+                            k_update_tc<<<static_cast<int>(st.upd2_blocks), 256, kTcSmem, st_>>>(
+                                a, step_items_.ptr, step_prefix_.ptr, pdv, F, Linv, inv_off_.ptr, err_.ptr);
+                        }
+                    }
+                    if (!tc)
+                        k_update<T><<<static_cast<int>(st.upd_tiles), 256, potrf_smem(sizeof(T)), st_>>>(
+                            a, step_items_.ptr, step_prefix_.ptr, pdv, F, Linv, inv_off_.ptr, err_.ptr);
                 });
                 if (prof) {
                     for (int it = 0; it < st.nitems; ++it) {
@@ -1094,7 +1286,7 @@ void KktEngine::ensure_fronts(bool fp32) {
 }
 
 bool KktEngine::factor(const double* d_theta, double delta, bool fp32) {
-    const int q = fp32 ? 1 : 0;
+    const int q = fp32 ? (tensor_ ? 2 : 1) : 0;
     ensure_fronts(fp32);
     fp32_ = fp32;
     double hp[4] = {delta, 0, 0, 0};
@@ -1111,9 +1303,10 @@ bool KktEngine::factor(const double* d_theta, double delta, bool fp32) {
         gfac_theta_[q] = d_theta;
     }
     SK_CUDA(cudaGraphLaunch(gfac_[q], st_));
-    int herr[2];
+    int herr[3];
     SK_CUDA(cudaMemcpyAsync(herr, err_.ptr, sizeof(herr), cudaMemcpyDeviceToHost, st_));
     SK_CUDA(cudaStreamSynchronize(st_));
+    if (herr[2]) throw std::runtime_error("tensor-core update: an MMA did not complete in time");
     failed_sn_ = herr[0] ? herr[1] : -1;
     return herr[0] == 0;
 }

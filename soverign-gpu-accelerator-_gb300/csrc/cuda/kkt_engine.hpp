@@ -28,6 +28,9 @@ public:
     // in FP64 (fp32 = false) or FP32 fronts. Returns true when every pivot was
     // positive (one host synchronisation).
     bool factor(const double* d_theta, double delta, bool fp32);
+    // FP32 fronts: trailing updates on the tensor cores (tcgen05, TF32 x3; default) or
+    // as exact FP32 SIMT arithmetic. Applies to the next factor() call.
+    void set_tensor_update(bool on) { tensor_ = on; }
     // dst = D L^{-T} L^{-1} D src (batch row order), using the last factor. src
     // and dst may alias. Asynchronous on the engine stream.
     void apply_inverse(const double* d_src, double* d_dst);
@@ -92,9 +95,10 @@ private:
     bool fp32_ = false;
     int failed_sn_ = -1;
     const double* theta_bound_ = nullptr;
-    cudaGraphExec_t gfac_[2] = {nullptr, nullptr};
+    bool tensor_ = true;
+    cudaGraphExec_t gfac_[3] = {nullptr, nullptr, nullptr};   // FP64, FP32 SIMT update, FP32 tensor-core update
     cudaGraphExec_t gsol_[2] = {nullptr, nullptr};
-    const double* gfac_theta_[2] = {nullptr, nullptr};
+    const double* gfac_theta_[3] = {nullptr, nullptr, nullptr};
 };
 
 }  // namespace dev

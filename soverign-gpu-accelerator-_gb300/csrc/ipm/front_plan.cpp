@@ -118,6 +118,16 @@ static void build_schedule(FrontPlan& p) {
                 p.step_prefix.push_back(static_cast<int>(acc));
             }
             st.upd_tiles = acc;
+            st.upd2_prefix_off = static_cast<int>(p.step_prefix.size());
+            acc = 0;
+            p.step_prefix.push_back(0);
+            for (int s : items) {
+                const int64_t w = std::min<int64_t>(kTile, p.sn_ncols[s] - static_cast<int64_t>(k) * kTile);
+                const int64_t t = p.sn_nrows[s] - static_cast<int64_t>(k) * kTile - w;
+                acc += tri(ceil_div(t, 2 * kTile));
+                p.step_prefix.push_back(static_cast<int>(acc));
+            }
+            st.upd2_blocks = acc;
             p.steps.push_back(st);
         }
         p.step_level_ptr[l + 1] = static_cast<int>(p.steps.size());

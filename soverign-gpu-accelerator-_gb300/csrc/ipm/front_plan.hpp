@@ -47,6 +47,8 @@ struct PlanStep {            // one tile step of one level
     int upd_prefix_off = 0;  // into step_prefix: nitems+1 entries (lower tiles of the trailing part)
     int64_t trsm_tiles = 0;
     int64_t upd_tiles = 0;
+    int upd2_prefix_off = 0; // into step_prefix: nitems+1 entries (lower 128x128 blocks of the trailing part)
+    int64_t upd2_blocks = 0;
 };
 
 struct PlanRound {           // one extend-add round after a level

@@ -306,9 +306,10 @@ class Solver:
         check(lib().sk_solver_result(self.h, k, None, None, None, C.byref(info)), "sk_solver_result")
         return info.as_dict(), None, None, None
 
-    def profile(self, fp32=True):
+    def profile(self, fp32=True, tensor=True):
+        """Kernel-class breakdown; fp32 fronts use tensor-core updates unless tensor=False."""
         out = np.zeros(16)
-        n = lib().sk_solver_profile(self.h, 1 if fp32 else 0, out, 16)
+        n = lib().sk_solver_profile(self.h, (1 if tensor else 2) if fp32 else 0, out, 16)
         if n < 0:
             raise RuntimeError("sk_solver_profile failed (%d): %s" % (n, last_error()))
         names = ["assembly", "potrf", "trsm", "update", "extend_add", "fwd_solve", "bwd_solve"]
