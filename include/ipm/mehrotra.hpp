@@ -32,6 +32,10 @@ struct MehrotraOptions {
     int strict = 0;
     double delta32 = 1e-8;
     double delta64 = 1e-14;
+    // false (default, as the reference): lb / ub of the model are ignored and x >= 0
+    // is solved; true: the model's bounds are honoured through the host standard form
+    // (core/standard_form.hpp).
+    bool honor_bounds = false;
 };
 
 struct MehrotraResult {

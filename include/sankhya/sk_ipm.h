@@ -110,6 +110,17 @@ int sk_ipm_solve_csc(int m, int n, const int* col_ptrs, const int* row_idx, cons
                      const double* b, const double* c, const sk_options* opt,
                      double* x, double* y, double* s, sk_info* info);
 
+/* As sk_ipm_solve_csc for min c^T x, A x = b, lb <= x <= ub (lb / ub may be NULL:
+ * 0 / +infinity; +-HUGE_VAL = unbounded). The LP is brought to standard form on the
+ * host (shifts, reflections, free-variable splits, one extra row per finite upper
+ * bound), solved on the device and mapped back: x (n) in the original variables, y
+ * (m) for the original rows, s = c - A^T y; info->objective is c^T x, the relative
+ * measures refer to the standard-form LP. No reference counterpart: the reference's
+ * device IPM ignores lb / ub (parsers::read_mps sets them, mps_reader.cpp:259-298). */
+int sk_ipm_solve_bounded(int m, int n, const int* col_ptrs, const int* row_idx, const double* vals,
+                         const double* b, const double* c, const double* lb, const double* ub,
+                         const sk_options* opt, double* x, double* y, double* s, sk_info* info);
+
 /* Persistent solver over a batch of independent LPs (num_lps >= 1), all resident in
  * device memory after creation. The batch is solved as one block-diagonal problem
  * with per-LP step lengths, merit and convergence.
@@ -257,6 +268,13 @@ int sk_lp_dims(const sk_lp* lp, int* m, int* n, int* nnz);
 int sk_lp_arrays(const sk_lp* lp, const int** col_ptrs, const int** row_idx, const double** vals,
                  const double** b, const double** c);
 int sk_lp_bounds(const sk_lp* lp, const double** lb, const double** ub);
+/* Host standard form of min c^T x, A x = b, lb <= x <= ub (see sk_ipm_solve_bounded):
+ * a new sk_lp with x' >= 0 and c^T x = c'^T x' + *obj_offset. Original column j is
+ * standard-form column j (negated when only ub is finite); free columns add one
+ * column each (after the n originals), finite upper bounds one row (after the m
+ * originals) and one slack column (last). */
+int sk_lp_standard_form(int m, int n, const int* col_ptrs, const int* row_idx, const double* vals, const double* b,
+                        const double* c, const double* lb, const double* ub, sk_lp** out, double* obj_offset);
 void sk_lp_free(sk_lp* lp);
 
 /* Last error message of the calling thread ("" if none). */

@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "api/sk_error.hpp"
+#include "core/standard_form.hpp"
 #include "cuda/device_ipm.hpp"
 #include "cuda/gnn.hpp"
 #include "cuda/kkt_engine.hpp"
@@ -93,6 +94,34 @@ int sk_ipm_solve_csc(int m, int n, const int* col_ptrs, const int* row_idx, cons
         dev::DeviceIPM solver({v}, {b}, {c}, o);
         solver.run();
         solver.result(0, x, y, s, info);
+        return SK_OK;
+    } catch (...) {
+        return api::status_of_current_exception();
+    }
+}
+
+int sk_ipm_solve_bounded(int m, int n, const int* col_ptrs, const int* row_idx, const double* vals,
+                         const double* b, const double* c, const double* lb, const double* ub, const sk_options* opt,
+                         double* x, double* y, double* s, sk_info* info) {
+    api::clear_error();
+    try {
+        const sk_options o = opts_or_default(opt);
+        check_options(o);
+        check_csc(m, n, col_ptrs, row_idx, vals, b, c);
+        core::BoundedLp bl;
+        bl.m = m; bl.n = n; bl.col_ptrs = col_ptrs; bl.row_idx = row_idx; bl.vals = vals; bl.b = b; bl.c = c;
+        bl.lb = lb; bl.ub = ub;
+        const core::StandardForm sf = core::to_standard_form(bl);
+        ipm::LpView v;
+        v.m = sf.m; v.n = sf.n; v.col_ptrs = sf.col_ptrs.data(); v.row_idx = sf.row_idx.data(); v.vals = sf.vals.data();
+        dev::DeviceIPM solver({v}, {sf.b.data()}, {sf.c.data()}, o);
+        solver.run();
+        std::vector<double> xs(sf.n), ys(sf.m), ss(sf.n);
+        sk_info in{};
+        solver.result(0, xs.data(), ys.data(), ss.data(), &in);
+        const double obj = core::recover_solution(bl, sf, xs.data(), ys.data(), x, y, s);
+        in.objective = obj;
+        if (info) *info = in;
         return SK_OK;
     } catch (...) {
         return api::status_of_current_exception();

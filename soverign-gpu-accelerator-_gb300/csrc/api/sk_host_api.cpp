@@ -11,6 +11,7 @@
 #include "ipm/front_plan.hpp"
 #include "ipm/symbolic.hpp"
 #include "parsers/mps_reader.hpp"
+#include "core/standard_form.hpp"
 #include "sankhya/sk_ipm.h"
 
 struct sk_lp {
@@ -114,6 +115,26 @@ int sk_lp_random(int m, int n, double density, unsigned long long seed, sk_lp** 
         auto* lp = new sk_lp;
         lp->model = core::Model::from_csc(g.m, g.n, g.col_ptrs.data(), g.row_idx.data(), g.vals.data(),
                                           g.b.data(), g.c.data());
+        *out = lp;
+        return SK_OK;
+    } catch (...) {
+        return api::status_of_current_exception();
+    }
+}
+
+int sk_lp_standard_form(int m, int n, const int* col_ptrs, const int* row_idx, const double* vals, const double* b,
+                        const double* c, const double* lb, const double* ub, sk_lp** out, double* obj_offset) {
+    api::clear_error();
+    if (!out) return SK_ERR_INVALID;
+    try {
+        core::BoundedLp bl;
+        bl.m = m; bl.n = n; bl.col_ptrs = col_ptrs; bl.row_idx = row_idx; bl.vals = vals; bl.b = b; bl.c = c;
+        bl.lb = lb; bl.ub = ub;
+        const core::StandardForm sf = core::to_standard_form(bl);
+        auto* lp = new sk_lp;
+        lp->model = core::Model::from_csc(sf.m, sf.n, sf.col_ptrs.data(), sf.row_idx.data(), sf.vals.data(),
+                                          sf.b.data(), sf.c.data());
+        if (obj_offset) *obj_offset = sf.obj_offset;
         *out = lp;
         return SK_OK;
     } catch (...) {

@@ -1,5 +1,6 @@
 // JSON-telemetry CLI: sankhya_cli <file.mps> | --family F [--instance I]
-//                   [--fp64] [--reference-criteria] [--verbose]
+//                   [--fp64] [--reference-criteria] [--bounds] [--verbose]
+// --bounds honours the model's variable bounds (the reference's IPM ignores them).
 // Prints one JSON object on stdout with the reference CLI's keys in the same
 // order (tests/benchmark/sankhya_benchmark_cli.cpp:84-97) followed by added keys;
 // diagnostics go to stderr. The timer starts before the solver is constructed,
@@ -38,10 +39,11 @@ int main(int argc, char** argv) {
         else if (t == "--fp64") opts.precision = SK_PREC_FP64;
         else if (t == "--reference-criteria") opts.criteria = SK_CRIT_REFERENCE;
         else if (t == "--verbose") opts.verbose = 1;
+        else if (t == "--bounds") opts.honor_bounds = true;
         else path = t;
     }
     if (path.empty() && family < 0) {
-        std::fprintf(stderr, "Usage: sankhya_cli <mps_file> | --family F [--instance I] [--fp64]\n");
+        std::fprintf(stderr, "Usage: sankhya_cli <mps_file> | --family F [--instance I] [--fp64] [--bounds]\n");
         return 1;
     }
     core::Model model;

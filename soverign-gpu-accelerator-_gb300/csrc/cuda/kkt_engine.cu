@@ -753,6 +753,8 @@ __global__ void __launch_bounds__(256, 1) k_fwd_tasks(const int2* __restrict__ t
             li[k] = (zc < w && q <= zc) ? Li[zc + q * T64] : T(0);
         }
     }
+    // this block's right-hand side (written by the gather before this kernel), loaded up front
+    const T fown = (tid < T64 && row0 + tid < rend) ? f[row0 + tid] : T(0);
     T acc = T(0);
     const int jmax = own ? i : nb;
     for (int j = 0; j < jmax;) {
@@ -795,7 +797,7 @@ __global__ void __launch_bounds__(256, 1) k_fwd_tasks(const int2* __restrict__ t
     __syncthreads();
     if (tid < T64) {
         const int rw = row0 + tid;
-        fb[tid] = rw < rend ? f[rw] - ((red[0][tid] + red[1][tid]) + (red[2][tid] + red[3][tid])) : T(0);
+        fb[tid] = rw < rend ? fown - ((red[0][tid] + red[1][tid]) + (red[2][tid] + red[3][tid])) : T(0);
     }
     __syncthreads();
     if (own) {

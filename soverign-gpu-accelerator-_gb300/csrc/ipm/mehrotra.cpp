@@ -1,6 +1,8 @@
 // MehrotraSolver: the reference-compatible C++ front end over the C ABI.
 #include "ipm/mehrotra.hpp"
 
+#include "core/standard_form.hpp"
+
 #include <new>
 #include <stdexcept>
 #include <string>
@@ -62,12 +64,21 @@ public:
         cost.resize(model.obj.size());
         for (size_t j = 0; j < cost.size(); ++j) cost[j] = sign * model.obj[j];
         const sk_options c = to_c(opts);
-        const int m = model.A.rows, n = model.A.cols;
+        int m = model.A.rows, n = model.A.cols;
         const int* cp = model.A.col_ptrs.data();
         const int* ri = model.A.row_indices.data();
         const double* va = model.A.values.data();
         const double* b = model.rhs.data();
         const double* cc = cost.data();
+        if (opts.honor_bounds) {
+            if (model.lb.size() != static_cast<size_t>(n) || model.ub.size() != static_cast<size_t>(n))
+                throw std::invalid_argument("MehrotraSolver: bounds need one entry per column");
+            bl.m = m; bl.n = n; bl.col_ptrs = cp; bl.row_idx = ri; bl.vals = va; bl.b = b; bl.c = cc;
+            bl.lb = model.lb.data(); bl.ub = model.ub.data();
+            sf = core::to_standard_form(bl);
+            m = sf.m; n = sf.n;
+            cp = sf.col_ptrs.data(); ri = sf.row_idx.data(); va = sf.vals.data(); b = sf.b.data(); cc = sf.c.data();
+        }
         const int rc = sk_solver_create(1, &m, &n, &cp, &ri, &va, &b, &cc, &c, &handle);
         if (rc != SK_OK) raise(rc, "MehrotraSolver");
     }
@@ -79,8 +90,15 @@ public:
         std::vector<Float> x(static_cast<size_t>(model.A.cols)), y(static_cast<size_t>(model.A.rows)),
             s(static_cast<size_t>(model.A.cols));
         sk_info info{};
-        rc = sk_solver_result(handle, 0, x.data(), y.data(), s.data(), &info);
-        if (rc != SK_OK) raise(rc, "MehrotraSolver::solve");
+        if (opts.honor_bounds) {
+            std::vector<Float> xs(static_cast<size_t>(sf.n)), ys(static_cast<size_t>(sf.m)), ss(static_cast<size_t>(sf.n));
+            rc = sk_solver_result(handle, 0, xs.data(), ys.data(), ss.data(), &info);
+            if (rc != SK_OK) raise(rc, "MehrotraSolver::solve");
+            info.objective = core::recover_solution(bl, sf, xs.data(), ys.data(), x.data(), y.data(), s.data());
+        } else {
+            rc = sk_solver_result(handle, 0, x.data(), y.data(), s.data(), &info);
+            if (rc != SK_OK) raise(rc, "MehrotraSolver::solve");
+        }
         if (model.sense == OptimizationSense::Maximize) {
             info.objective = -info.objective;
             for (auto& v : y) v = -v;
@@ -92,6 +110,8 @@ public:
     const core::Model& model;
     MehrotraOptions opts;
     std::vector<Float> cost;
+    core::BoundedLp bl;
+    core::StandardForm sf;
     sk_solver* handle = nullptr;
 };
 

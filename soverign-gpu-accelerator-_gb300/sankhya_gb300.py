@@ -69,6 +69,8 @@ def _declare(L):
     L.sk_lp_arrays.argtypes = [vp] + [C.POINTER(vp)] * 5
     L.sk_lp_bounds.argtypes = [vp, C.POINTER(vp), C.POINTER(vp)]
     L.sk_lp_free.argtypes = [vp]
+    L.sk_lp_standard_form.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p, _f64p, _f64p, vp, vp, C.POINTER(vp),
+                                      C.POINTER(C.c_double)]
     L.sk_compute_amd_ordering.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _i32p]
     L.sk_fill_ordering.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _i32p]
     L.sk_plan_stats.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p, C.c_int, _f64p, C.c_int]
@@ -77,6 +79,8 @@ def _declare(L):
         L.sk_ipm_solve_csc.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p, _f64p, _f64p, C.POINTER(Options),
                                        vp, vp, vp, C.POINTER(Info)]
         L.sk_solver_create.argtypes = [C.c_int, vp, vp, vp, vp, vp, vp, vp, C.POINTER(Options), C.POINTER(vp)]
+        L.sk_ipm_solve_bounded.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p, _f64p, _f64p, vp, vp,
+                                           C.POINTER(Options), vp, vp, vp, C.POINTER(Info)]
         L.sk_solver_set_start.argtypes = [vp, C.c_int, vp, vp, vp]
         L.sk_solver_run.argtypes = [vp]
         L.sk_solver_result.argtypes = [vp, C.c_int, vp, vp, vp, C.POINTER(Info)]
@@ -188,6 +192,37 @@ def random_lp(m, n, density, seed):
     h = C.c_void_p()
     check(lib().sk_lp_random(m, n, density, seed, C.byref(h)), "sk_lp_random")
     return _lp_from_handle(h, "random%dx%d" % (m, n))
+
+
+def _bounds(n, lb, ub):
+    lb = None if lb is None else np.ascontiguousarray(lb, dtype=np.float64)
+    ub = None if ub is None else np.ascontiguousarray(ub, dtype=np.float64)
+    for v in (lb, ub):
+        if v is not None and v.shape != (n,):
+            raise ValueError("bounds need one entry per column")
+    return lb, ub
+
+
+def standard_form(lp, lb=None, ub=None):
+    """Host standard form of min c^T x, A x = b, lb <= x <= ub (sk_lp_standard_form):
+    returns (LP with x' >= 0, objective offset)."""
+    lb, ub = _bounds(lp.n, lb, ub)
+    h = C.c_void_p()
+    off = C.c_double()
+    check(lib().sk_lp_standard_form(lp.m, lp.n, lp.col_ptrs, lp.row_idx, lp.vals, lp.b, lp.c, _ptr(lb), _ptr(ub),
+                                    C.byref(h), C.byref(off)), "sk_lp_standard_form")
+    return _lp_from_handle(h, lp.name + "/std"), off.value
+
+
+def solve_bounded(lp, lb=None, ub=None, **opts):
+    """Device solve of min c^T x, A x = b, lb <= x <= ub (sk_ipm_solve_bounded)."""
+    lb, ub = _bounds(lp.n, lb, ub)
+    o = options(**opts)
+    x, y, s = np.zeros(lp.n), np.zeros(lp.m), np.zeros(lp.n)
+    info = Info()
+    check(lib().sk_ipm_solve_bounded(lp.m, lp.n, lp.col_ptrs, lp.row_idx, lp.vals, lp.b, lp.c, _ptr(lb), _ptr(ub),
+                                     C.byref(o), _ptr(x), _ptr(y), _ptr(s), C.byref(info)), "sk_ipm_solve_bounded")
+    return info.as_dict(), x, y, s
 
 
 def block_angular(seed, blocks, block_rows=500, block_cols=1200, link_rows=2000, nnz_per_col=5):

@@ -156,3 +156,38 @@ def test_mehrotra_start_reaches_reference_objective(gpu, oracle, case, precision
     assert meas["rel_pinf"] <= TOL and meas["rel_dinf"] <= TOL and meas["rel_gap"] <= TOL
     o, _, _, _ = oracle.ipm_solve(lp, start=1)
     assert o["status"] == 0 and abs(info["iterations"] - o["iterations"]) <= 2
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("seed", [3, 4])
+def test_bounded_lp_on_device(gpu, seed, precision):
+    # Variable bounds through sk_ipm_solve_bounded (host standard form, device solve,
+    # mapped back) against an independent solver (SciPy's HiGHS).
+    pytest.importorskip("scipy.optimize")
+    from bounded_cases import bounded_case, highs_objective
+    sk = gpu
+    lp, lb, ub, A = bounded_case(sk, seed)
+    ref = highs_objective(lp, lb, ub, A)
+    info, x, y, s = sk.solve_bounded(lp, lb, ub, precision=precision)
+    assert info["status"] == 0
+    assert abs(info["objective"] - ref) / (1 + abs(ref)) <= TOL
+    assert np.max(np.abs(A @ x - lp.b)) <= 1e-7 * (1 + np.max(np.abs(lp.b)))
+    assert np.all(x >= lb - 1e-7) and np.all(x <= ub + 1e-7)
+    np.testing.assert_allclose(s, lp.c - A.T @ y, atol=1e-9)
+
+
+def test_cli_honours_mps_bounds(gpu, tmp_path):
+    # An MPS file with LO / UP / MI / FR bounds through the CLI with --bounds.
+    pytest.importorskip("scipy.optimize")
+    import subprocess
+    from bounded_cases import bounded_case, highs_objective, write_mps
+    sk = gpu
+    lp, lb, ub, A = bounded_case(sk, 5)
+    ref = highs_objective(lp, lb, ub, A)
+    path = tmp_path / "bounded.mps"
+    write_mps(str(path), lp, lb, ub)
+    cli = os.path.join(os.path.dirname(sk.LIB_PATH), "sankhya_cli")
+    out = subprocess.run([cli, str(path), "--bounds"], capture_output=True, text=True, check=True).stdout
+    res = json.loads(out)
+    assert res["status"] == "Optimal"
+    assert abs(res["objective"] - ref) / (1 + abs(ref)) <= TOL
