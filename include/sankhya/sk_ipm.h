@@ -64,7 +64,7 @@ typedef struct sk_options {
                            * with e1, e2 or e3 > 1e-8 ends the LP with IterationLimit, as the reference
                            * does (src/ipm/mehrotra_device.cu:793-797, 814-822). 0 (default): such a
                            * miss first switches a mixed-precision solve to the FP64 factor; an FP64
-                           * direction is then used when it is finite with e1, e2, e3 <= 1e-6, and the
+                           * direction is then used when it is finite with e1, e2, e3 <= 1e-4, and the
                            * merit line search plus the exact stopping test decide progress. */
     double delta32;       /* first regularisation of FP32 fronts (default 1e-8); x10 per failed attempt */
     double delta64;       /* first regularisation of FP64 fronts (default 1e-14; strict mode uses 1e-9) */

@@ -588,7 +588,7 @@ int oracle_ipm_solve(int m, int n, const int* cp, const int* ri, const double* v
         for (int j = 0; j < n; ++j) { w.rxs[j] = -x[j] * s[j]; w.v[j] = -w.theta[j] * w.rd[j] - w.rxs[j] / s[j]; }
         spmv_A(&p, w.v, w.rkkt);
         for (int i = 0; i < m; ++i) w.rkkt[i] -= w.rp[i];
-        const double vlim = opts.strict ? 1e-8 : 1e-6;
+        const double vlim = opts.strict ? 1e-8 : 1e-4;
         if (!normal_solve(&p, &k, w.theta, w.rkkt, tol, w.dy_aff, &r.solves) && opts.strict) { r.status = 3; break; }
         spmv_At(&p, w.dy_aff, w.ds_aff);
         for (int j = 0; j < n; ++j) { w.ds_aff[j] = -w.rd[j] - w.ds_aff[j]; w.dx_aff[j] = -w.theta[j] * w.ds_aff[j] + w.rxs[j] / s[j]; }

@@ -53,7 +53,7 @@ typedef struct oracle_ipm_opts {
     int start;         /* 0: x = s = 1, y = 0 (reference :93-102); 1: Mehrotra's heuristic start */
     int strict;        /* 1: a missed solve tolerance or direction check ends the solve with
                         * IterationLimit (reference :793-797, :814-822); 0: the direction is
-                        * used when finite with e1, e2, e3 <= 1e-6 (the stopping test and the
+                        * used when finite with e1, e2, e3 <= 1e-4 (the stopping test and the
                         * merit line search still decide progress) */
 } oracle_ipm_opts;
 

@@ -39,6 +39,9 @@ constexpr double kLearnedSaturated = 0.99;   // learned start: upper bound on it
 constexpr double kShortStep = 0.1;           // learned-start restart: a step shorter than this ...
 constexpr int kShortSteps = 3;               // ... this many times ...
 constexpr int kRestartWindow = 10;           // ... within the first iterations
+// robust mode: a direction whose checks e1, e2, e3 stay below this is used (the merit
+// line search then decides); tighter checks stalled a few LPs just short of 1e-8
+constexpr double kUseDir = 1e-4;
 constexpr double kTensorMu = 1e-4;           // FP32 fronts: tensor-core updates while mu >= this
 constexpr int kLooseIters = 3;               // stall acceptance of the relative tests (see the stopping rule)
 constexpr int kProgressIter = 12;            // learned-start restart: by this iteration the distance to the
@@ -941,7 +944,7 @@ void DeviceIPM::run() {
             const bool fin = std::isfinite(ds_.e1[k]) && std::isfinite(ds_.e2[k]) && std::isfinite(ds_.e3[k]) &&
                              std::isfinite(ds_.rx[k]) && std::isfinite(ds_.rs[k]);
             acc[k] = solved[k] && fin && e <= 1e-8;
-            use[k] = o.strict ? acc[k] : (fin && e <= 1e-6);
+            use[k] = o.strict ? acc[k] : (fin && e <= kUseDir);
         }
     };
     auto any_active_missing = [&](const std::vector<char>& v) {
