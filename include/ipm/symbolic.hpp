@@ -29,6 +29,20 @@ void compute_symbolic_factorization(const core::CSRMatrix& A, const std::vector<
 // external degrees) on the graph of A A^T; P[k] = original row eliminated k-th.
 std::vector<Index> fill_reducing_ordering(const core::CSRMatrix& A);
 
+// The same ordering on an explicit graph: Av[i] = sorted neighbours of vertex i
+// (no self loops, symmetric). P[k] = vertex eliminated k-th.
+std::vector<Index> min_degree_order(std::vector<std::vector<Index>> Av);
+
+// Sorted, duplicate-free adjacency of A A^T without self loops.
+std::vector<std::vector<Index>> aat_graph(const core::CSRMatrix& A);
+
+// Nested dissection of the graph of A A^T: recursive vertex separators from
+// breadth-first level structures (a level, or the minimum vertex cut through a band
+// of adjacent levels), separators ordered after both sides; parts whose best
+// separator is larger than the smaller side, and parts of at most `leaf`
+// vertices, are ordered by min_degree_order.
+std::vector<Index> nested_dissection_ordering(const core::CSRMatrix& A, Index leaf = 1000);
+
 // Lower adjacency of A A^T in CSR with rows / columns in the given order:
 // row k lists j < k (increasing) such that rows P[k], P[j] of A share a column.
 void permuted_lower_pattern(const core::CSRMatrix& A, const std::vector<Index>& P_inv,

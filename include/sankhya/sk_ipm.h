@@ -46,9 +46,13 @@ extern "C" {
 #define SK_CRIT_REFERENCE 1    /* ||rp||_2, ||rd||_2, mu < 1e-6 on the scaled LP (src/ipm/mehrotra_device.cu:746-748) */
 
 /* Fill-reducing ordering of A A^T. */
-#define SK_ORDER_AUTO 0        /* approximate minimum degree, or one dense front when A A^T is dense */
+#define SK_ORDER_AUTO 0        /* one dense front when A A^T is dense; else approximate minimum degree; for
+                                  LPs of >= 50000 rows the given row order or nested dissection, whichever
+                                  needs fewer factorisation flops */
 #define SK_ORDER_REFERENCE 1   /* exact minimum degree, lowest index wins ties (src/ipm/symbolic.cpp:11-98) */
 #define SK_ORDER_NATURAL 2
+#define SK_ORDER_MINDEG 3      /* approximate minimum degree */
+#define SK_ORDER_DISSECTION 4  /* nested dissection (level-structure separators, minimum vertex covers) */
 
 typedef struct sk_options {
     int precision;        /* SK_PREC_* (default SK_PREC_MIXED) */
@@ -215,6 +219,10 @@ int sk_compute_symbolic(int m, int n, const int* row_ptrs, const int* col_idx, c
 /* Fill-reducing approximate minimum degree order of A A^T used by the solver (no
  * reference counterpart beyond compute_amd_ordering's role). */
 int sk_fill_ordering(int m, int n, const int* row_ptrs, const int* col_idx, int* P);
+/* Nested dissection order of A A^T (SK_ORDER_DISSECTION; no reference counterpart):
+ * separators from breadth-first level structures narrowed to minimum vertex covers,
+ * each ordered after the two parts it splits. */
+int sk_dissection_ordering(int m, int n, const int* row_ptrs, const int* col_idx, int* P);
 
 /* Host-only analysis of one LP's normal matrix (no device needed): builds the
  * multifrontal plan the solver would use and writes out[0..15] =
@@ -263,6 +271,10 @@ int sk_lp_random(int m, int n, double density, unsigned long long seed, sk_lp** 
  * blocks=40, block_rows=500, block_cols=1200, link_rows=2000, nnz_per_col=5). */
 int sk_lp_block_angular(unsigned long long seed, int blocks, int block_rows, int block_cols, int link_rows,
                         int nnz_per_col, sk_lp** out);
+/* Staircase transportation member of family 2 with a chosen shape (family 2 itself is
+ * stages=50, supply=demand=1000, cap=2000, arcs=8000: m = stages (supply + demand + cap),
+ * n = stages (arcs + cap)). */
+int sk_lp_staircase(unsigned long long seed, int stages, int supply, int demand, int cap, int arcs, sk_lp** out);
 int sk_lp_dims(const sk_lp* lp, int* m, int* n, int* nnz);
 /* Pointers into the LP's own storage (valid until sk_lp_free). lb / ub may be NULL. */
 int sk_lp_arrays(const sk_lp* lp, const int** col_ptrs, const int** row_idx, const double** vals,

@@ -68,7 +68,7 @@ void check_options(const sk_options& o) {
     if (o.criteria != SK_CRIT_RELATIVE && o.criteria != SK_CRIT_REFERENCE) throw std::invalid_argument("bad criteria");
     if (!(o.tol > 0.0) || o.max_iter < 0 || o.ruiz_passes < 0) throw std::invalid_argument("bad tolerance / limits");
     if (!(o.learned_accept >= 0.0)) throw std::invalid_argument("bad learned_accept");
-    if (o.ordering < SK_ORDER_AUTO || o.ordering > SK_ORDER_NATURAL) throw std::invalid_argument("bad ordering");
+    if (o.ordering < SK_ORDER_AUTO || o.ordering > SK_ORDER_DISSECTION) throw std::invalid_argument("bad ordering");
 }
 
 void check_csc(int m, int n, const int* cp, const int* ri, const double* v, const double* b, const double* c) {

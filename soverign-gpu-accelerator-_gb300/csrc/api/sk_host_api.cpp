@@ -142,6 +142,22 @@ int sk_lp_standard_form(int m, int n, const int* col_ptrs, const int* row_idx, c
     }
 }
 
+int sk_lp_staircase(unsigned long long seed, int stages, int supply, int demand, int cap, int arcs, sk_lp** out) {
+    api::clear_error();
+    if (!out || stages <= 0 || supply <= 0 || demand <= 0 || cap <= 1 || arcs < supply || arcs < demand)
+        return SK_ERR_INVALID;
+    try {
+        auto g = gen::staircase_transport_lp(seed, stages, supply, demand, cap, arcs);
+        auto* lp = new sk_lp;
+        lp->model = core::Model::from_csc(g.m, g.n, g.col_ptrs.data(), g.row_idx.data(), g.vals.data(),
+                                          g.b.data(), g.c.data());
+        *out = lp;
+        return SK_OK;
+    } catch (...) {
+        return api::status_of_current_exception();
+    }
+}
+
 int sk_lp_block_angular(unsigned long long seed, int blocks, int block_rows, int block_cols, int link_rows,
                         int nnz_per_col, sk_lp** out) {
     api::clear_error();
@@ -224,6 +240,18 @@ int sk_fill_ordering(int m, int n, const int* row_ptrs, const int* col_idx, int*
     if (!P) return SK_ERR_INVALID;
     try {
         auto p = ipm::fill_reducing_ordering(api::pattern_csr(m, n, row_ptrs, col_idx));
+        std::memcpy(P, p.data(), sizeof(int) * static_cast<size_t>(m));
+        return SK_OK;
+    } catch (...) {
+        return api::status_of_current_exception();
+    }
+}
+
+int sk_dissection_ordering(int m, int n, const int* row_ptrs, const int* col_idx, int* P) {
+    api::clear_error();
+    if (!P) return SK_ERR_INVALID;
+    try {
+        auto p = ipm::nested_dissection_ordering(api::pattern_csr(m, n, row_ptrs, col_idx));
         std::memcpy(P, p.data(), sizeof(int) * static_cast<size_t>(m));
         return SK_OK;
     } catch (...) {

@@ -181,10 +181,12 @@ GeneratedLP block_angular_lp(uint64_t seed, Index blocks, Index block_rows, Inde
     return lp;
 }
 
-GeneratedLP staircase_transport_lp(uint64_t seed, Index stages) {
-    constexpr Index kSupply = 1000, kDemand = 1000, kCap = 2000, kArcs = 8000;
-    constexpr Index kRowsPerStage = kSupply + kDemand + kCap;
-    constexpr Index kColsPerStage = kArcs + kCap;
+GeneratedLP staircase_transport_lp(uint64_t seed, Index stages, Index kSupply, Index kDemand, Index kCap,
+                                   Index kArcs) {
+    if (stages <= 0 || kSupply <= 0 || kDemand <= 0 || kCap <= 1 || kArcs < std::max(kSupply, kDemand))
+        throw std::invalid_argument("staircase_transport_lp: bad shape");
+    const Index kRowsPerStage = kSupply + kDemand + kCap;
+    const Index kColsPerStage = kArcs + kCap;
     Rng g(seed);
     GeneratedLP lp;
     lp.m = stages * kRowsPerStage;

@@ -50,7 +50,10 @@ GeneratedLP random_sparse_lp(Index m, Index n, double density, uint64_t seed);
 GeneratedLP block_angular_lp(uint64_t seed, Index blocks = 40, Index block_rows = 500,
                              Index block_cols = 1200, Index link_rows = 2000,
                              Index nnz_per_block_col = 5);
-GeneratedLP staircase_transport_lp(uint64_t seed, Index stages = 50);
+// Family 2 is stages=50, supply=demand=1000, cap=2000, arcs=8000 (rows per stage
+// supply + demand + cap, columns per stage arcs + cap).
+GeneratedLP staircase_transport_lp(uint64_t seed, Index stages = 50, Index supply = 1000, Index demand = 1000,
+                                   Index cap = 2000, Index arcs = 8000);
 GeneratedLP family_lp(int family, int instance);
 
 }  // namespace gen

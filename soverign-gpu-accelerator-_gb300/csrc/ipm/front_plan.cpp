@@ -219,6 +219,40 @@ static void finish_offsets(FrontPlan& p) {
     }
 }
 
+namespace {
+
+// Automatic ordering from this many rows (of the largest LP) on: the given row
+// order or nested dissection, whichever needs fewer factorisation flops. Minimum
+// degree is left out there: its quotient-graph elimination (no supervariables)
+// takes minutes at 200000 rows.
+constexpr Index kLargeRows = 50000;
+
+// Factorisation flops sum_j c_j^2 (c_j = column count of L incl. the diagonal)
+// of the normal matrix in elimination order perm.
+double factor_flops(const core::CSRMatrix& A, const std::vector<Index>& perm) {
+    const Index M = A.rows;
+    std::vector<Index> iperm(static_cast<size_t>(M));
+    for (Index k = 0; k < M; ++k) iperm[perm[k]] = k;
+    std::vector<Index> rp, ci;
+    permuted_lower_pattern(A, iperm, rp, ci);
+    const std::vector<Index> parent = elimination_tree(M, rp, ci);
+    std::vector<int64_t> cc(static_cast<size_t>(M), 1);
+    std::vector<Index> mark(static_cast<size_t>(M), -1);
+    for (Index i = 0; i < M; ++i) {
+        mark[i] = i;
+        for (Index q = rp[i]; q < rp[i + 1]; ++q)
+            for (Index j = ci[q]; j != -1 && mark[j] != i; j = parent[j]) {
+                mark[j] = i;
+                cc[j]++;
+            }
+    }
+    double f = 0.0;
+    for (Index j = 0; j < M; ++j) f += static_cast<double>(cc[j]) * static_cast<double>(cc[j]);
+    return f;
+}
+
+}  // namespace
+
 void build_front_plan(const std::vector<LpView>& lps, const core::CSRMatrix& A, int ordering, FrontPlan& p,
                       const std::vector<Index>* explicit_perm) {
     p = FrontPlan();
@@ -278,9 +312,27 @@ void build_front_plan(const std::vector<LpView>& lps, const core::CSRMatrix& A, 
         perm0.resize(static_cast<size_t>(p.M));
         std::iota(perm0.begin(), perm0.end(), 0);
         p.ordering_used = 2;
+    } else if (ordering == 4) {
+        perm0 = nested_dissection_ordering(A);
+        p.ordering_used = 4;
     } else {
-        perm0 = fill_reducing_ordering(A);
-        p.ordering_used = 0;
+        Index largest = 0;
+        for (const auto& v : lps) largest = std::max(largest, v.m);
+        if (ordering == 0 && largest >= kLargeRows) {
+            // the given row order (stage-major models are nearly banded) or nested
+            // dissection, whichever needs fewer flops
+            perm0.resize(static_cast<size_t>(p.M));
+            std::iota(perm0.begin(), perm0.end(), 0);
+            p.ordering_used = 2;
+            std::vector<Index> nd = nested_dissection_ordering(A);
+            if (factor_flops(A, nd) < factor_flops(A, perm0)) {
+                perm0.swap(nd);
+                p.ordering_used = 4;
+            }
+        } else {
+            perm0 = fill_reducing_ordering(A);
+            p.ordering_used = 0;
+        }
     }
     std::vector<Index> iperm0(static_cast<size_t>(p.M));
     for (Index k = 0; k < p.M; ++k) iperm0[perm0[k]] = k;

@@ -100,8 +100,12 @@ struct FrontPlan {
     std::vector<Float> w_val;
 };
 
-// Builds the plan. ordering: 0 auto (AMD or dense), 1 reference exact minimum
-// degree, 2 natural. A_csr is the batch matrix (block diagonal) in CSR.
+// Builds the plan. ordering: 0 auto (dense or approximate minimum degree; from
+// 50000 rows on the given row order or nested dissection, whichever needs fewer
+// flops), 1 reference exact minimum degree, 2 natural, 3 approximate minimum
+// degree, 4 nested dissection.
+// ordering_used: 0 minimum degree, 1 reference, 2 natural / dense, 3 explicit,
+// 4 nested dissection. A_csr is the batch matrix (block diagonal) in CSR.
 // explicit_perm (optional, sparse mode): use this elimination order as given
 // (no postorder relabelling), e.g. the reference's ordering in parity tests.
 void build_front_plan(const std::vector<LpView>& lps, const core::CSRMatrix& A_csr, int ordering,

@@ -23,6 +23,8 @@ void column_rows(const core::CSRMatrix& A, std::vector<Index>& cptr, std::vector
         for (Index k = A.row_ptrs[i]; k < A.row_ptrs[i + 1]; ++k) crow[next[A.col_indices[k]]++] = i;
 }
 
+}  // namespace
+
 // Sorted, duplicate-free adjacency of A A^T without self loops.
 std::vector<std::vector<Index>> aat_graph(const core::CSRMatrix& A) {
     std::vector<Index> cptr, crow;
@@ -43,8 +45,6 @@ std::vector<std::vector<Index>> aat_graph(const core::CSRMatrix& A) {
     }
     return adj;
 }
-
-}  // namespace
 
 std::vector<Index> compute_amd_ordering(const core::CSRMatrix& A) {
     const Index m = A.rows;
@@ -175,11 +175,14 @@ void compute_symbolic_factorization(const core::CSRMatrix& A, const std::vector<
 // A lazily kept variable popped as pivot is re-scored first.
 // Ties go to the most recently inserted variable of the minimum-degree bucket.
 std::vector<Index> fill_reducing_ordering(const core::CSRMatrix& A) {
-    const Index m = A.rows;
+    return min_degree_order(aat_graph(A));
+}
+
+std::vector<Index> min_degree_order(std::vector<std::vector<Index>> Av) {
+    const Index m = static_cast<Index>(Av.size());
     std::vector<Index> order;
     order.reserve(static_cast<size_t>(m));
     if (m == 0) return order;
-    auto Av = aat_graph(A);                        // variable neighbours
     std::vector<std::vector<Index>> Ev(static_cast<size_t>(m));   // adjacent elements
     std::vector<std::vector<Index>> Le(static_cast<size_t>(m));   // element members (live variables)
     std::vector<char> eliminated(static_cast<size_t>(m), 0), dead_elem(static_cast<size_t>(m), 0);

@@ -18,7 +18,7 @@ STATUS = {0: "Optimal", 1: "Infeasible", 2: "Unbounded", 3: "IterationLimit"}
 PREC_FP64, PREC_MIXED = 0, 1
 START_UNIT, START_MEHROTRA, START_USER, START_LEARNED = 0, 1, 2, 3
 CRIT_RELATIVE, CRIT_REFERENCE = 0, 1
-ORDER_AUTO, ORDER_REFERENCE, ORDER_NATURAL = 0, 1, 2
+ORDER_AUTO, ORDER_REFERENCE, ORDER_NATURAL, ORDER_MINDEG, ORDER_DISSECTION = 0, 1, 2, 3, 4
 
 _i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
 _f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
@@ -65,6 +65,7 @@ def _declare(L):
     L.sk_lp_random.argtypes = [C.c_int, C.c_int, C.c_double, C.c_ulonglong, C.POINTER(vp)]
     L.sk_lp_read_mps.argtypes = [C.c_char_p, C.POINTER(vp)]
     L.sk_lp_block_angular.argtypes = [C.c_ulonglong, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(vp)]
+    L.sk_lp_staircase.argtypes = [C.c_ulonglong, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(vp)]
     L.sk_lp_dims.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
     L.sk_lp_arrays.argtypes = [vp] + [C.POINTER(vp)] * 5
     L.sk_lp_bounds.argtypes = [vp, C.POINTER(vp), C.POINTER(vp)]
@@ -73,6 +74,7 @@ def _declare(L):
                                       C.POINTER(C.c_double)]
     L.sk_compute_amd_ordering.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _i32p]
     L.sk_fill_ordering.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _i32p]
+    L.sk_dissection_ordering.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _i32p]
     L.sk_plan_stats.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p, C.c_int, _f64p, C.c_int]
     L.sk_compute_symbolic.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _i32p, _i32p, _i32p, _i32p, _i32p, C.c_int]
     if hasattr(L, "sk_ipm_solve_csc"):
@@ -232,6 +234,12 @@ def block_angular(seed, blocks, block_rows=500, block_cols=1200, link_rows=2000,
     return _lp_from_handle(h, "block_angular%dx%d" % (blocks, link_rows))
 
 
+def staircase(seed, stages, supply=1000, demand=1000, cap=2000, arcs=8000):
+    h = C.c_void_p()
+    check(lib().sk_lp_staircase(seed, stages, supply, demand, cap, arcs, C.byref(h)), "sk_lp_staircase")
+    return _lp_from_handle(h, "staircase%dx%d" % (stages, supply + demand + cap))
+
+
 def read_mps(path):
     h = C.c_void_p()
     check(lib().sk_lp_read_mps(path.encode(), C.byref(h)), "sk_lp_read_mps")
@@ -247,6 +255,12 @@ def amd_ordering(m, n, rp, ci):
 def fill_ordering(m, n, rp, ci):
     P = np.zeros(m, dtype=np.int32)
     check(lib().sk_fill_ordering(m, n, rp, ci, P), "sk_fill_ordering")
+    return P
+
+
+def dissection_ordering(m, n, rp, ci):
+    P = np.zeros(m, dtype=np.int32)
+    check(lib().sk_dissection_ordering(m, n, rp, ci, P), "sk_dissection_ordering")
     return P
 
 

@@ -78,3 +78,33 @@ def test_symbolic_rejects_bad_permutation(sk):
     ci = np.array([0, 1], dtype=np.int32)
     with pytest.raises(RuntimeError):
         sk.symbolic(2, 2, rp, ci, np.array([0, 0], dtype=np.int32))
+
+
+def test_dissection_ordering_is_permutation(sk):
+    # several components (the staircase has coupling rows without arcs) and a random LP
+    for lp in (sk.staircase(3, 4, 100, 100, 200, 800), sk.random_lp(600, 1400, 0.008, 4)):
+        rp, ci, _ = lp.csr()
+        P = sk.dissection_ordering(lp.m, lp.n, rp, ci)
+        assert sorted(P.tolist()) == list(range(lp.m))
+        st = sk.plan_stats(lp, sk.ORDER_DISSECTION)
+        assert st["ordering_used"] == 4 and st["consistent"] == 1
+
+
+def test_dissection_beats_minimum_degree_on_staircase(sk):
+    # 8 stages of 250 supply + 250 demand + 500 capacity rows: the coupling rows of
+    # each stage separate the stages, which greedy minimum degree interleaves
+    lp = sk.staircase(7, 8, 250, 250, 500, 2000)
+    nd = sk.plan_stats(lp, sk.ORDER_DISSECTION)
+    md = sk.plan_stats(lp, sk.ORDER_MINDEG)
+    assert nd["consistent"] == 1 and md["ordering_used"] == 0
+    assert nd["flops_factor"] < 0.75 * md["flops_factor"]
+
+
+def test_auto_ordering_of_a_large_staircase(sk):
+    # >= 50000 rows: the automatic choice takes the cheaper of the row order and
+    # nested dissection (13 stages, m = 52000)
+    lp = sk.staircase(0xC2, 13)
+    auto = sk.plan_stats(lp, sk.ORDER_AUTO)
+    nat = sk.plan_stats(lp, sk.ORDER_NATURAL)
+    assert auto["ordering_used"] in (2, 4) and auto["consistent"] == 1
+    assert auto["flops_factor"] <= nat["flops_factor"] * (1 + 1e-12)
