@@ -168,6 +168,60 @@ def batch_comparison(sk, nlps):
     return out
 
 
+def family2_comparison(sk):
+    """Time-to-1e-8 on the family-2 staircase LP (m=200000, n=500000): mixed precision with
+    the learned start (falling back to Mehrotra's start), mixed precision with the plain
+    method's unit start, and the plain FP64 IPM. One solve per arm (each solve is tens of
+    seconds); host analysis (ordering, plan) is timed separately from the device solve."""
+    lp = sk.generate(2, 0)
+    ref = None
+    fixture = os.path.join(ROOT, "tests", "golden", "highs_large_objectives.json")
+    if os.path.exists(fixture):
+        with open(fixture) as f:
+            for c in json.load(f)["cases"]:
+                if c["name"] == "family2_0" and c["digest"]["nnz"] == lp.nnz:
+                    ref = c["objective"]
+    net = None
+    if os.path.exists(WEIGHTS):
+        net = sk.Gnn(1)
+        net.load(WEIGHTS)
+    out = {"workload": "staircase transportation LP, 50 stages (m=200000, n=500000, 4 nnz/col), seed 0xC2",
+           "objective_reference": "HiGHS (tests/golden/highs_large_objectives.json)" if ref is not None else None}
+    arms = [("mixed_learned", sk.PREC_MIXED, sk.START_LEARNED), ("mixed_unit_start", sk.PREC_MIXED, sk.START_UNIT),
+            ("plain_fp64", sk.PREC_FP64, sk.START_UNIT)]
+    for name, prec, start in arms:
+        if start == sk.START_LEARNED and net is None:
+            continue
+        t0 = time.perf_counter()
+        s = sk.Solver([lp], precision=prec, start=start)
+        t1 = time.perf_counter()
+        if start == sk.START_LEARNED:
+            s.set_gnn(net)
+        s.run()
+        info, *_ = s.result(0, want_vectors=False)
+        t2 = time.perf_counter()
+        s.close()
+        arm = {"status": info["status"], "iterations": info["iterations"], "device_ms": info["device_ms"],
+               "analysis_s": t1 - t0, "wall_s": t2 - t0, "objective": info["objective"],
+               "rel_pinf": info["rel_pinf"], "rel_dinf": info["rel_dinf"], "rel_gap": info["rel_gap"],
+               "precision_path": info["precision_path"], "switch_iteration": info["switch_iteration"],
+               "factorizations": info["factorizations"], "solves": info["solves"],
+               "nnz_factor": info["nnz_factor"], "flops_per_factorization": info["flops_factor"]}
+        if start == sk.START_LEARNED:
+            arm["learned_used"] = info["learned_start"]
+        if ref is not None:
+            arm["rel_obj_err_vs_highs"] = abs(info["objective"] - ref) / (1.0 + abs(ref))
+        out[name] = arm
+    if net is not None:
+        net.close()
+    base = out["plain_fp64"]
+    for name in ("mixed_learned", "mixed_unit_start"):
+        if name in out:
+            out[name]["speedup_device_vs_plain_fp64"] = base["device_ms"] / out[name]["device_ms"]
+            out[name]["speedup_wall_vs_plain_fp64"] = base["wall_s"] / out[name]["wall_s"]
+    return out
+
+
 def dist_setup(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -240,6 +294,7 @@ def run_ours(args):
     prof64 = fp64.profile(fp32=False)
     fp64.close()
     batch = batch_comparison(sk, args.batch_lps) if args.batch_lps > 0 else None
+    family2 = family2_comparison(sk) if args.family2 else None
     # end to end through the C ABI (host arrays in, host solution out)
     e2e_t = []
     for _ in range(max(1, args.steps)):
@@ -300,6 +355,7 @@ def run_ours(args):
                        "solves": info["solves"], "nnz_factor": info["nnz_factor"],
                        "supernodes": info["num_supernodes"], "flops_per_factorization": info["flops_factor"]},
             "batch_family3": batch,
+            "staircase_family2": family2,
             "plain_fp64": {"ms_per_solve": info64b["device_ms"], "iterations": info64b["iterations"],
                            "lps_per_s": 1000.0 / info64b["device_ms"] if info64b["device_ms"] > 0 else None,
                            "speedup_mixed_vs_fp64": info64b["device_ms"] / (total_ms / args.steps)},
@@ -388,6 +444,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch-lps", type=int, default=32,
                     help="family-3 batch members for the mixed+learned vs plain FP64 batch comparison (0: skip)")
+    ap.add_argument("--family2", action="store_true",
+                    help="add the family-2 staircase LP (m=200000) comparison (about 5 minutes)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

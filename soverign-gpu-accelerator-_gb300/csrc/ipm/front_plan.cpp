@@ -2,6 +2,7 @@
 #include "ipm/front_plan.hpp"
 
 #include <algorithm>
+#include <future>
 #include <numeric>
 #include <stdexcept>
 
@@ -324,8 +325,10 @@ void build_front_plan(const std::vector<LpView>& lps, const core::CSRMatrix& A, 
             perm0.resize(static_cast<size_t>(p.M));
             std::iota(perm0.begin(), perm0.end(), 0);
             p.ordering_used = 2;
+            auto natural = std::async(std::launch::async, [&]() { return factor_flops(A, perm0); });
             std::vector<Index> nd = nested_dissection_ordering(A);
-            if (factor_flops(A, nd) < factor_flops(A, perm0)) {
+            const double natural_flops = natural.get();
+            if (factor_flops(A, nd) < natural_flops) {
                 perm0.swap(nd);
                 p.ordering_used = 4;
             }

@@ -15,6 +15,8 @@
 // most `leaf` vertices, and parts whose best separator is larger than the smaller
 // side, are ordered by minimum degree on their induced graph.
 #include <algorithm>
+#include <atomic>
+#include <future>
 #include <numeric>
 #include <utility>
 
@@ -30,6 +32,8 @@ constexpr Index kUnset = -1;
 constexpr int kMinSideDiv = 5;      // each side of a separator holds at least 1/5 of the part
 constexpr Index kSlackNum = 11, kSlackDen = 10;   // a separator up to 10% wider wins when better balanced
 constexpr int kNoGain = 2;          // ball radii tried after the last narrower cut
+constexpr int kParallelDepth = 3;   // separators whose sides are dissected concurrently: 2^3 threads at most
+constexpr Index kParallelRows = 20000;
 
 // Minimum vertex cut through a band of vertices 0..nb-1 (adjacency inside the band
 // in CSR ptr/adj, both directions listed) between the vertices outside the band
@@ -114,71 +118,101 @@ private:
     }
 };
 
+// Per-thread scratch of the separator search.
+struct Scratch {
+    BandCut cut;
+    std::vector<Index> ptr, adj;
+    std::vector<char> src, snk, side;
+};
+
+// Parts are disjoint vertex sets, so the two sides of a separator are dissected
+// concurrently (large parts only). Every per-vertex array is written only for the
+// vertices of the part that owns them; labels of other parts may change while a
+// part reads them, but never to its own label, so labels are relaxed atomics.
 class Dissector {
 public:
-    Dissector(std::vector<std::vector<Index>>&& g, Index leaf) : g_(std::move(g)), leaf_(std::max<Index>(leaf, 8)) {
+    Dissector(std::vector<std::vector<Index>>&& g, Index leaf)
+        : g_(std::move(g)), leaf_(std::max<Index>(leaf, 8)), label_(g_.size()) {
         const Index m = static_cast<Index>(g_.size());
-        label_.assign(static_cast<size_t>(m), 0);
+        for (auto& l : label_) l.store(0, std::memory_order_relaxed);
         level_.assign(static_cast<size_t>(m), kUnset);
         loc_.assign(static_cast<size_t>(m), kUnset);
-        out_.reserve(static_cast<size_t>(m));
     }
 
     std::vector<Index> run() {
         const Index m = static_cast<Index>(g_.size());
         std::vector<Index> all(static_cast<size_t>(m));
         std::iota(all.begin(), all.end(), 0);
-        next_label_ = 1;
-        dissect(std::move(all), 0);
-        return std::move(out_);
+        next_label_.store(1);
+        Scratch sc;
+        return dissect(std::move(all), 0, 0, sc);
     }
 
 private:
     std::vector<std::vector<Index>> g_;
     Index leaf_;
-    std::vector<Index> label_, level_, loc_, out_;
-    Index next_label_ = 0;
-    BandCut cut_;
-    std::vector<Index> ptr_, adj_;
-    std::vector<char> src_, snk_, side_;
+    std::vector<std::atomic<Index>> label_;
+    std::vector<Index> level_, loc_;
+    std::atomic<Index> next_label_{0};
 
-    void dissect(std::vector<Index> V, Index lab) {
-        if (static_cast<Index>(V.size()) <= leaf_) { order_min_degree(V, lab); return; }
+    Index lab_of(Index v) const { return label_[v].load(std::memory_order_relaxed); }
+    void set_lab(Index v, Index l) { label_[v].store(l, std::memory_order_relaxed); }
+    Index fresh() { return next_label_.fetch_add(1, std::memory_order_relaxed); }
+
+    // Order of the part V (all labelled lab): its sub-parts, then its separator.
+    std::vector<Index> dissect(std::vector<Index> V, Index lab, int depth, Scratch& sc) {
+        std::vector<Index> out;
+        out.reserve(V.size());
+        if (static_cast<Index>(V.size()) <= leaf_) { order_min_degree(V, lab, out); return out; }
         std::vector<std::vector<Index>> comps = components(V, lab);
         if (comps.size() > 1) {
             V.clear();
             V.shrink_to_fit();
             for (auto& c : comps) {
-                const Index cl = label_[c[0]];
-                dissect(std::move(c), cl);
+                const Index cl = lab_of(c[0]);
+                const std::vector<Index> o = dissect(std::move(c), cl, depth, sc);
+                out.insert(out.end(), o.begin(), o.end());
             }
-            return;
+            return out;
         }
-        lab = label_[V[0]];   // the single component's fresh label
+        lab = lab_of(V[0]);   // the single component's fresh label
         std::vector<Index> S, A, B;
-        if (!separate(V, lab, S, A, B)) { order_min_degree(V, lab); return; }
+        if (!separate(V, lab, S, A, B, sc)) { order_min_degree(V, lab, out); return out; }
         V.clear();
         V.shrink_to_fit();
-        const Index la = next_label_++, lb = next_label_++, ls = next_label_++;
-        for (Index v : A) label_[v] = la;
-        for (Index v : B) label_[v] = lb;
-        for (Index v : S) label_[v] = ls;
-        dissect(std::move(A), la);
-        dissect(std::move(B), lb);
-        order_min_degree(S, ls);
+        const Index la = fresh(), lb = fresh(), ls = fresh();
+        for (Index v : A) set_lab(v, la);
+        for (Index v : B) set_lab(v, lb);
+        for (Index v : S) set_lab(v, ls);
+        std::vector<Index> oa, ob;
+        if (depth < kParallelDepth && static_cast<Index>(A.size() + B.size()) >= kParallelRows) {
+            auto fa = std::async(std::launch::async, [&]() {
+                Scratch s2;
+                return dissect(std::move(A), la, depth + 1, s2);
+            });
+            ob = dissect(std::move(B), lb, depth + 1, sc);
+            oa = fa.get();
+        } else {
+            oa = dissect(std::move(A), la, depth + 1, sc);
+            ob = dissect(std::move(B), lb, depth + 1, sc);
+        }
+        out.insert(out.end(), oa.begin(), oa.end());
+        out.insert(out.end(), ob.begin(), ob.end());
+        order_min_degree(S, ls, out);
+        return out;
     }
 
     // Connected components of the part; each gets a fresh label.
     std::vector<std::vector<Index>> components(const std::vector<Index>& V, Index lab) {
         std::vector<std::vector<Index>> comps;
         for (Index s : V) {
-            if (label_[s] != lab) continue;
-            const Index cl = next_label_++;
+            if (lab_of(s) != lab) continue;
+            const Index cl = fresh();
             std::vector<Index> c{s};
-            label_[s] = cl;
+            set_lab(s, cl);
             for (size_t h = 0; h < c.size(); ++h)
                 for (Index w : g_[c[h]])
-                    if (label_[w] == lab) { label_[w] = cl; c.push_back(w); }
+                    if (lab_of(w) == lab) { set_lab(w, cl); c.push_back(w); }
             comps.push_back(std::move(c));
         }
         return comps;
@@ -196,14 +230,14 @@ private:
             const Index u = order[h];
             if (static_cast<Index>(start.size()) - 1 < level_[u]) start.push_back(static_cast<Index>(h));
             for (Index w : g_[u])
-                if (label_[w] == lab && level_[w] == kUnset) { level_[w] = level_[u] + 1; order.push_back(w); }
+                if (lab_of(w) == lab && level_[w] == kUnset) { level_[w] = level_[u] + 1; order.push_back(w); }
         }
         start.push_back(static_cast<Index>(order.size()));
         for (Index v : order) level_[v] = kUnset;
     }
 
     bool separate(const std::vector<Index>& V, Index lab, std::vector<Index>& S, std::vector<Index>& A,
-                  std::vector<Index>& B) {
+                  std::vector<Index>& B, Scratch& sc) {
         const Index n = static_cast<Index>(V.size());
         std::vector<Index> order, start, order_v, start_v;
         // pseudo-peripheral pair: restart from a lowest-degree vertex of the last
@@ -253,7 +287,7 @@ private:
         int narrowest = -1;
         for (Index k = std::min(e, ev) / 2; k >= 0 && no_gain < kNoGain; --k) {
             Cand c;
-            const int rc = ball_cut(order, order_v, start[k + 1], start_v[k + 1], lab, c.a, c.s, c.b);
+            const int rc = ball_cut(order, order_v, start[k + 1], start_v[k + 1], lab, c.a, c.s, c.b, sc);
             if (rc < 0) continue;   // balls touch: shrink them
             if (static_cast<Index>(std::min(c.a.size(), c.b.size())) < min_side) break;
             if (narrowest < 0 || rc < narrowest) { narrowest = rc; no_gain = 0; } else ++no_gain;
@@ -280,7 +314,8 @@ private:
     // the minimum vertex cut between them through the rest of the part. Returns -1
     // when X and Y touch (no cut exists), else the cut size.
     int ball_cut(const std::vector<Index>& order_u, const std::vector<Index>& order_v, Index nx, Index ny,
-                  Index lab, std::vector<Index>& a_set, std::vector<Index>& s_set, std::vector<Index>& b_set) {
+                  Index lab, std::vector<Index>& a_set, std::vector<Index>& s_set, std::vector<Index>& b_set,
+                  Scratch& sc) {
         const Index n = static_cast<Index>(order_u.size());
         constexpr Index kX = -2, kY = -3;
         for (Index q = 0; q < nx; ++q) loc_[order_u[q]] = kX;
@@ -290,55 +325,55 @@ private:
         bool adjacent = false;
         std::vector<Index> band;
         for (Index v : order_u) {
-            if (loc_[v] == kY) { for (Index w : g_[v]) adjacent |= (label_[w] == lab && loc_[w] == kX); }
+            if (loc_[v] == kY) { for (Index w : g_[v]) adjacent |= (lab_of(w) == lab && loc_[w] == kX); }
             else if (loc_[v] != kX) band.push_back(v);
         }
         const Index nb = static_cast<Index>(band.size());
         const bool ok = !adjacent && nb > 0;
         if (ok) {
             for (Index q = 0; q < nb; ++q) loc_[band[q]] = q;
-            ptr_.assign(static_cast<size_t>(nb) + 1, 0);
-            adj_.clear();
-            src_.assign(static_cast<size_t>(nb), 0);
-            snk_.assign(static_cast<size_t>(nb), 0);
+            sc.ptr.assign(static_cast<size_t>(nb) + 1, 0);
+            sc.adj.clear();
+            sc.src.assign(static_cast<size_t>(nb), 0);
+            sc.snk.assign(static_cast<size_t>(nb), 0);
             for (Index q = 0; q < nb; ++q) {
                 for (Index w : g_[band[q]]) {
-                    if (label_[w] != lab) continue;
-                    if (loc_[w] == kX) src_[q] = 1;
-                    else if (loc_[w] == kY) snk_[q] = 1;
-                    else adj_.push_back(loc_[w]);
+                    if (lab_of(w) != lab) continue;
+                    if (loc_[w] == kX) sc.src[q] = 1;
+                    else if (loc_[w] == kY) sc.snk[q] = 1;
+                    else sc.adj.push_back(loc_[w]);
                 }
-                ptr_[q + 1] = static_cast<Index>(adj_.size());
+                sc.ptr[q + 1] = static_cast<Index>(sc.adj.size());
             }
-            cut_.run(nb, ptr_, adj_, src_, snk_, side_);
+            sc.cut.run(nb, sc.ptr, sc.adj, sc.src, sc.snk, sc.side);
             a_set.clear(); s_set.clear(); b_set.clear();
             for (Index v : order_u) {
                 const Index l = loc_[v];
                 if (l == kX) a_set.push_back(v);
                 else if (l == kY) b_set.push_back(v);
-                else (side_[l] == 0 ? a_set : side_[l] == 1 ? s_set : b_set).push_back(v);
+                else (sc.side[l] == 0 ? a_set : sc.side[l] == 1 ? s_set : b_set).push_back(v);
             }
         }
         for (Index v : order_u) loc_[v] = kUnset;
         return ok ? static_cast<int>(s_set.size()) : -1;
     }
 
-    // Minimum degree on the part's induced graph; appends the part to the order.
-    void order_min_degree(const std::vector<Index>& V, Index lab) {
+    // Minimum degree on the part's induced graph; appends the part to out.
+    void order_min_degree(const std::vector<Index>& V, Index lab, std::vector<Index>& out) {
         const Index n = static_cast<Index>(V.size());
         if (n == 0) return;
         for (Index q = 0; q < n; ++q) loc_[V[q]] = q;
         std::vector<std::vector<Index>> sub(static_cast<size_t>(n));
         for (Index q = 0; q < n; ++q) {
             for (Index w : g_[V[q]])
-                if (label_[w] == lab) sub[q].push_back(loc_[w]);
+                if (lab_of(w) == lab) sub[q].push_back(loc_[w]);
             std::sort(sub[q].begin(), sub[q].end());
         }
         for (Index q = 0; q < n; ++q) loc_[V[q]] = kUnset;
         const std::vector<Index> p = min_degree_order(std::move(sub));
         for (Index q : p) {
-            out_.push_back(V[q]);
-            label_[V[q]] = kUnset;
+            out.push_back(V[q]);
+            set_lab(V[q], kUnset);
         }
     }
 };

@@ -35,26 +35,35 @@ def highs(lp, method):
     return res, time.time() - t
 
 
+def record(out, case):
+    """Adds one case to the fixture under an exclusive lock (several runs may share it)."""
+    import fcntl
+    with open(out + ".lock", "w") as lk:
+        fcntl.flock(lk, fcntl.LOCK_EX)
+        cases = json.load(open(out))["cases"] if os.path.exists(out) else []
+        cases = [c for c in cases if c["name"] != case["name"]] + [case]
+        with open(out, "w") as f:
+            json.dump({"generator": "tests/golden/make_highs_objectives.py",
+                       "source": "scipy.optimize.linprog (HiGHS), tolerances 1e-10", "cases": cases}, f, indent=1)
+
+
 def main():
+    """Usage: make_highs_objectives.py [case names...] (default: all cases)."""
     out = os.path.join(HERE, "highs_large_objectives.json")
-    cases = json.load(open(out))["cases"] if os.path.exists(out) else []
-    done = {c["name"] for c in cases}
     todo = [("family1_0", lambda: sk.generate(1, 0), "highs-ipm"),
             ("staircase_13", lambda: sk.staircase(0xC2, 13), "highs-ipm"),
             ("family2_0", lambda: sk.generate(2, 0), "highs-ipm")]
+    want = set(sys.argv[1:]) or {t[0] for t in todo}
     for name, make, method in todo:
-        if name in done:
+        if name not in want:
             continue
         lp = make()
         res, secs = highs(lp, method)
         print(name, res.status, repr(res.fun), "%.1f s" % secs, flush=True)
         if res.status != 0:
             continue
-        cases.append({"name": name, "digest": digest(lp), "method": method, "objective": float(res.fun),
-                      "seconds": secs})
-        with open(out, "w") as f:
-            json.dump({"generator": "tests/golden/make_highs_objectives.py",
-                       "source": "scipy.optimize.linprog (HiGHS), tolerances 1e-10", "cases": cases}, f, indent=1)
+        record(out, {"name": name, "digest": digest(lp), "method": method, "objective": float(res.fun),
+                     "seconds": secs})
 
 
 if __name__ == "__main__":

@@ -32,3 +32,26 @@ def test_batch_members_full_certificate(gpu, oracle):
         meas = oracle.kkt_measures(lp, x, y, s)
         assert max(meas["rel_pinf"], meas["rel_dinf"], meas["rel_gap"]) <= TOL, (i, meas)
     solver.close()
+
+
+def test_staircase_rows_beyond_the_large_lp_threshold(gpu, oracle):
+    # 13 stages of the family-2 staircase (m = 52000 >= 50000): the automatic ordering
+    # picks the row order or nested dissection by flops; certificate, FP64 / mixed
+    # agreement and the HiGHS objective (third-party cross-check fixture)
+    import json
+    import os
+    sk = gpu
+    lp = sk.staircase(0xC2, 13)
+    info_m, x, y, s = sk.solve(lp, precision=1, start=sk.START_MEHROTRA)
+    assert info_m["status"] == 0, info_m
+    meas = oracle.kkt_measures(lp, x, y, s)
+    assert max(meas["rel_pinf"], meas["rel_dinf"], meas["rel_gap"]) <= TOL, meas
+    assert meas["min_x"] > 0 and meas["min_s"] > 0
+    info_d, *_ = sk.solve(lp, precision=0)
+    assert info_d["status"] == 0, info_d
+    assert abs(info_d["objective"] - info_m["objective"]) / (1 + abs(info_d["objective"])) <= TOL
+    fixture = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "highs_large_objectives.json")
+    with open(fixture) as f:
+        case = [c for c in json.load(f)["cases"] if c["name"] == "staircase_13"][0]
+    assert case["digest"]["nnz"] == lp.nnz and case["digest"]["m"] == lp.m
+    assert abs(info_m["objective"] - case["objective"]) / (1 + abs(case["objective"])) <= TOL
