@@ -168,7 +168,7 @@ def batch_comparison(sk, nlps):
     return out
 
 
-def family2_comparison(sk):
+def family2_comparison(sk, unit_start_arm=False):
     """Time-to-1e-8 on the family-2 staircase LP (m=200000, n=500000): mixed precision with
     the learned start (falling back to Mehrotra's start), mixed precision with the plain
     method's unit start, and the plain FP64 IPM. One solve per arm (each solve is tens of
@@ -189,6 +189,8 @@ def family2_comparison(sk):
            "objective_reference": "HiGHS (tests/golden/highs_large_objectives.json)" if ref is not None else None}
     arms = [("mixed_learned", sk.PREC_MIXED, sk.START_LEARNED), ("mixed_unit_start", sk.PREC_MIXED, sk.START_UNIT),
             ("plain_fp64", sk.PREC_FP64, sk.START_UNIT)]
+    if not unit_start_arm:
+        arms = [a for a in arms if a[0] != "mixed_unit_start"]
     for name, prec, start in arms:
         if start == sk.START_LEARNED and net is None:
             continue
@@ -294,7 +296,7 @@ def run_ours(args):
     prof64 = fp64.profile(fp32=False)
     fp64.close()
     batch = batch_comparison(sk, args.batch_lps) if args.batch_lps > 0 else None
-    family2 = family2_comparison(sk) if args.family2 else None
+    family2 = None if args.no_family2 else family2_comparison(sk, args.family2_unit_start)
     # end to end through the C ABI (host arrays in, host solution out)
     e2e_t = []
     for _ in range(max(1, args.steps)):
@@ -333,6 +335,11 @@ def run_ours(args):
     roof = upd_roof(prof64, "k_update<double> (FP64 frontal trailing update)", fp64_peak,
                     "nominal GB300 dense FP64 1.25 TFLOP/s (of nominal; MEASURED_PEAKS.json has no FP64 entry)",
                     "fp64")
+    # DRAM bytes of one captured launch (ncu, profiles/k_update_fp64_family1.md): 15.1 MB read, 0 written,
+    # against 59.5 MB of operand bytes for that launch's 465 tiles (panels and C are L2 hits)
+    roof["traffic"] = 15.1e6
+    roof["traffic_note"] = ("dram__bytes_read.sum + dram__bytes_write.sum of one captured launch (465 output "
+                            "tiles; operand bytes 59.5 MB), profiles/k_update_fp64_family1.md")
     rooflines = [roof,
                  upd_roof(prof, "k_update_tc (FP32 frontal trailing update, tcgen05 TF32 x3; flops counted once)",
                           bf16, "%s bf16 dense tensor peak (MEASURED_PEAKS.json bf16_tflops)" % src, "tensor"),
@@ -444,8 +451,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch-lps", type=int, default=32,
                     help="family-3 batch members for the mixed+learned vs plain FP64 batch comparison (0: skip)")
-    ap.add_argument("--family2", action="store_true",
-                    help="add the family-2 staircase LP (m=200000) comparison (about 5 minutes)")
+    ap.add_argument("--no-family2", action="store_true",
+                    help="skip the family-2 staircase LP (m=200000) comparison (about 3 minutes)")
+    ap.add_argument("--family2-unit-start", action="store_true",
+                    help="add a mixed-precision unit-start arm to the family-2 comparison")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
