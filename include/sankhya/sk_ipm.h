@@ -22,6 +22,8 @@ extern "C" {
 #define SK_ERR_ALLOC 5         /* device allocation failed (std::bad_alloc in src/gpu/vram_arena.cu:58-60) */
 #define SK_ERR_INTERNAL 6
 #define SK_ERR_TOO_LARGE 7     /* request exceeds a stated maximum size */
+#define SK_ERR_RANK_DEFICIENT 8 /* crossover: an artificial column stays in the basis ("Crossover failed:
+                                   Matrix is rank deficient", src/ipm/crossover.cu:455-457) */
 
 /* Solver status, numbered as the reference's simplex::SimplexStatus (src/simplex/primal.hpp:26-31). */
 #define SK_STATUS_OPTIMAL 0
@@ -235,6 +237,23 @@ int sk_dissection_ordering(int m, int n, const int* row_ptrs, const int* col_idx
  * Returns 16. No reference counterpart. */
 int sk_plan_stats(int m, int n, const int* col_ptrs, const int* row_idx, const double* vals, int ordering,
                   double* out, int cap);
+
+/* ---- Crossover (basis purification) ----
+ * Replaces: ipm::generate_crossover_basis (src/ipm/crossover.cuh:30-33, crossover.cu:322-460),
+ * same decisions. From a point x (n) with A x = b and lb <= x <= ub (lb / ub NULL: 0 / +inf),
+ * strictly interior columns are pivoted into the basis or moved to a bound, then the
+ * remaining artificial rows are filled. Outputs: basic (m) = the column of each basis
+ * row (>= n: artificial), status (n) = SK_BASIS_* per column, x_out (n, may be NULL) =
+ * x after the moves. Returns SK_OK; SK_ERR_NUMERICAL when a column has no admissible
+ * move ("Crossover failed: Invalid pivot encountered"); SK_ERR_RANK_DEFICIENT; and
+ * SK_ERR_TOO_LARGE for m > SK_CROSSOVER_MAX_ROWS (the basis inverse is a dense m x m
+ * FP64 matrix on the device). Outputs are filled in every case but SK_ERR_TOO_LARGE. */
+#define SK_CROSSOVER_MAX_ROWS 32768
+#define SK_BASIS_BASIC 0
+#define SK_BASIS_AT_LOWER 1
+#define SK_BASIS_AT_UPPER 2
+int sk_crossover(int m, int n, const int* col_ptrs, const int* row_idx, const double* vals, const double* lb,
+                 const double* ub, const double* x, int* basic, int* status, double* x_out);
 
 /* ---- Allocation-free small KKT solve ----
  * No counterpart in the reference. Solves (A diag(theta) A^T) dy = rhs in place

@@ -9,6 +9,7 @@
 
 #include "api/sk_error.hpp"
 #include "core/standard_form.hpp"
+#include "cuda/crossover.hpp"
 #include "cuda/device_ipm.hpp"
 #include "cuda/gnn.hpp"
 #include "cuda/kkt_engine.hpp"
@@ -648,3 +649,24 @@ int sk_solver_set_capture(sk_solver* h, double mu_threshold) {
 }
 
 }  // extern "C"
+
+extern "C" int sk_crossover(int m, int n, const int* col_ptrs, const int* row_idx, const double* vals,
+                            const double* lb, const double* ub, const double* x, int* basic, int* status,
+                            double* x_out) {
+    api::clear_error();
+    if (m <= 0 || n <= 0 || !col_ptrs || !row_idx || !vals || !x || !basic || !status) return SK_ERR_INVALID;
+    if (m > SK_CROSSOVER_MAX_ROWS) {
+        api::set_error("sk_crossover: m exceeds SK_CROSSOVER_MAX_ROWS");
+        return SK_ERR_TOO_LARGE;
+    }
+    try {
+        std::string msg;
+        const int rc = dev::crossover(m, n, col_ptrs, row_idx, vals, lb, ub, x, basic, status, x_out, &msg);
+        if (rc == dev::kCrossoverInvalidPivot) { api::set_error(msg); return SK_ERR_NUMERICAL; }
+        if (rc == dev::kCrossoverRankDeficient) { api::set_error(msg); return SK_ERR_RANK_DEFICIENT; }
+        if (rc == dev::kCrossoverTooLarge) return SK_ERR_TOO_LARGE;
+        return SK_OK;
+    } catch (...) {
+        return api::status_of_current_exception();
+    }
+}

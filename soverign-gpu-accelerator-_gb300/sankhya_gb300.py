@@ -77,6 +77,8 @@ def _declare(L):
     L.sk_dissection_ordering.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _i32p]
     L.sk_plan_stats.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p, C.c_int, _f64p, C.c_int]
     L.sk_compute_symbolic.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _i32p, _i32p, _i32p, _i32p, _i32p, C.c_int]
+    if hasattr(L, "sk_crossover"):
+        L.sk_crossover.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p, vp, vp, _f64p, _i32p, _i32p, vp]
     if hasattr(L, "sk_ipm_solve_csc"):
         L.sk_ipm_solve_csc.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p, _f64p, _f64p, C.POINTER(Options),
                                        vp, vp, vp, C.POINTER(Info)]
@@ -256,6 +258,26 @@ def fill_ordering(m, n, rp, ci):
     P = np.zeros(m, dtype=np.int32)
     check(lib().sk_fill_ordering(m, n, rp, ci, P), "sk_fill_ordering")
     return P
+
+
+BASIS_BASIC, BASIS_AT_LOWER, BASIS_AT_UPPER = 0, 1, 2
+ERR_NUMERICAL, ERR_RANK_DEFICIENT = 3, 8
+
+
+def crossover(lp, x, lb=None, ub=None):
+    """Basis purification from the point x: (rc, basic (m), status (n), x after the moves).
+    rc is SK_OK, SK_ERR_NUMERICAL (invalid pivot) or SK_ERR_RANK_DEFICIENT; other codes raise."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    basic = np.zeros(lp.m, dtype=np.int32)
+    status = np.zeros(lp.n, dtype=np.int32)
+    xo = np.zeros(lp.n, dtype=np.float64)
+    lbv = None if lb is None else np.ascontiguousarray(lb, dtype=np.float64)
+    ubv = None if ub is None else np.ascontiguousarray(ub, dtype=np.float64)
+    rc = lib().sk_crossover(lp.m, lp.n, lp.col_ptrs, lp.row_idx, lp.vals, _ptr(lbv) if lbv is not None else None,
+                            _ptr(ubv) if ubv is not None else None, x, basic, status, _ptr(xo))
+    if rc not in (0, ERR_NUMERICAL, ERR_RANK_DEFICIENT):
+        check(rc, "sk_crossover")
+    return rc, basic, status, xo
 
 
 def dissection_ordering(m, n, rp, ci):

@@ -57,6 +57,7 @@ def main():
     for name, make, method in todo:
         if name not in want:
             continue
+        method = os.environ.get("HIGHS_METHOD", method)
         lp = make()
         res, secs = highs(lp, method)
         print(name, res.status, repr(res.fun), "%.1f s" % secs, flush=True)
