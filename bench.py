@@ -202,6 +202,9 @@ def family2_comparison(sk, unit_start_arm=False):
         s.run()
         info, *_ = s.result(0, want_vectors=False)
         t2 = time.perf_counter()
+        if name == "mixed_learned":
+            # instrumented replay of one FP32 factorisation at the final iterate (not part of the solve time)
+            out["profile_fp32"] = s.profile(fp32=True)
         s.close()
         arm = {"status": info["status"], "iterations": info["iterations"], "device_ms": info["device_ms"],
                "analysis_s": t1 - t0, "wall_s": t2 - t0, "objective": info["objective"],
@@ -222,6 +225,111 @@ def family2_comparison(sk, unit_start_arm=False):
             out[name]["speedup_device_vs_plain_fp64"] = base["device_ms"] / out[name]["device_ms"]
             out[name]["speedup_wall_vs_plain_fp64"] = base["wall_s"] / out[name]["wall_s"]
     return out
+
+
+def _block_diag_csr(parts, col_offsets):
+    """Concatenates per-LP CSR arrays (row_ptrs, col_idx, vals) into the CSR of the
+    block-diagonal matrix, shifting each block's columns by its offset."""
+    import numpy as np
+    rps, cis, vs, base = [], [], [], 0
+    for (rp, ci, v), co in zip(parts, col_offsets):
+        rps.append(rp[:-1].astype(np.int64) + base)
+        cis.append(ci.astype(np.int64) + co)
+        vs.append(v)
+        base += len(v)
+    rps.append(np.array([base], dtype=np.int64))
+    if base >= 2 ** 31:
+        raise ValueError("batch too large for int32 indices")
+    return (np.concatenate(rps).astype(np.int32), np.concatenate(cis).astype(np.int32),
+            np.ascontiguousarray(np.concatenate(vs)))
+
+
+def spmv_rooflines(sk, hbm, src, nlps=512, warm=3, reps=10):
+    """HBM roofline of the solver's SpMV kernel (autotuned plan, sk_spmv_plan_*) for
+    y = A x and y = A^T x on the block-diagonal matrix of the family-3 batch (512
+    LPs: 61 M nonzeros, 0.73 GB of CSR indices and values per product, several times
+    the 129 MB L2). A 256 MB buffer is written before each timed launch; each launch
+    sits between CUDA events on the launching stream (torch's current stream).
+    Algorithmic bytes: 12 nnz + 4 (rows + 1) + 8 cols + 8 rows (CSR read once, x read
+    once, y written once). The same product through torch's CSR matmul (cuSPARSE)
+    is timed the same way for comparison, and the two results are compared."""
+    import numpy as np
+    import torch
+    lps = [sk.generate(3, k) for k in range(nlps)]
+    roff = np.cumsum([0] + [lp.m for lp in lps])[:-1]
+    coff = np.cumsum([0] + [lp.n for lp in lps])[:-1]
+    M, N = sum(lp.m for lp in lps), sum(lp.n for lp in lps)
+    mats = [("A x", M, N, _block_diag_csr([lp.csr() for lp in lps], coff)),
+            ("A^T y", N, M, _block_diag_csr([(lp.col_ptrs, lp.row_idx, lp.vals) for lp in lps], roff))]
+    del lps
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    out = []
+    for name, rows, cols, (rp, ci, v) in mats:
+        nnz = len(v)
+        d_rp, d_ci, d_v = (torch.from_numpy(a).cuda() for a in (rp, ci, v))
+        x = torch.randn(cols, dtype=torch.float64, device="cuda")
+        y = torch.zeros(rows, dtype=torch.float64, device="cuda")
+        plan = sk.SpmvPlan(rows, cols, nnz, d_rp.data_ptr(), d_ci.data_ptr(), d_v.data_ptr(),
+                           stream=stream.cuda_stream)
+        tune = plan.info()
+
+        def timed(fn):
+            for _ in range(warm):
+                fn()
+            evs = []
+            for _ in range(reps):
+                flush.zero_()
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                fn()
+                b.record(stream)
+                evs.append((a, b))
+            torch.cuda.synchronize()
+            return statistics.mean(a.elapsed_time(b) for a, b in evs)
+
+        ms = timed(lambda: plan.execute(x.data_ptr(), y.data_ptr(), stream=stream.cuda_stream))
+        lib_ms, max_rel = None, None
+        try:
+            A = torch.sparse_csr_tensor(d_rp, d_ci, d_v, size=(rows, cols))
+            xc = x.view(-1, 1)
+            z = A.matmul(xc)
+            lib_ms = timed(lambda: A.matmul(xc))
+            torch.cuda.synchronize()
+            scale = torch.sparse_csr_tensor(d_rp, d_ci, d_v.abs(), size=(rows, cols)).matmul(x.abs().view(-1, 1))
+            max_rel = float(((z.view(-1) - y).abs() / (1.0 + scale.view(-1))).max())
+        except Exception as e:      # torch build without CUDA CSR matmul: comparison left out
+            lib_ms = "unavailable: %s" % type(e).__name__
+        nbytes = 12.0 * nnz + 4.0 * (rows + 1) + 8.0 * cols + 8.0 * rows
+        a = nbytes / (ms / 1000.0) / 1e9
+        out.append({"kernel": "k_spmv<%d, EpiAxpby> (%s, family-3 batch of %d LPs as one block-diagonal matrix)"
+                              % (tune["group"], name, nlps),
+                    "bound": "hbm", "achieved": a, "peak": hbm, "unit": "GB/s", "frac": a / hbm,
+                    "peak_source": "%s copy bandwidth (MEASURED_PEAKS.json hbm_gbs)" % src, "traffic": None,
+                    "rows": rows, "cols": cols, "nnz": nnz, "algorithmic_bytes": nbytes, "ms_per_launch": ms,
+                    "launches_timed": reps, "l2": "256 MB written before each launch",
+                    "lanes_per_row": tune["group"], "rule_lanes_per_row": tune["heuristic_group"],
+                    "autotune_ms_per_width": tune["ms_per_group"],
+                    "cusparse_ms_per_launch": lib_ms, "max_rel_diff_vs_cusparse": max_rel})
+        plan.close()
+        del d_rp, d_ci, d_v, x, y
+    del flush
+    torch.cuda.empty_cache()
+    return out
+
+
+def assembly_roofline(prof, hbm, src, workload, note):
+    """Assembly class of an instrumented replay (sk_solver_profile): algorithmic bytes of
+    one assembly over its event-timed duration (both assembly kernels)."""
+    a_ms, a_b = prof["assembly"]["ms"], prof.get("assembly_bytes")
+    if not a_b or a_ms <= 0:
+        return None
+    a = a_b / (a_ms / 1000.0) / 1e9
+    return {"kernel": "k_asm_diag_* + k_asm_slots_sparse / k_asm_cols_dense (assembly of D A Theta A^T D + "
+                      "delta I, %s)" % workload,
+            "bound": "hbm", "achieved": a, "peak": hbm, "unit": "GB/s", "frac": a / hbm,
+            "peak_source": "%s copy bandwidth (MEASURED_PEAKS.json hbm_gbs)" % src, "traffic": None,
+            "ms_total": a_ms, "launches": prof["assembly"]["launches"], "algorithmic_bytes": a_b, "note": note}
 
 
 def dist_setup(args):
@@ -347,6 +455,13 @@ def run_ours(args):
                           "%s bf16 dense tensor peak (MEASURED_PEAKS.json bf16_tflops)" % src, "tensor"),
                  solve_roof(prof, "k_fwd_tasks<float> + k_bwd_tasks<float> (one triangular solve pair)", 4),
                  solve_roof(prof64, "k_fwd_tasks<double> + k_bwd_tasks<double> (one triangular solve pair)", 8)]
+    rooflines.append(assembly_roofline(prof, hbm, src, "family-1 LP, FP32 fronts", note))
+    if family2 is not None and "profile_fp32" in family2:
+        rooflines.append(assembly_roofline(family2.pop("profile_fp32"), hbm, src,
+                                           "family-2 staircase LP, FP32 fronts", note))
+    if args.spmv_lps > 0:
+        rooflines.extend(spmv_rooflines(sk, hbm, src, nlps=args.spmv_lps))
+    rooflines = [r for r in rooflines if r is not None]
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(sk, cores=1)
@@ -451,6 +566,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch-lps", type=int, default=32,
                     help="family-3 batch members for the mixed+learned vs plain FP64 batch comparison (0: skip)")
+    ap.add_argument("--spmv-lps", type=int, default=512,
+                    help="family-3 members in the block-diagonal matrix of the SpMV roofline (0: skip)")
     ap.add_argument("--no-family2", action="store_true",
                     help="skip the family-2 staircase LP (m=200000) comparison (about 3 minutes)")
     ap.add_argument("--family2-unit-start", action="store_true",

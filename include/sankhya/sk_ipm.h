@@ -148,9 +148,12 @@ void sk_solver_destroy(sk_solver* h);
  * c = 0 assembly, 1 potrf, 2 trsm, 3 update, 4 extend-add, 5 forward solve,
  * 6 backward solve; out[14] = algorithmic flops of the update launches, out[15] =
  * bytes the update launches must move at least (each input tile read once, each
- * output tile read and written once). fp32: 0 = FP64 fronts, 1 = FP32 fronts with
- * tensor-core (tcgen05) updates, 2 = FP32 fronts with SIMT updates. Returns the
- * number of values written (16). No reference counterpart. */
+ * output tile read and written once); with cap >= 17, out[16] = algorithmic bytes
+ * of the assembly launches (A or the Khatri-Rao map read once, Theta read once,
+ * each normal-matrix entry written once, the diagonal and D written once).
+ * fp32: 0 = FP64 fronts, 1 = FP32 fronts with tensor-core (tcgen05) updates, 2 =
+ * FP32 fronts with SIMT updates. Returns the number of values written (16 or 17).
+ * No reference counterpart. */
 int sk_solver_profile(sk_solver* h, int fp32, double* out, int cap);
 
 /* ---- Learned start: bipartite row / column message-passing network ----
@@ -273,11 +276,53 @@ int sk_crossover(int m, int n, const int* col_ptrs, const int* row_idx, const do
 int sk_kkt_solve_noalloc(int m, int n, const int* d_row_ptrs, const int* d_col_idx, const double* d_vals,
                          const double* d_theta, double* d_rhs, double tol, void* stream);
 
+/* ---- Presolve: Ruiz equilibration of a model (host) ----
+ * Replaces: presolve::apply_ruiz_scaling(core::Model&, int max_iterations)
+ * (src/presolve/scaling.hpp:25, src/presolve/scaling.cpp:18-146), with the
+ * same arithmetic (bit-identical results). Up to max_iterations passes (the
+ * reference's default is 10) scale A's rows, then its columns, by
+ * 1/sqrt(largest |entry|), stopping once all those maxima were within 1e-4 of 1;
+ * columns with integer_cols[j] != 0 are never scaled (integer_cols may be NULL:
+ * all continuous). vals (CSC, in place) is scaled; row_scale (m) and col_scale
+ * (n) hold the model's scale vectors on entry (ones for a model not scaled
+ * before) and the accumulated ones on return; then b <- row_scale .* b,
+ * c <- col_scale .* c, finite lb / ub <- bound ./ col_scale (b, c, lb, ub may be
+ * NULL). Host only: needs no device. */
+int sk_presolve_ruiz(int m, int n, const int* col_ptrs, const int* row_idx, double* vals, double* b, double* c,
+                     double* lb, double* ub, const unsigned char* integer_cols, int max_iterations,
+                     double* row_scale, double* col_scale);
+
 /* ---- Device kernels exposed for parity tests (device pointers, stream may be NULL) ---- */
 /* y = alpha * A x + beta * y for CSR A (rows x ?). Replaces cusparseSpMV CSR FP64
  * (src/ipm/mehrotra_device.cu:512,603,635,936). */
 int sk_spmv_csr(int rows, const int* d_row_ptrs, const int* d_col_idx, const double* d_vals,
                 const double* d_x, double alpha, double beta, double* d_y, void* stream);
+
+/* ---- Autotuned SpMV plans ----
+ * Replaces the reference's descriptor-based cuSPARSE SpMV (cusparseCreateCsr at
+ * src/ipm/mehrotra_device.cu:424-428, cusparseSpMV_bufferSize + cusparseSpMV at
+ * :508-530 and :596-624) for one CSR matrix kept on the device by the caller (rows x cols,
+ * nnz entries, int32 indices, FP64 values; the arrays must outlive the plan).
+ * sk_spmv_plan_create times the project's vector CSR kernel for 2, 4, 8, 16 and
+ * 32 lanes per row on this matrix (it allocates and frees its own x / y scratch
+ * and synchronises `stream`) and keeps the fastest; the width is remembered for
+ * the process under (device, rows, cols, nnz), so later plans and solvers on the
+ * same shape reuse it. sk_spmv_plan_execute computes y = alpha A x + beta y
+ * asynchronously on `stream` (NULL = legacy default stream). sk_spmv_plan_info
+ * reports the width in use, the row-length rule's width, and the fastest timed
+ * launch of each width in milliseconds (ms_per_group: 5 entries in the order
+ * 2, 4, 8, 16, 32; all zero if the width came from an earlier plan). */
+typedef struct sk_spmv_plan sk_spmv_plan;
+int sk_spmv_plan_create(int rows, int cols, long long nnz, const int* d_row_ptrs, const int* d_col_idx,
+                        const double* d_vals, void* stream, sk_spmv_plan** out);
+int sk_spmv_plan_execute(const sk_spmv_plan* plan, const double* d_x, double alpha, double beta, double* d_y,
+                         void* stream);
+int sk_spmv_plan_info(const sk_spmv_plan* plan, int* group, int* heuristic_group, double* ms_per_group);
+/* Overrides the plan's width (2, 4, 8, 16 or 32 lanes per row; other values:
+ * SK_ERR_INVALID). Every width computes the same products; only the order of
+ * the additions within a row differs. */
+int sk_spmv_plan_set_group(sk_spmv_plan* plan, int group);
+void sk_spmv_plan_destroy(sk_spmv_plan* plan);
 
 /* ---- Model input ----
  * Replaces: parsers::read_mps (src/parsers/mps_reader.hpp:20) and the seeded

@@ -9,6 +9,7 @@
 #include "core/sparse_matrix.hpp"
 #include "ipm/symbolic.hpp"
 #include "numerics/sparse_lu.hpp"
+#include "presolve/scaling.hpp"
 #include "simplex/phase1.hpp"
 #include "verifier/certificate.hpp"
 
@@ -96,6 +97,45 @@ int ref_verify_optimal(int m, int n, const int* cp, const int* ri, const double*
         core::Model model = model_of(m, n, cp, ri, va, b, c);
         std::vector<Float> xv(x, x + n), pv(pi, pi + m);
         return verifier::verify_optimal(model, xv, pv) ? 1 : 0;
+    } catch (...) {
+        return -1;
+    }
+}
+
+// The reference's presolve::apply_ruiz_scaling on the model built from the CSC
+// arrays (bounds and integer flags included); writes back the scaled CSC values,
+// b, c, lb, ub and the scale vectors. Returns -2 if the reference's CSC order
+// differs from the input's (rows must be sorted within each column).
+int ref_ruiz_scaling(int m, int n, const int* cp, const int* ri, const double* va, const double* b, const double* c,
+                     const double* lb, const double* ub, const unsigned char* is_int, int max_iter,
+                     double* vals_out, double* b_out, double* c_out, double* lb_out, double* ub_out,
+                     double* row_scale, double* col_scale) {
+    try {
+        core::Model model;
+        for (int j = 0; j < n; ++j)
+            model.add_variable(c[j], lb[j], ub[j], is_int[j] ? VariableType::Integer : VariableType::Continuous);
+        std::vector<std::vector<Index>> rc(static_cast<size_t>(m));
+        std::vector<std::vector<Float>> rv(static_cast<size_t>(m));
+        for (int j = 0; j < n; ++j)
+            for (int k = cp[j]; k < cp[j + 1]; ++k) {
+                rc[static_cast<size_t>(ri[k])].push_back(j);
+                rv[static_cast<size_t>(ri[k])].push_back(va[k]);
+            }
+        for (int i = 0; i < m; ++i) model.add_constraint(rc[static_cast<size_t>(i)], rv[static_cast<size_t>(i)], b[i]);
+        model.finalize();
+        for (int j = 0; j <= n; ++j)
+            if (model.A.col_ptrs[static_cast<size_t>(j)] != cp[j]) return -2;
+        for (int k = 0; k < cp[n]; ++k)
+            if (model.A.row_indices[static_cast<size_t>(k)] != ri[k]) return -2;
+        presolve::apply_ruiz_scaling(model, max_iter);
+        std::memcpy(vals_out, model.A.values.data(), sizeof(double) * static_cast<size_t>(cp[n]));
+        std::memcpy(b_out, model.rhs.data(), sizeof(double) * static_cast<size_t>(m));
+        std::memcpy(c_out, model.obj.data(), sizeof(double) * static_cast<size_t>(n));
+        std::memcpy(lb_out, model.lb.data(), sizeof(double) * static_cast<size_t>(n));
+        std::memcpy(ub_out, model.ub.data(), sizeof(double) * static_cast<size_t>(n));
+        std::memcpy(row_scale, model.row_scale.data(), sizeof(double) * static_cast<size_t>(m));
+        std::memcpy(col_scale, model.col_scale.data(), sizeof(double) * static_cast<size_t>(n));
+        return 0;
     } catch (...) {
         return -1;
     }

@@ -75,6 +75,10 @@ def reference():
         L.ref_simplex_solve.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p, _f64p, _f64p, _f64p,
                                         C.POINTER(C.c_double)]
         L.ref_verify_optimal.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p, _f64p, _f64p, _f64p, _f64p]
+        if hasattr(L, "ref_ruiz_scaling"):
+            _u8p = np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")
+            L.ref_ruiz_scaling.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p, _f64p, _f64p, _f64p, _f64p, _u8p,
+                                           C.c_int] + [_f64p] * 7
         _r = L
     return _r
 
@@ -149,3 +153,17 @@ def ref_simplex(lp):
     obj = C.c_double()
     st = reference().ref_simplex_solve(lp.m, lp.n, lp.col_ptrs, lp.row_idx, lp.vals, lp.b, lp.c, x, C.byref(obj))
     return st, obj.value, x
+
+
+def ref_ruiz(lp, lb, ub, integer, max_iter=10):
+    """The reference's presolve::apply_ruiz_scaling on the LP with bounds and integer
+    flags: dict(vals, b, c, lb, ub, row_scale, col_scale)."""
+    L = reference()
+    out = {k: np.zeros(n) for k, n in (("vals", lp.nnz), ("b", lp.m), ("c", lp.n), ("lb", lp.n), ("ub", lp.n),
+                                        ("row_scale", lp.m), ("col_scale", lp.n))}
+    rc = L.ref_ruiz_scaling(lp.m, lp.n, lp.col_ptrs, lp.row_idx, lp.vals, lp.b, lp.c,
+                            np.ascontiguousarray(lb, dtype=np.float64), np.ascontiguousarray(ub, dtype=np.float64),
+                            np.ascontiguousarray(integer, dtype=np.uint8), max_iter, out["vals"], out["b"], out["c"],
+                            out["lb"], out["ub"], out["row_scale"], out["col_scale"])
+    assert rc == 0, rc
+    return out

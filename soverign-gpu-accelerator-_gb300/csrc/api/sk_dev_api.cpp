@@ -2,6 +2,7 @@
 // persistent IPM solves, the KKT engine and the SpMV kernel.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -9,6 +10,7 @@
 
 #include "api/sk_error.hpp"
 #include "core/standard_form.hpp"
+#include "cuda/autotune.hpp"
 #include "cuda/crossover.hpp"
 #include "cuda/device_ipm.hpp"
 #include "cuda/gnn.hpp"
@@ -199,8 +201,11 @@ int sk_solver_profile(sk_solver* h, int fp32, double* out, int cap) {
     api::clear_error();
     if (!h || !out || cap < 16) return -SK_ERR_INVALID;
     try {
-        h->ipm->profile(fp32 != 0, fp32 == 1, out);
-        return 16;
+        double all[17];
+        h->ipm->profile(fp32 != 0, fp32 == 1, all);
+        const int nv = cap >= 17 ? 17 : 16;
+        for (int q = 0; q < nv; ++q) out[q] = all[q];
+        return nv;
     } catch (...) {
         return -api::status_of_current_exception();
     }
@@ -407,6 +412,92 @@ int sk_spmv_csr(int rows, const int* d_row_ptrs, const int* d_col_idx, const dou
     }
 }
 
+struct sk_spmv_plan {
+    int rows = 0, cols = 0;
+    long long nnz = 0;
+    const int* rp = nullptr;
+    const int* ci = nullptr;
+    const double* v = nullptr;
+    dev::SpmvTuning tune;
+};
+
+int sk_spmv_plan_create(int rows, int cols, long long nnz, const int* d_row_ptrs, const int* d_col_idx,
+                        const double* d_vals, void* stream, sk_spmv_plan** out) {
+    api::clear_error();
+    if (!out || rows < 0 || cols < 0 || nnz < 0 || !d_row_ptrs || (nnz > 0 && (!d_col_idx || !d_vals)))
+        return SK_ERR_INVALID;
+    *out = nullptr;
+    double* xs = nullptr;
+    double* ys = nullptr;
+    try {
+        int ndev = 0;
+        if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+            throw api::sk_exception(SK_ERR_NO_DEVICE, "no CUDA device visible");
+        std::unique_ptr<sk_spmv_plan> p(new sk_spmv_plan);
+        p->rows = rows;
+        p->cols = cols;
+        p->nnz = nnz;
+        p->rp = d_row_ptrs;
+        p->ci = d_col_idx;
+        p->v = d_vals;
+        auto st = static_cast<cudaStream_t>(stream);
+        const int cached = dev::spmv_tuned_group(rows, cols, nnz);
+        p->tune.heuristic = dev::spmv_heuristic_group(nnz, rows);
+        p->tune.group = cached;
+        if (rows > 0 && nnz > 0) {
+            SK_CUDA(cudaMalloc(&xs, sizeof(double) * std::max(1, cols)));
+            SK_CUDA(cudaMalloc(&ys, sizeof(double) * rows));
+            SK_CUDA(cudaMemsetAsync(xs, 0, sizeof(double) * std::max(1, cols), st));
+            p->tune = dev::spmv_tune(rows, cols, nnz, d_row_ptrs, d_col_idx, d_vals, xs, ys, st);
+            SK_CUDA(cudaFree(xs));
+            xs = nullptr;
+            SK_CUDA(cudaFree(ys));
+            ys = nullptr;
+        }
+        *out = p.release();
+        return SK_OK;
+    } catch (...) {
+        if (xs) cudaFree(xs);
+        if (ys) cudaFree(ys);
+        return api::status_of_current_exception();
+    }
+}
+
+int sk_spmv_plan_execute(const sk_spmv_plan* p, const double* d_x, double alpha, double beta, double* d_y,
+                         void* stream) {
+    api::clear_error();
+    if (!p || (p->rows > 0 && (!d_x || !d_y))) return SK_ERR_INVALID;
+    try {
+        dev::spmv_axpby(p->rows, p->tune.group, p->rp, p->ci, p->v, d_x, alpha, beta, d_y,
+                        static_cast<cudaStream_t>(stream));
+        return SK_OK;
+    } catch (...) {
+        return api::status_of_current_exception();
+    }
+}
+
+int sk_spmv_plan_info(const sk_spmv_plan* p, int* group, int* heuristic_group, double* ms_per_group) {
+    api::clear_error();
+    if (!p) return SK_ERR_INVALID;
+    if (group) *group = p->tune.group;
+    if (heuristic_group) *heuristic_group = p->tune.heuristic;
+    if (ms_per_group)
+        for (int k = 0; k < dev::kSpmvNumGroups; ++k) ms_per_group[k] = p->tune.from_cache ? 0.0 : p->tune.ms[k];
+    return SK_OK;
+}
+
+int sk_spmv_plan_set_group(sk_spmv_plan* p, int group) {
+    api::clear_error();
+    if (!p) return SK_ERR_INVALID;
+    for (int k = 0; k < dev::kSpmvNumGroups; ++k)
+        if (dev::kSpmvGroups[k] == group) {
+            p->tune.group = group;
+            return SK_OK;
+        }
+    return SK_ERR_INVALID;
+}
+
+void sk_spmv_plan_destroy(sk_spmv_plan* p) { delete p; }
 
 int sk_gnn_create(unsigned long long seed, sk_gnn** out) {
     api::clear_error();

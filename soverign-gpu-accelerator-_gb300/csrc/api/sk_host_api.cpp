@@ -11,6 +11,7 @@
 #include "ipm/front_plan.hpp"
 #include "ipm/symbolic.hpp"
 #include "parsers/mps_reader.hpp"
+#include "presolve/scaling.hpp"
 #include "core/standard_form.hpp"
 #include "sankhya/sk_ipm.h"
 
@@ -222,6 +223,29 @@ int sk_lp_bounds(const sk_lp* lp, const double** lb, const double** ub) {
 }
 
 void sk_lp_free(sk_lp* lp) { delete lp; }
+
+int sk_presolve_ruiz(int m, int n, const int* col_ptrs, const int* row_idx, double* vals, double* b, double* c,
+                     double* lb, double* ub, const unsigned char* integer_cols, int max_iterations,
+                     double* row_scale, double* col_scale) {
+    sankhya::api::clear_error();
+    if (m < 0 || n < 0 || max_iterations < 0) return SK_ERR_INVALID;
+    if (m > 0 && n > 0 && (!col_ptrs || !row_idx || !vals || !row_scale || !col_scale)) return SK_ERR_INVALID;
+    try {
+        if (m > 0 && n > 0) {
+            if (col_ptrs[0] != 0) throw std::invalid_argument("col_ptrs[0] must be 0");
+            for (int j = 0; j < n; ++j)
+                if (col_ptrs[j + 1] < col_ptrs[j]) throw std::invalid_argument("col_ptrs must not decrease");
+            for (int q = 0; q < col_ptrs[n]; ++q)
+                if (row_idx[q] < 0 || row_idx[q] >= m) throw std::invalid_argument("row index out of range");
+        }
+        return sankhya::presolve::ruiz_scale_csc(m, n, col_ptrs, row_idx, vals, b, c, lb, ub, integer_cols,
+                                                 max_iterations, row_scale, col_scale) >= 0
+                   ? SK_OK
+                   : SK_ERR_INTERNAL;
+    } catch (...) {
+        return sankhya::api::status_of_current_exception();
+    }
+}
 
 int sk_compute_amd_ordering(int m, int n, const int* row_ptrs, const int* col_idx, int* P) {
     api::clear_error();

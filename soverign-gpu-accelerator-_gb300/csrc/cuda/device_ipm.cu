@@ -19,7 +19,9 @@
 // deterministic per LP, and in mixed precision the factor is FP32 until mu drops
 // below the switch threshold or an FP32 solve misses its tolerance.
 #include "cuda/device_ipm.hpp"
+#include "cuda/autotune.hpp"
 #include "cuda/gnn.hpp"
+#include "cuda/spmv.cuh"
 
 #include <algorithm>
 #include <chrono>
@@ -52,49 +54,9 @@ enum { OP_SUM = 0, OP_MAX = 1, OP_MIN = 2 };
 inline int nblk(int64_t n, int t = 256) { return static_cast<int>((n + t - 1) / t); }
 
 // ---------------------------------------------------------------- SpMV
+// k_spmv / spmv() / EpiAxpby: spmv.cuh; the lane-group width of A and A^T is
+// chosen at set-up by spmv_tune() (autotune.hpp).
 
-template <int G, class Epi>
-__global__ void __launch_bounds__(256) k_spmv(int rows, const int* __restrict__ rp, const int* __restrict__ ci,
-                                              const double* __restrict__ v, const double* __restrict__ x, Epi epi) {
-    const int gid = blockIdx.x * blockDim.x + threadIdx.x;
-    const int row = gid / G, lane = gid % G;
-    const bool valid = row < rows;
-    double acc = 0.0;
-    if (valid)
-        for (int q = rp[row] + lane; q < rp[row + 1]; q += G) acc += v[q] * x[ci[q]];
-#pragma unroll
-    for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, G);
-    if (valid && lane == 0) epi(row, acc);
-}
-
-template <class Epi>
-void spmv(int rows, int group, const int* rp, const int* ci, const double* v, const double* x, Epi epi,
-          cudaStream_t st) {
-    if (rows <= 0) return;
-    const int64_t threads = static_cast<int64_t>(rows) * group;
-    switch (group) {
-    case 2: k_spmv<2><<<nblk(threads), 256, 0, st>>>(rows, rp, ci, v, x, epi); break;
-    case 4: k_spmv<4><<<nblk(threads), 256, 0, st>>>(rows, rp, ci, v, x, epi); break;
-    case 8: k_spmv<8><<<nblk(threads), 256, 0, st>>>(rows, rp, ci, v, x, epi); break;
-    case 16: k_spmv<16><<<nblk(threads), 256, 0, st>>>(rows, rp, ci, v, x, epi); break;
-    default: k_spmv<32><<<nblk(threads), 256, 0, st>>>(rows, rp, ci, v, x, epi); break;
-    }
-}
-
-int pick_group(int64_t nnz, int rows) {
-    const double avg = rows > 0 ? static_cast<double>(nnz) / rows : 0.0;
-    if (avg <= 3) return 2;
-    if (avg <= 6) return 4;
-    if (avg <= 12) return 8;
-    if (avg <= 24) return 16;
-    return 32;
-}
-
-struct EpiAxpby {
-    double alpha, beta;
-    double* y;
-    __device__ void operator()(int i, double d) const { y[i] = beta == 0.0 ? alpha * d : alpha * d + beta * y[i]; }
-};
 struct EpiSub {          // out = d - a
     const double* a;
     double* out;
@@ -444,7 +406,8 @@ struct DeviceIPM::Impl {
     double solve_ms = 0.0, device_ms = 0.0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::vector<double> hx0, hy0, hs0;      // user start (scaled)
-    int ga = 4, gt = 4;
+    int ga = 4, gt = 4;                 // SpMV lanes per row of A and A^T (autotuned at set-up)
+    SpmvTuning tune_a, tune_t;
     Gnn* gnn = nullptr;                     // network of SK_START_LEARNED (not owned)
     double capture_mu = 0.0;                // iterate capture for training targets
     std::vector<char> captured;
@@ -634,8 +597,17 @@ DeviceIPM::DeviceIPM(const std::vector<ipm::LpView>& lps, const std::vector<cons
     upload(I.row_lp, h_row_lp, I.st); upload(I.col_lp, h_col_lp, I.st);
     upload(I.mc_s, ms, I.st); upload(I.mc_e, me, I.st); upload(I.mc_p, mp, I.st);
     upload(I.nc_s, ns_, I.st); upload(I.nc_e, ne, I.st); upload(I.nc_p, np_, I.st);
-    I.ga = pick_group(nnz, M);
-    I.gt = pick_group(nnz, N);
+    // lane-group widths of A x and A^T y, timed on this batch (x and y zeroed first
+    // so the timed launches read defined values)
+    SK_CUDA(cudaMemsetAsync(I.x.ptr, 0, sizeof(double) * N, I.st));
+    SK_CUDA(cudaMemsetAsync(I.y.ptr, 0, sizeof(double) * M, I.st));
+    I.tune_a = spmv_tune(M, N, nnz, I.a_rp.ptr, I.a_ci.ptr, I.a_v.ptr, I.x.ptr, I.r.ptr, I.st);
+    I.tune_t = spmv_tune(N, M, nnz, I.t_rp.ptr, I.t_ci.ptr, I.t_v.ptr, I.y.ptr, I.v.ptr, I.st);
+    I.ga = I.tune_a.group;
+    I.gt = I.tune_t.group;
+    if (opt.verbose)
+        std::fprintf(stderr, "[sankhya] SpMV lanes per row: A %d (rule %d), A^T %d (rule %d)\n", I.ga,
+                     I.tune_a.heuristic, I.gt, I.tune_t.heuristic);
     lp_.nlp = I.nlp; lp_.M = M; lp_.N = N; lp_.nnz = nnz;
     lp_.a_rp = I.a_rp.ptr; lp_.a_ci = I.a_ci.ptr; lp_.a_v = I.a_v.ptr;
     lp_.t_rp = I.t_rp.ptr; lp_.t_ci = I.t_ci.ptr; lp_.t_v = I.t_v.ptr;
@@ -652,7 +624,7 @@ DeviceIPM::DeviceIPM(const std::vector<ipm::LpView>& lps, const std::vector<cons
     setup_ms_ = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }
 
-void DeviceIPM::profile(bool fp32, bool tensor, double* out16) {
+void DeviceIPM::profile(bool fp32, bool tensor, double* out17) {
     Impl& I = *im_;
     std::vector<double> ones(I.nlp, 1.0);
     I.put_scalars(0, ones);
@@ -660,7 +632,7 @@ void DeviceIPM::profile(bool fp32, bool tensor, double* out16) {
     k_fill<<<nblk(I.M), 256, 0, I.st>>>(I.M, I.r.ptr, 1.0);
     kkt_->set_active(std::vector<char>(I.nlp, 1));   // every front, whatever the last run left on
     kkt_->set_tensor_update(tensor);
-    kkt_->profile(I.theta.ptr, fp32 ? 1e-7 : 1e-9, fp32, I.r.ptr, I.corr.ptr, out16);
+    kkt_->profile(I.theta.ptr, fp32 ? 1e-7 : 1e-9, fp32, I.r.ptr, I.corr.ptr, out17);
 }
 
 DeviceIPM::~DeviceIPM() {

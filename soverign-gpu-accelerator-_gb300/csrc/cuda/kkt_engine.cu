@@ -73,15 +73,28 @@ __device__ __forceinline__ void tri_index(int lt, int& ti, int& tj) {
 
 // ------------------------------------------------------------------ assembly
 
-__global__ void k_asm_diag_sparse(int M, const int64_t* __restrict__ w_ptr, const int* __restrict__ w_col,
-                                  const double* __restrict__ w_val, const double* __restrict__ theta,
-                                  double* __restrict__ Mdiag, double* __restrict__ D) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= M) return;
+// Diagonal of A Theta A^T and the equilibration D = 1/sqrt(max(|m_ii|, 1e-12))
+// (reference src/cuda/kkt.cu:65-94). Row i of W holds a_ik^2 for the entries of
+// row i of A, so the rows have A's row lengths: G lanes share a row, G being the
+// width the SpMV autotuner chose for A.
+template <int G>
+__global__ void __launch_bounds__(256) k_asm_diag_sparse(int M, const int64_t* __restrict__ w_ptr,
+                                                         const int* __restrict__ w_col,
+                                                         const double* __restrict__ w_val,
+                                                         const double* __restrict__ theta,
+                                                         double* __restrict__ Mdiag, double* __restrict__ D) {
+    const int64_t gid = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int i = static_cast<int>(gid / G), lane = static_cast<int>(gid % G);
+    const bool valid = i < M;
     double acc = 0.0;
-    for (int64_t t = w_ptr[i]; t < w_ptr[i + 1]; ++t) acc += w_val[t] * theta[w_col[t]];
-    Mdiag[i] = acc;
-    D[i] = 1.0 / sqrt(fmax(fabs(acc), 1e-12));
+    if (valid)
+        for (int64_t t = w_ptr[i] + lane; t < w_ptr[i + 1]; t += G) acc += w_val[t] * theta[w_col[t]];
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, G);
+    if (valid && lane == 0) {
+        Mdiag[i] = acc;
+        D[i] = 1.0 / sqrt(fmax(fabs(acc), 1e-12));
+    }
 }
 
 template <class T>
@@ -104,16 +117,49 @@ __global__ void k_asm_slots_sparse(int64_t nslots, int M, const int64_t* __restr
     F[pos[s]] = static_cast<T>(v);
 }
 
-__global__ void k_asm_diag_dense(int M, const int* __restrict__ rp, const int* __restrict__ ci,
-                                 const double* __restrict__ av, const double* __restrict__ theta,
-                                 double* __restrict__ Mdiag, double* __restrict__ D) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= M) return;
+template <int G>
+__global__ void __launch_bounds__(256) k_asm_diag_dense(int M, const int* __restrict__ rp, const int* __restrict__ ci,
+                                                        const double* __restrict__ av,
+                                                        const double* __restrict__ theta,
+                                                        double* __restrict__ Mdiag, double* __restrict__ D) {
+    const int64_t gid = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int i = static_cast<int>(gid / G), lane = static_cast<int>(gid % G);
+    const bool valid = i < M;
     double acc = 0.0;
-    for (int q = rp[i]; q < rp[i + 1]; ++q) acc += av[q] * av[q] * theta[ci[q]];
-    Mdiag[i] = acc;
-    D[i] = 1.0 / sqrt(fmax(fabs(acc), 1e-12));
+    if (valid)
+        for (int q = rp[i] + lane; q < rp[i + 1]; q += G) acc += av[q] * av[q] * theta[ci[q]];
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, G);
+    if (valid && lane == 0) {
+        Mdiag[i] = acc;
+        D[i] = 1.0 / sqrt(fmax(fabs(acc), 1e-12));
+    }
 }
+
+// Launches a diagonal kernel K<G> with G lanes per row (2, 4, 8, 16; else 32).
+template <template <int> class K, class... Args>
+void launch_diag(int M, int group, cudaStream_t st, Args... args) {
+    if (M <= 0) return;
+    const int64_t threads = static_cast<int64_t>(M) * group;
+    const int blocks = static_cast<int>((threads + 255) / 256);
+    switch (group) {
+    case 2: K<2>::launch(blocks, st, M, args...); break;
+    case 4: K<4>::launch(blocks, st, M, args...); break;
+    case 8: K<8>::launch(blocks, st, M, args...); break;
+    case 16: K<16>::launch(blocks, st, M, args...); break;
+    default: K<32>::launch(blocks, st, M, args...); break;
+    }
+}
+template <int G>
+struct DiagSparse {
+    template <class... A>
+    static void launch(int blocks, cudaStream_t st, A... a) { k_asm_diag_sparse<G><<<blocks, 256, 0, st>>>(a...); }
+};
+template <int G>
+struct DiagDense {
+    template <class... A>
+    static void launch(int blocks, cudaStream_t st, A... a) { k_asm_diag_dense<G><<<blocks, 256, 0, st>>>(a...); }
+};
 
 // One warp per column j of M (dense mode: one front per LP, natural order).
 // Column j below the diagonal is sum_k a_jk theta_k A(:,k); the k loop is
@@ -1162,14 +1208,14 @@ void KktEngine::launch_factor(T* F, T* Linv, Prof* prof) {
     const double* theta = theta_bound_;
     run(0, [&] {
         if (p.dense_mode) {
-            k_asm_diag_dense<<<blocks_for(p.M, 256), 256, 0, st_>>>(p.M, lp_.a_rp, lp_.a_ci, lp_.a_v, theta,
-                                                                     Mdiag_.ptr, D_.ptr);
+            launch_diag<DiagDense>(p.M, lp_.spmv_group_A, st_, lp_.a_rp, lp_.a_ci, lp_.a_v, theta, Mdiag_.ptr,
+                                   D_.ptr);
             k_asm_cols_dense<T><<<blocks_for(static_cast<int64_t>(p.M) * 32, 256), 256, 0, st_>>>(
                 p.M, lp_.a_rp, lp_.a_ci, lp_.a_v, lp_.t_rp, lp_.t_ci, lp_.t_v, theta, Mdiag_.ptr, D_.ptr, lp_.row_lp,
                 pdv, params_.ptr, F);
         } else {
-            k_asm_diag_sparse<<<blocks_for(p.M, 256), 256, 0, st_>>>(p.M, w_ptr_.ptr, w_col_.ptr, w_val_.ptr, theta,
-                                                                      Mdiag_.ptr, D_.ptr);
+            launch_diag<DiagSparse>(p.M, lp_.spmv_group_A, st_, w_ptr_.ptr, w_col_.ptr, w_val_.ptr, theta,
+                                    Mdiag_.ptr, D_.ptr);
             k_asm_slots_sparse<T><<<blocks_for(p.nslots, 256), 256, 0, st_>>>(
                 p.nslots, p.M, w_ptr_.ptr, w_col_.ptr, w_val_.ptr, theta, slot_i_.ptr, slot_j_.ptr, slot_pos_.ptr,
                 Mdiag_.ptr, D_.ptr, params_.ptr, F);
@@ -1385,6 +1431,25 @@ void KktEngine::profile(const double* d_theta, double delta, bool fp32, const do
     }
     out[14] = pr.upd_flops;
     out[15] = pr.upd_bytes;
+    out[16] = assembly_bytes(fp32 ? sizeof(float) : sizeof(double));
+}
+
+double KktEngine::assembly_bytes(size_t elem) const {
+    const auto& p = plan_;
+    const double M = p.M, N = p.N;
+    const double diag_out = 16.0 * M;               // Mdiag and D
+    if (p.dense_mode) {
+        // A as CSR for the diagonal and as CSR + CSC for the columns (12 bytes per entry
+        // and 4 per pointer each), Theta, and the lower triangle of every front written once
+        double tri = 0.0;
+        for (int s = 0; s < p.ns; ++s) tri += 0.5 * double(p.sn_nrows[s]) * (p.sn_nrows[s] + 1.0);
+        return 3.0 * 12.0 * lp_.nnz + 8.0 * (M + 1) + 4.0 * (N + 1) + 8.0 * N + diag_out + elem * tri;
+    }
+    // Khatri-Rao map: 12 bytes per entry, 8 per row pointer; per off-diagonal slot its
+    // two row indices (8), front position (8) and the front entry written; Theta once
+    const double w = static_cast<double>(p.w_ptr.empty() ? 0 : p.w_ptr.back());
+    const double offd = static_cast<double>(p.nslots) - M;
+    return 12.0 * w + 8.0 * (p.nslots + 1.0) + 8.0 * N + diag_out + (16.0 + elem) * offd + elem * M;
 }
 
 std::vector<double> KktEngine::fronts_host() {

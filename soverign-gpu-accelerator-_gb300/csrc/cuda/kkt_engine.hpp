@@ -41,12 +41,14 @@ public:
     void set_active(const std::vector<char>& on);
 
     // Diagnostics: one factorisation + one solve (of d_rhs) without graphs, with
-    // CUDA events around every launch; fills out[16] as sk_solver_profile documents.
+    // CUDA events around every launch; fills out[17] as sk_solver_profile documents.
     void profile(const double* d_theta, double delta, bool fp32, const double* d_rhs, double* d_out, double* out);
 
     bool last_fp32() const { return fp32_; }
     int failed_supernode() const { return failed_sn_; }
     const ipm::FrontPlan& plan() const { return plan_; }
+    // Algorithmic bytes of one assembly (normal matrix into the fronts of element size `elem`).
+    double assembly_bytes(size_t elem) const;
     double* diag_D() const { return D_.ptr; }
     // Copies the factored fronts to the host (FP64) for inspection.
     std::vector<double> fronts_host();

@@ -73,6 +73,8 @@ def _declare(L):
     L.sk_lp_standard_form.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p, _f64p, _f64p, vp, vp, C.POINTER(vp),
                                       C.POINTER(C.c_double)]
     L.sk_compute_amd_ordering.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _i32p]
+    _u8p = np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")
+    L.sk_presolve_ruiz.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p, vp, vp, vp, vp, vp, C.c_int, _f64p, _f64p]
     L.sk_fill_ordering.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _i32p]
     L.sk_dissection_ordering.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _i32p]
     L.sk_plan_stats.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p, C.c_int, _f64p, C.c_int]
@@ -98,6 +100,11 @@ def _declare(L):
         L.sk_kkt_get_factor.argtypes = [vp, _f64p, _f64p]
         L.sk_kkt_destroy.argtypes = [vp]
         L.sk_spmv_csr.argtypes = [C.c_int, vp, vp, vp, vp, C.c_double, C.c_double, vp, vp]
+        L.sk_spmv_plan_create.argtypes = [C.c_int, C.c_int, C.c_longlong, vp, vp, vp, vp, C.POINTER(vp)]
+        L.sk_spmv_plan_execute.argtypes = [vp, vp, C.c_double, C.c_double, vp, vp]
+        L.sk_spmv_plan_info.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), _f64p]
+        L.sk_spmv_plan_set_group.argtypes = [vp, C.c_int]
+        L.sk_spmv_plan_destroy.argtypes = [vp]
         _f32p = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
         L.sk_gnn_create.argtypes = [C.c_ulonglong, C.POINTER(vp)]
         L.sk_gnn_destroy.argtypes = [vp]
@@ -227,6 +234,22 @@ def solve_bounded(lp, lb=None, ub=None, **opts):
     check(lib().sk_ipm_solve_bounded(lp.m, lp.n, lp.col_ptrs, lp.row_idx, lp.vals, lp.b, lp.c, _ptr(lb), _ptr(ub),
                                      C.byref(o), _ptr(x), _ptr(y), _ptr(s), C.byref(info)), "sk_ipm_solve_bounded")
     return info.as_dict(), x, y, s
+
+
+def presolve_ruiz(lp, lb=None, ub=None, integer=None, max_iter=10, row_scale=None, col_scale=None):
+    """Ruiz equilibration of the model (sk_presolve_ruiz, host): returns dict(vals, b,
+    c, lb, ub, row_scale, col_scale) of the scaled model; lp is not modified."""
+    out = {"vals": np.array(lp.vals, dtype=np.float64), "b": np.array(lp.b, dtype=np.float64),
+           "c": np.array(lp.c, dtype=np.float64),
+           "lb": None if lb is None else np.array(lb, dtype=np.float64),
+           "ub": None if ub is None else np.array(ub, dtype=np.float64),
+           "row_scale": np.ones(lp.m) if row_scale is None else np.array(row_scale, dtype=np.float64),
+           "col_scale": np.ones(lp.n) if col_scale is None else np.array(col_scale, dtype=np.float64)}
+    ints = None if integer is None else np.ascontiguousarray(integer, dtype=np.uint8)
+    check(lib().sk_presolve_ruiz(lp.m, lp.n, lp.col_ptrs, lp.row_idx, out["vals"], _ptr(out["b"]), _ptr(out["c"]),
+                                 _ptr(out["lb"]), _ptr(out["ub"]), _ptr(ints), max_iter, out["row_scale"],
+                                 out["col_scale"]), "sk_presolve_ruiz")
+    return out
 
 
 def block_angular(seed, blocks, block_rows=500, block_cols=1200, link_rows=2000, nnz_per_col=5):
@@ -379,19 +402,60 @@ class Solver:
 
     def profile(self, fp32=True, tensor=True):
         """Kernel-class breakdown; fp32 fronts use tensor-core updates unless tensor=False."""
-        out = np.zeros(16)
-        n = lib().sk_solver_profile(self.h, (1 if tensor else 2) if fp32 else 0, out, 16)
+        out = np.zeros(17)
+        n = lib().sk_solver_profile(self.h, (1 if tensor else 2) if fp32 else 0, out, 17)
         if n < 0:
             raise RuntimeError("sk_solver_profile failed (%d): %s" % (n, last_error()))
         names = ["assembly", "potrf", "trsm", "update", "extend_add", "fwd_solve", "bwd_solve"]
         d = {nm: {"ms": out[2 * i], "launches": int(out[2 * i + 1])} for i, nm in enumerate(names)}
         d["update_flops"] = out[14]
         d["update_min_bytes"] = out[15]
+        d["assembly_bytes"] = out[16] if n >= 17 else None
         return d
 
     def close(self):
         if self.h:
             lib().sk_solver_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+SPMV_GROUPS = (2, 4, 8, 16, 32)
+
+
+class SpmvPlan:
+    """Autotuned SpMV of one device CSR matrix (sk_spmv_plan_*). Pointers are raw
+    device addresses (ints); the arrays must stay alive while the plan is used."""
+
+    def __init__(self, rows, cols, nnz, d_row_ptrs, d_col_idx, d_vals, stream=None):
+        self.rows = rows
+        self.h = C.c_void_p()
+        check(lib().sk_spmv_plan_create(rows, cols, nnz, C.c_void_p(d_row_ptrs), C.c_void_p(d_col_idx),
+                                        C.c_void_p(d_vals), C.c_void_p(stream) if stream else None,
+                                        C.byref(self.h)), "sk_spmv_plan_create")
+
+    def info(self):
+        g, hg = C.c_int(), C.c_int()
+        ms = np.zeros(len(SPMV_GROUPS))
+        check(lib().sk_spmv_plan_info(self.h, C.byref(g), C.byref(hg), ms), "sk_spmv_plan_info")
+        return {"group": g.value, "heuristic_group": hg.value, "ms_per_group": dict(zip(SPMV_GROUPS, ms.tolist()))}
+
+    def set_group(self, group):
+        check(lib().sk_spmv_plan_set_group(self.h, group), "sk_spmv_plan_set_group")
+
+    def execute(self, d_x, d_y, alpha=1.0, beta=0.0, stream=None):
+        """y = alpha A x + beta y on `stream` (raw CUDA stream handle; None = legacy default)."""
+        check(lib().sk_spmv_plan_execute(self.h, C.c_void_p(d_x), alpha, beta, C.c_void_p(d_y),
+                                         C.c_void_p(stream) if stream else None), "sk_spmv_plan_execute")
+
+    def close(self):
+        if self.h:
+            lib().sk_spmv_plan_destroy(self.h)
             self.h = C.c_void_p()
 
     def __del__(self):
