@@ -302,14 +302,17 @@ def spmv_rooflines(sk, hbm, src, nlps=512, warm=3, reps=10):
             lib_ms = "unavailable: %s" % type(e).__name__
         nbytes = 12.0 * nnz + 4.0 * (rows + 1) + 8.0 * cols + 8.0 * rows
         a = nbytes / (ms / 1000.0) / 1e9
-        out.append({"kernel": "k_spmv<%d, EpiAxpby> (%s, family-3 batch of %d LPs as one block-diagonal matrix)"
-                              % (tune["group"], name, nlps),
+        kname = "k_spmv_win" if tune["windowed"] else "k_spmv"
+        out.append({"kernel": "%s<%d, EpiAxpby> (%s, family-3 batch of %d LPs as one block-diagonal matrix)"
+                              % (kname, tune["group"], name, nlps),
                     "bound": "hbm", "achieved": a, "peak": hbm, "unit": "GB/s", "frac": a / hbm,
                     "peak_source": "%s copy bandwidth (MEASURED_PEAKS.json hbm_gbs)" % src, "traffic": None,
                     "rows": rows, "cols": cols, "nnz": nnz, "algorithmic_bytes": nbytes, "ms_per_launch": ms,
                     "launches_timed": reps, "l2": "256 MB written before each launch",
                     "lanes_per_row": tune["group"], "rule_lanes_per_row": tune["heuristic_group"],
+                    "shared_memory_windows": tune["windowed"],
                     "autotune_ms_per_width": tune["ms_per_group"],
+                    "autotune_ms_per_width_windowed": tune["ms_windowed_per_group"],
                     "cusparse_ms_per_launch": lib_ms, "max_rel_diff_vs_cusparse": max_rel})
         plan.close()
         del d_rp, d_ci, d_v, x, y

@@ -301,27 +301,35 @@ int sk_spmv_csr(int rows, const int* d_row_ptrs, const int* d_col_idx, const dou
 /* ---- Autotuned SpMV plans ----
  * Replaces the reference's descriptor-based cuSPARSE SpMV (cusparseCreateCsr at
  * src/ipm/mehrotra_device.cu:424-428, cusparseSpMV_bufferSize + cusparseSpMV at
- * :508-530 and :596-624) for one CSR matrix kept on the device by the caller (rows x cols,
- * nnz entries, int32 indices, FP64 values; the arrays must outlive the plan).
- * sk_spmv_plan_create times the project's vector CSR kernel for 2, 4, 8, 16 and
- * 32 lanes per row on this matrix (it allocates and frees its own x / y scratch
- * and synchronises `stream`) and keeps the fastest; the width is remembered for
- * the process under (device, rows, cols, nnz), so later plans and solvers on the
- * same shape reuse it. sk_spmv_plan_execute computes y = alpha A x + beta y
- * asynchronously on `stream` (NULL = legacy default stream). sk_spmv_plan_info
- * reports the width in use, the row-length rule's width, and the fastest timed
- * launch of each width in milliseconds (ms_per_group: 5 entries in the order
- * 2, 4, 8, 16, 32; all zero if the width came from an earlier plan). */
+ * :508-530 and :596-624) for one CSR matrix kept on the device by the caller
+ * (rows x cols, nnz entries, int32 indices, FP64 values; the arrays must outlive
+ * the plan). sk_spmv_plan_create cuts the rows into chunks whose columns fit a
+ * shared-memory window of x (up to 24576 columns), then times the project's two
+ * vector CSR kernels (x gathered from global memory, or staged per chunk in
+ * shared memory) for 2, 4, 8, 16 and 32 lanes per row on this matrix and keeps
+ * the fastest. It allocates and frees its own x / y scratch, keeps the chunk
+ * table in device memory until sk_spmv_plan_destroy, and synchronises `stream`.
+ * The choice is remembered for the process under (device, rows, cols, nnz), so
+ * later plans and solvers on the same shape reuse it without timing.
+ * sk_spmv_plan_execute computes y = alpha A x + beta y asynchronously on `stream`
+ * (NULL = legacy default stream). sk_spmv_plan_info reports the width in use,
+ * whether shared-memory windows are in use, the row-length rule's width, and
+ * the fastest timed launch of each width in milliseconds for the plain and the
+ * windowed kernel (5 entries each in the order 2, 4, 8, 16, 32; zero when not
+ * timed or when the choice came from an earlier plan); any output may be NULL. */
 typedef struct sk_spmv_plan sk_spmv_plan;
 int sk_spmv_plan_create(int rows, int cols, long long nnz, const int* d_row_ptrs, const int* d_col_idx,
                         const double* d_vals, void* stream, sk_spmv_plan** out);
 int sk_spmv_plan_execute(const sk_spmv_plan* plan, const double* d_x, double alpha, double beta, double* d_y,
                          void* stream);
-int sk_spmv_plan_info(const sk_spmv_plan* plan, int* group, int* heuristic_group, double* ms_per_group);
-/* Overrides the plan's width (2, 4, 8, 16 or 32 lanes per row; other values:
- * SK_ERR_INVALID). Every width computes the same products; only the order of
- * the additions within a row differs. */
-int sk_spmv_plan_set_group(sk_spmv_plan* plan, int group);
+int sk_spmv_plan_info(const sk_spmv_plan* plan, int* group, int* windowed, int* heuristic_group,
+                      double* ms_per_group, double* ms_windowed_per_group);
+/* Overrides the plan's choice: `group` lanes per row (2, 4, 8, 16 or 32) and
+ * windowed 0 (global gathers) or 1 (shared-memory windows); other values give
+ * SK_ERR_INVALID. Every choice computes the same products; only the order of
+ * the additions within a row depends on `group` (windowed or not gives the same
+ * bits for the same group). */
+int sk_spmv_plan_set_group(sk_spmv_plan* plan, int group, int windowed);
 void sk_spmv_plan_destroy(sk_spmv_plan* plan);
 
 /* ---- Model input ----

@@ -419,6 +419,8 @@ struct sk_spmv_plan {
     const int* ci = nullptr;
     const double* v = nullptr;
     dev::SpmvTuning tune;
+    dev::SpmvWindows win;
+    dev::SpmvShape shape;
 };
 
 int sk_spmv_plan_create(int rows, int cols, long long nnz, const int* d_row_ptrs, const int* d_col_idx,
@@ -448,12 +450,14 @@ int sk_spmv_plan_create(int rows, int cols, long long nnz, const int* d_row_ptrs
             SK_CUDA(cudaMalloc(&xs, sizeof(double) * std::max(1, cols)));
             SK_CUDA(cudaMalloc(&ys, sizeof(double) * rows));
             SK_CUDA(cudaMemsetAsync(xs, 0, sizeof(double) * std::max(1, cols), st));
-            p->tune = dev::spmv_tune(rows, cols, nnz, d_row_ptrs, d_col_idx, d_vals, xs, ys, st);
+            p->win.build(rows, d_row_ptrs, d_col_idx, st);
+            p->tune = dev::spmv_tune(rows, cols, nnz, d_row_ptrs, d_col_idx, d_vals, xs, ys, st, &p->win);
             SK_CUDA(cudaFree(xs));
             xs = nullptr;
             SK_CUDA(cudaFree(ys));
             ys = nullptr;
         }
+        p->shape = p->win.shape(p->tune.group, p->tune.windowed);
         *out = p.release();
         return SK_OK;
     } catch (...) {
@@ -468,7 +472,7 @@ int sk_spmv_plan_execute(const sk_spmv_plan* p, const double* d_x, double alpha,
     api::clear_error();
     if (!p || (p->rows > 0 && (!d_x || !d_y))) return SK_ERR_INVALID;
     try {
-        dev::spmv_axpby(p->rows, p->tune.group, p->rp, p->ci, p->v, d_x, alpha, beta, d_y,
+        dev::spmv_axpby(p->rows, p->shape, p->rp, p->ci, p->v, d_x, alpha, beta, d_y,
                         static_cast<cudaStream_t>(stream));
         return SK_OK;
     } catch (...) {
@@ -476,22 +480,27 @@ int sk_spmv_plan_execute(const sk_spmv_plan* p, const double* d_x, double alpha,
     }
 }
 
-int sk_spmv_plan_info(const sk_spmv_plan* p, int* group, int* heuristic_group, double* ms_per_group) {
+int sk_spmv_plan_info(const sk_spmv_plan* p, int* group, int* windowed, int* heuristic_group,
+                      double* ms_per_group, double* ms_windowed_per_group) {
     api::clear_error();
     if (!p) return SK_ERR_INVALID;
-    if (group) *group = p->tune.group;
+    if (group) *group = p->shape.group;
+    if (windowed) *windowed = p->shape.windowed ? 1 : 0;
     if (heuristic_group) *heuristic_group = p->tune.heuristic;
-    if (ms_per_group)
-        for (int k = 0; k < dev::kSpmvNumGroups; ++k) ms_per_group[k] = p->tune.from_cache ? 0.0 : p->tune.ms[k];
+    for (int k = 0; k < dev::kSpmvNumGroups; ++k) {
+        if (ms_per_group) ms_per_group[k] = p->tune.from_cache ? 0.0 : p->tune.ms[k];
+        if (ms_windowed_per_group) ms_windowed_per_group[k] = p->tune.from_cache ? 0.0 : p->tune.ms_win[k];
+    }
     return SK_OK;
 }
 
-int sk_spmv_plan_set_group(sk_spmv_plan* p, int group) {
+int sk_spmv_plan_set_group(sk_spmv_plan* p, int group, int windowed) {
     api::clear_error();
-    if (!p) return SK_ERR_INVALID;
+    if (!p || (windowed != 0 && windowed != 1)) return SK_ERR_INVALID;
     for (int k = 0; k < dev::kSpmvNumGroups; ++k)
         if (dev::kSpmvGroups[k] == group) {
-            p->tune.group = group;
+            if (windowed && p->rows > 0 && p->win.chunks() == 0) return SK_ERR_INVALID;
+            p->shape = p->win.shape(group, windowed != 0);
             return SK_OK;
         }
     return SK_ERR_INVALID;

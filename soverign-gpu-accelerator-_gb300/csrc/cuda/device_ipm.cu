@@ -406,8 +406,9 @@ struct DeviceIPM::Impl {
     double solve_ms = 0.0, device_ms = 0.0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::vector<double> hx0, hy0, hs0;      // user start (scaled)
-    int ga = 4, gt = 4;                 // SpMV lanes per row of A and A^T (autotuned at set-up)
+    SpmvShape ga, gt;                       // SpMV launch shapes of A and A^T (autotuned at set-up)
     SpmvTuning tune_a, tune_t;
+    SpmvWindows win_a, win_t;               // shared-memory chunk tables of A and A^T
     Gnn* gnn = nullptr;                     // network of SK_START_LEARNED (not owned)
     double capture_mu = 0.0;                // iterate capture for training targets
     std::vector<char> captured;
@@ -601,13 +602,16 @@ DeviceIPM::DeviceIPM(const std::vector<ipm::LpView>& lps, const std::vector<cons
     // so the timed launches read defined values)
     SK_CUDA(cudaMemsetAsync(I.x.ptr, 0, sizeof(double) * N, I.st));
     SK_CUDA(cudaMemsetAsync(I.y.ptr, 0, sizeof(double) * M, I.st));
-    I.tune_a = spmv_tune(M, N, nnz, I.a_rp.ptr, I.a_ci.ptr, I.a_v.ptr, I.x.ptr, I.r.ptr, I.st);
-    I.tune_t = spmv_tune(N, M, nnz, I.t_rp.ptr, I.t_ci.ptr, I.t_v.ptr, I.y.ptr, I.v.ptr, I.st);
-    I.ga = I.tune_a.group;
-    I.gt = I.tune_t.group;
+    I.win_a.build(M, I.a_rp.ptr, I.a_ci.ptr, I.st);
+    I.win_t.build(N, I.t_rp.ptr, I.t_ci.ptr, I.st);
+    I.tune_a = spmv_tune(M, N, nnz, I.a_rp.ptr, I.a_ci.ptr, I.a_v.ptr, I.x.ptr, I.r.ptr, I.st, &I.win_a);
+    I.tune_t = spmv_tune(N, M, nnz, I.t_rp.ptr, I.t_ci.ptr, I.t_v.ptr, I.y.ptr, I.v.ptr, I.st, &I.win_t);
+    I.ga = I.win_a.shape(I.tune_a.group, I.tune_a.windowed);
+    I.gt = I.win_t.shape(I.tune_t.group, I.tune_t.windowed);
     if (opt.verbose)
-        std::fprintf(stderr, "[sankhya] SpMV lanes per row: A %d (rule %d), A^T %d (rule %d)\n", I.ga,
-                     I.tune_a.heuristic, I.gt, I.tune_t.heuristic);
+        std::fprintf(stderr, "[sankhya] SpMV: A %d lanes per row%s (rule %d), A^T %d%s (rule %d)\n", I.ga.group,
+                     I.ga.windowed ? ", shared-memory windows" : "", I.tune_a.heuristic, I.gt.group,
+                     I.gt.windowed ? ", shared-memory windows" : "", I.tune_t.heuristic);
     lp_.nlp = I.nlp; lp_.M = M; lp_.N = N; lp_.nnz = nnz;
     lp_.a_rp = I.a_rp.ptr; lp_.a_ci = I.a_ci.ptr; lp_.a_v = I.a_v.ptr;
     lp_.t_rp = I.t_rp.ptr; lp_.t_ci = I.t_ci.ptr; lp_.t_v = I.t_v.ptr;
@@ -616,7 +620,7 @@ DeviceIPM::DeviceIPM(const std::vector<ipm::LpView>& lps, const std::vector<cons
     lp_.n_mchunks = static_cast<int>(ms.size()); lp_.n_nchunks = static_cast<int>(ns_.size());
     lp_.mc_start = I.mc_s.ptr; lp_.mc_end = I.mc_e.ptr; lp_.mc_ptr = I.mc_p.ptr;
     lp_.nc_start = I.nc_s.ptr; lp_.nc_end = I.nc_e.ptr; lp_.nc_ptr = I.nc_p.ptr;
-    lp_.spmv_group_A = I.ga; lp_.spmv_group_T = I.gt;
+    lp_.spmv_group_A = I.ga.group; lp_.spmv_group_T = I.gt.group;
     kkt_.reset(new KktEngine(plan, lp_, I.st));
     SK_CUDA(cudaStreamSynchronize(I.st));
     I.res.assign(I.nlp, LpResult());

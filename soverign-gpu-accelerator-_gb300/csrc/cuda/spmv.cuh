@@ -13,7 +13,10 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
+
+#include "cuda/spmv_shape.hpp"
 
 namespace sankhya {
 namespace dev {
@@ -47,6 +50,98 @@ void spmv(int rows, int group, const int* rp, const int* ci, const double* v, co
     case 16: k_spmv<16><<<spmv_blocks(threads), 256, 0, st>>>(rows, rp, ci, v, x, epi); break;
     default: k_spmv<32><<<spmv_blocks(threads), 256, 0, st>>>(rows, rp, ci, v, x, epi); break;
     }
+}
+
+// ---- windowed variant: x staged in shared memory per chunk of rows ----
+//
+// Rows are cut into chunks (int4 {row0, row1, col0, ncols}) whose entries all lie
+// in columns [col0, col0 + ncols); one CTA of kWinThreads threads copies that
+// window of x into shared memory once and then runs the chunk's rows with G lanes
+// per row, so the per-entry gathers of x hit shared memory instead of each
+// taking its own L1 sector lookup. A chunk with ncols < 0 holds rows too wide for
+// any window and gathers from global memory. Built by SpmvWindows (autotune.hpp).
+template <int G, class Epi>
+__global__ void __launch_bounds__(kWinThreads) k_spmv_win(const int4* __restrict__ chunks,
+                                                           const int* __restrict__ rp, const int* __restrict__ ci,
+                                                           const double* __restrict__ v,
+                                                           const double* __restrict__ x, Epi epi) {
+    extern __shared__ double xs[];
+    const int4 ch = chunks[blockIdx.x];
+    const bool staged = ch.w >= 0;
+    if (staged)
+        for (int t = threadIdx.x; t < ch.w; t += blockDim.x) xs[t] = x[ch.z + t];
+    __syncthreads();
+    const int groups = blockDim.x / G;
+    const int g = threadIdx.x / G, lane = threadIdx.x % G;
+    // the trip count depends on the chunk only, so every lane reaches the shuffles
+    for (int base = ch.x; base < ch.y; base += groups) {
+        const int row = base + g;
+        const bool valid = row < ch.y;
+        double acc = 0.0;
+        if (valid) {
+            const int q1 = rp[row + 1];
+            if (staged)
+                for (int q = rp[row] + lane; q < q1; q += G) acc += v[q] * xs[ci[q] - ch.z];
+            else
+                for (int q = rp[row] + lane; q < q1; q += G) acc += v[q] * x[ci[q]];
+        }
+#pragma unroll
+        for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, G);
+        if (valid && lane == 0) epi(row, acc);
+    }
+}
+
+// Opts k_spmv_win<G, Epi> into kWinMaxCols doubles of dynamic shared memory on
+// the current device (once per instantiation and device; devices 0..63).
+// Returns false if the device refuses (the caller then runs the plain kernel).
+template <int G, class Epi>
+inline bool win_smem_attr() {
+    static std::atomic<unsigned long long> done{0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return false;
+    const unsigned long long bit = 1ull << (dev & 63);
+    if (done.load() & bit) return true;
+    if (cudaFuncSetAttribute(k_spmv_win<G, Epi>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             kWinMaxCols * static_cast<int>(sizeof(double))) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    done.fetch_or(bit);
+    return true;
+}
+
+template <class Epi>
+void spmv_win(int rows, const SpmvShape& sh, const int* rp, const int* ci, const double* v, const double* x, Epi epi,
+              cudaStream_t st) {
+    if (sh.nchunks <= 0) return;
+    const int smem = sh.max_cols * static_cast<int>(sizeof(double));
+    bool ok = false;
+    switch (sh.group) {
+    case 2: if ((ok = win_smem_attr<2, Epi>()))
+            k_spmv_win<2><<<sh.nchunks, kWinThreads, smem, st>>>(sh.chunks, rp, ci, v, x, epi);
+        break;
+    case 4: if ((ok = win_smem_attr<4, Epi>()))
+            k_spmv_win<4><<<sh.nchunks, kWinThreads, smem, st>>>(sh.chunks, rp, ci, v, x, epi);
+        break;
+    case 8: if ((ok = win_smem_attr<8, Epi>()))
+            k_spmv_win<8><<<sh.nchunks, kWinThreads, smem, st>>>(sh.chunks, rp, ci, v, x, epi);
+        break;
+    case 16: if ((ok = win_smem_attr<16, Epi>()))
+            k_spmv_win<16><<<sh.nchunks, kWinThreads, smem, st>>>(sh.chunks, rp, ci, v, x, epi);
+        break;
+    default: if ((ok = win_smem_attr<32, Epi>()))
+            k_spmv_win<32><<<sh.nchunks, kWinThreads, smem, st>>>(sh.chunks, rp, ci, v, x, epi);
+        break;
+    }
+    if (!ok) spmv(rows, sh.group, rp, ci, v, x, epi, st);
+}
+
+// The SpMV of a matrix as its shape says: windowed or plain, with its lane width.
+template <class Epi>
+void spmv(int rows, const SpmvShape& sh, const int* rp, const int* ci, const double* v, const double* x, Epi epi,
+          cudaStream_t st) {
+    if (sh.windowed) spmv_win(rows, sh, rp, ci, v, x, epi, st);
+    else spmv(rows, sh.group, rp, ci, v, x, epi, st);
 }
 
 struct EpiAxpby {        // y = alpha d + beta y

@@ -568,6 +568,41 @@ void build_front_plan(const std::vector<LpView>& lps, const core::CSRMatrix& A, 
             p.slot_j[sl] = ci[q];
             p.slot_pos[sl] = fpos(i, ci[q]);
         }
+    // 9. off-diagonal slots in front-position order: the assembly runs one thread per
+    // slot, so consecutive threads then store consecutive entries of a front column
+    // (coalesced) instead of entries one leading dimension apart. Each slot keeps its
+    // own W entries in their order, so every value is summed exactly as before.
+    {
+        const int64_t noff_s = p.nslots - p.M;
+        std::vector<int64_t> ord(static_cast<size_t>(noff_s));
+        for (int64_t k = 0; k < noff_s; ++k) ord[k] = p.M + k;
+        std::stable_sort(ord.begin(), ord.end(),
+                         [&](int64_t a, int64_t b) { return p.slot_pos[a] < p.slot_pos[b]; });
+        std::vector<int64_t> wp(static_cast<size_t>(p.nslots) + 1), sp(static_cast<size_t>(p.nslots));
+        std::vector<Index> si(static_cast<size_t>(p.nslots)), sj(static_cast<size_t>(p.nslots));
+        std::vector<Index> wc(p.w_col.size());
+        std::vector<Float> wv(p.w_val.size());
+        int64_t at = 0;
+        auto take = [&](int64_t dst, int64_t src) {
+            wp[dst] = at;
+            for (int64_t t = p.w_ptr[src]; t < p.w_ptr[src + 1]; ++t, ++at) {
+                wc[at] = p.w_col[t];
+                wv[at] = p.w_val[t];
+            }
+            sp[dst] = p.slot_pos[src];
+            si[dst] = p.slot_i[src];
+            sj[dst] = p.slot_j[src];
+        };
+        for (int64_t s0 = 0; s0 < p.M; ++s0) take(s0, s0);
+        for (int64_t k = 0; k < noff_s; ++k) take(p.M + k, ord[k]);
+        wp[p.nslots] = at;
+        p.w_ptr.swap(wp);
+        p.w_col.swap(wc);
+        p.w_val.swap(wv);
+        p.slot_pos.swap(sp);
+        p.slot_i.swap(si);
+        p.slot_j.swap(sj);
+    }
 }
 
 }  // namespace ipm

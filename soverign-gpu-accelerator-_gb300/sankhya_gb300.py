@@ -102,8 +102,9 @@ def _declare(L):
         L.sk_spmv_csr.argtypes = [C.c_int, vp, vp, vp, vp, C.c_double, C.c_double, vp, vp]
         L.sk_spmv_plan_create.argtypes = [C.c_int, C.c_int, C.c_longlong, vp, vp, vp, vp, C.POINTER(vp)]
         L.sk_spmv_plan_execute.argtypes = [vp, vp, C.c_double, C.c_double, vp, vp]
-        L.sk_spmv_plan_info.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), _f64p]
-        L.sk_spmv_plan_set_group.argtypes = [vp, C.c_int]
+        L.sk_spmv_plan_info.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int), _f64p,
+                                        _f64p]
+        L.sk_spmv_plan_set_group.argtypes = [vp, C.c_int, C.c_int]
         L.sk_spmv_plan_destroy.argtypes = [vp]
         _f32p = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
         L.sk_gnn_create.argtypes = [C.c_ulonglong, C.POINTER(vp)]
@@ -440,13 +441,15 @@ class SpmvPlan:
                                         C.byref(self.h)), "sk_spmv_plan_create")
 
     def info(self):
-        g, hg = C.c_int(), C.c_int()
-        ms = np.zeros(len(SPMV_GROUPS))
-        check(lib().sk_spmv_plan_info(self.h, C.byref(g), C.byref(hg), ms), "sk_spmv_plan_info")
-        return {"group": g.value, "heuristic_group": hg.value, "ms_per_group": dict(zip(SPMV_GROUPS, ms.tolist()))}
+        g, w, hg = C.c_int(), C.c_int(), C.c_int()
+        ms, msw = np.zeros(len(SPMV_GROUPS)), np.zeros(len(SPMV_GROUPS))
+        check(lib().sk_spmv_plan_info(self.h, C.byref(g), C.byref(w), C.byref(hg), ms, msw), "sk_spmv_plan_info")
+        return {"group": g.value, "windowed": bool(w.value), "heuristic_group": hg.value,
+                "ms_per_group": dict(zip(SPMV_GROUPS, ms.tolist())),
+                "ms_windowed_per_group": dict(zip(SPMV_GROUPS, msw.tolist()))}
 
-    def set_group(self, group):
-        check(lib().sk_spmv_plan_set_group(self.h, group), "sk_spmv_plan_set_group")
+    def set_group(self, group, windowed=False):
+        check(lib().sk_spmv_plan_set_group(self.h, group, 1 if windowed else 0), "sk_spmv_plan_set_group")
 
     def execute(self, d_x, d_y, alpha=1.0, beta=0.0, stream=None):
         """y = alpha A x + beta y on `stream` (raw CUDA stream handle; None = legacy default)."""
