@@ -30,8 +30,10 @@ void compute_symbolic_factorization(const core::CSRMatrix& A, const std::vector<
 std::vector<Index> fill_reducing_ordering(const core::CSRMatrix& A);
 
 // The same ordering on an explicit graph: Av[i] = sorted neighbours of vertex i
-// (no self loops, symmetric). P[k] = vertex eliminated k-th.
-std::vector<Index> min_degree_order(std::vector<std::vector<Index>> Av);
+// (no self loops, symmetric). P[k] = vertex eliminated k-th. Vertices flagged in
+// last_rows are eliminated after all others, in their index order.
+std::vector<Index> min_degree_order(std::vector<std::vector<Index>> Av,
+                                    const std::vector<char>* last_rows = nullptr);
 
 // Sorted, duplicate-free adjacency of A A^T without self loops.
 std::vector<std::vector<Index>> aat_graph(const core::CSRMatrix& A);

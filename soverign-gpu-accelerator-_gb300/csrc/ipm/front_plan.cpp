@@ -574,10 +574,12 @@ void build_front_plan(const std::vector<LpView>& lps, const core::CSRMatrix& A, 
     // own W entries in their order, so every value is summed exactly as before.
     {
         const int64_t noff_s = p.nslots - p.M;
+        std::vector<std::pair<int64_t, int64_t>> key(static_cast<size_t>(noff_s));   // (front position, slot)
+        for (int64_t k = 0; k < noff_s; ++k) key[k] = {p.slot_pos[p.M + k], p.M + k};
+        std::sort(key.begin(), key.end());        // positions are distinct
         std::vector<int64_t> ord(static_cast<size_t>(noff_s));
-        for (int64_t k = 0; k < noff_s; ++k) ord[k] = p.M + k;
-        std::stable_sort(ord.begin(), ord.end(),
-                         [&](int64_t a, int64_t b) { return p.slot_pos[a] < p.slot_pos[b]; });
+        for (int64_t k = 0; k < noff_s; ++k) ord[k] = key[k].second;
+        std::vector<std::pair<int64_t, int64_t>>().swap(key);
         std::vector<int64_t> wp(static_cast<size_t>(p.nslots) + 1), sp(static_cast<size_t>(p.nslots));
         std::vector<Index> si(static_cast<size_t>(p.nslots)), sj(static_cast<size_t>(p.nslots));
         std::vector<Index> wc(p.w_col.size());
