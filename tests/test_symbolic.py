@@ -108,3 +108,47 @@ def test_auto_ordering_of_a_large_staircase(sk):
     nat = sk.plan_stats(lp, sk.ORDER_NATURAL)
     assert auto["ordering_used"] in (2, 4) and auto["consistent"] == 1
     assert auto["flops_factor"] <= nat["flops_factor"] * (1 + 1e-12)
+
+
+def _row_spans(lp):
+    rp, ci, _ = lp.csr()
+    lo = np.minimum.reduceat(ci, rp[:-1])
+    hi = np.maximum.reduceat(ci, rp[:-1])
+    return rp, ci, hi - lo + 1
+
+
+def test_linking_rows_are_ordered_last(sk):
+    # block-angular LP: rows spanning more than a quarter of the columns (the linking rows)
+    # come last; the blocks before them are ordered by minimum degree
+    lp = sk.block_angular(0xB1, 12, 150, 360, 200, 4)
+    rp, ci, span = _row_spans(lp)
+    wide = span * 4 > lp.n
+    assert 0 < wide.sum() <= lp.m // 4
+    P = sk.fill_ordering(lp.m, lp.n, rp, ci)
+    assert sorted(P.tolist()) == list(range(lp.m))
+    nw = int(wide.sum())
+    assert wide[P[-nw:]].all() and not wide[P[:-nw]].any()
+    assert P[-nw:].tolist() == sorted(P[-nw:].tolist())      # in their given order
+
+
+def test_constrained_ordering_is_repeatable_and_not_worse(sk):
+    # the blocks are ordered on worker threads; the result must not depend on scheduling,
+    # and the constraint must not cost fill against the natural order
+    lp = sk.block_angular(0xB2, 16, 120, 300, 160, 4)
+    rp, ci, _ = _row_spans(lp)
+    first = sk.fill_ordering(lp.m, lp.n, rp, ci)
+    for _ in range(5):
+        assert np.array_equal(sk.fill_ordering(lp.m, lp.n, rp, ci), first)
+    auto = sk.plan_stats(lp, ordering=sk.ORDER_MINDEG)
+    natural = sk.plan_stats(lp, ordering=sk.ORDER_NATURAL)
+    assert auto["consistent"] == 1.0
+    assert auto["flops_factor"] <= natural["flops_factor"]
+
+
+def test_family1_ordering_flops(sk):
+    # the family-1 LP (40 blocks + 2000 linking rows): the constrained minimum degree keeps
+    # the factorisation at or below the 2.121e10 flops of the unconstrained ordering
+    lp = sk.generate(1, 0)
+    st = sk.plan_stats(lp)
+    assert st["consistent"] == 1.0
+    assert st["flops_factor"] <= 2.121e10 * 1.0001
