@@ -503,108 +503,103 @@ void build_front_plan(const std::vector<LpView>& lps, const core::CSRMatrix& A, 
     }
     finish_offsets(p);
     build_schedule(p);
-    // 8. Khatri-Rao assembly map W
+    // 8. Khatri-Rao assembly map W. Slots: the M diagonal entries of A A^T first (slot i),
+    // then its strictly lower entries in front-position order: the assembly runs one
+    // thread per slot, so consecutive threads store consecutive entries of a front
+    // column. Columns j are visited in order (fronts are laid out in column order, and
+    // a front's rows are sorted), so the positions come out sorted without a sort.
     const int64_t noff = static_cast<int64_t>(ci.size());
     p.nslots = p.M + noff;
-    std::vector<int64_t> cnt(static_cast<size_t>(p.nslots) + 1, 0);
-    // CSC view of the batch: column k of lp L lives at col_off[L] + local
-    auto slot_of = [&](Index pi, Index pj) -> int64_t {
-        if (pi == pj) return pi;
-        const Index* b = ci.data() + rp[pi];
-        const Index* e = ci.data() + rp[pi + 1];
-        const Index* it = std::lower_bound(b, e, pj);
-        return p.M + (it - ci.data());
-    };
-    for (int L = 0; L < p.nlp; ++L) {
-        const LpView& v = lps[L];
-        for (Index j = 0; j < v.n; ++j)
-            for (Index a = v.col_ptrs[j]; a < v.col_ptrs[j + 1]; ++a)
-                for (Index b = a; b < v.col_ptrs[j + 1]; ++b) {
-                    const Index pa = p.iperm[p.row_off[L] + v.row_idx[a]];
-                    const Index pb = p.iperm[p.row_off[L] + v.row_idx[b]];
-                    cnt[slot_of(std::max(pa, pb), std::min(pa, pb)) + 1]++;
-                }
+    p.slot_pos.resize(static_cast<size_t>(p.nslots));
+    p.slot_i.resize(static_cast<size_t>(p.nslots));
+    p.slot_j.resize(static_cast<size_t>(p.nslots));
+    // column view of the strictly lower pattern (rows ascending within a column)
+    std::vector<int64_t> lcp(static_cast<size_t>(p.M) + 1, 0);
+    for (int64_t q = 0; q < noff; ++q) lcp[ci[q] + 1]++;
+    for (Index j = 0; j < p.M; ++j) lcp[j + 1] += lcp[j];
+    std::vector<Index> lrow(static_cast<size_t>(noff));
+    {
+        std::vector<int64_t> cur(lcp.begin(), lcp.end() - 1);
+        for (Index i = 0; i < p.M; ++i)
+            for (Index q = rp[i]; q < rp[i + 1]; ++q) lrow[cur[ci[q]]++] = i;
     }
-    for (int64_t s = 0; s < p.nslots; ++s) cnt[s + 1] += cnt[s];
-    p.w_ptr = cnt;
+    std::vector<int64_t> sid_row(static_cast<size_t>(noff));   // slot of row-view entry q
+    {
+        std::vector<Index> rowpos(static_cast<size_t>(p.M), -1);
+        std::vector<int64_t> rcur(rp.begin(), rp.end() - 1);
+        int64_t next = p.M, last_pos = -1;
+        bool sorted = true;
+        int tprev = -1;
+        for (Index j = 0; j < p.M; ++j) {
+            const int t = p.sn_of_col[j];
+            const int64_t o = p.sn_rows_off[t];
+            if (t != tprev) {
+                for (Index q = 0; q < p.sn_nrows[t]; ++q) rowpos[p.rows[o + q]] = q;
+                tprev = t;
+            }
+            auto fpos = [&](Index i) -> int64_t {
+                const Index q = rowpos[i];
+                if (q < 0 || q >= p.sn_nrows[t] || p.rows[o + q] != i)
+                    throw std::runtime_error("front plan: M entry outside the factor structure");
+                return p.sn_F_off[t] + q + static_cast<int64_t>(j - p.sn_first[t]) * p.sn_lda[t];
+            };
+            p.slot_i[j] = j;
+            p.slot_j[j] = j;
+            p.slot_pos[j] = fpos(j);
+            for (int64_t e = lcp[j]; e < lcp[j + 1]; ++e) {
+                const Index i = lrow[e];
+                const int64_t sl = next++;
+                p.slot_i[sl] = i;
+                p.slot_j[sl] = j;
+                p.slot_pos[sl] = fpos(i);
+                if (p.slot_pos[sl] <= last_pos) sorted = false;
+                last_pos = p.slot_pos[sl];
+                sid_row[rcur[i]++] = sl;
+            }
+        }
+        if (!sorted) throw std::runtime_error("front plan: front positions out of column order");
+    }
+    // W entries of each slot, row by row: row i of the permuted A A^T meets row j <= i in
+    // every column k holding both; the entries of a slot follow in increasing k, as a
+    // column-by-column sweep of A would give them.
+    std::vector<int> col_lp(static_cast<size_t>(p.N), 0);
+    for (int L = 0; L < p.nlp; ++L)
+        for (Index k = p.col_off[L]; k < p.col_off[L + 1]; ++k) col_lp[k] = L;
+    std::vector<int64_t> slot_of_col(static_cast<size_t>(p.M), -1);
+    auto sweep = [&](auto&& visit) {
+        for (Index i = 0; i < p.M; ++i) {
+            for (Index q = rp[i]; q < rp[i + 1]; ++q) slot_of_col[ci[q]] = sid_row[q];
+            slot_of_col[i] = i;
+            const Index r = p.perm[i];
+            for (Index kk = A.row_ptrs[r]; kk < A.row_ptrs[r + 1]; ++kk) {
+                const Index k = A.col_indices[kk];
+                const int L = col_lp[k];
+                const LpView& v = lps[L];
+                const Index jl = k - p.col_off[L], ro = p.row_off[L];
+                Float ar = 0.0;
+                for (Index e = v.col_ptrs[jl]; e < v.col_ptrs[jl + 1]; ++e)
+                    if (ro + v.row_idx[e] == r) { ar = v.vals[e]; break; }
+                for (Index e = v.col_ptrs[jl]; e < v.col_ptrs[jl + 1]; ++e) {
+                    const Index j2 = p.iperm[ro + v.row_idx[e]];
+                    if (j2 <= i) visit(slot_of_col[j2], k, ar * v.vals[e]);
+                }
+            }
+        }
+    };
+    std::vector<int64_t> cnt(static_cast<size_t>(p.nslots) + 1, 0);
+    sweep([&](int64_t sl, Index, Float) { cnt[sl + 1]++; });
+    for (int64_t sl = 0; sl < p.nslots; ++sl) cnt[sl + 1] += cnt[sl];
     p.w_col.resize(static_cast<size_t>(cnt.back()));
     p.w_val.resize(static_cast<size_t>(cnt.back()));
     {
         std::vector<int64_t> nx(cnt.begin(), cnt.end() - 1);
-        for (int L = 0; L < p.nlp; ++L) {
-            const LpView& v = lps[L];
-            for (Index j = 0; j < v.n; ++j)
-                for (Index a = v.col_ptrs[j]; a < v.col_ptrs[j + 1]; ++a)
-                    for (Index b = a; b < v.col_ptrs[j + 1]; ++b) {
-                        const Index pa = p.iperm[p.row_off[L] + v.row_idx[a]];
-                        const Index pb = p.iperm[p.row_off[L] + v.row_idx[b]];
-                        const int64_t sl = slot_of(std::max(pa, pb), std::min(pa, pb));
-                        const int64_t d = nx[sl]++;
-                        p.w_col[d] = p.col_off[L] + j;
-                        p.w_val[d] = v.vals[a] * v.vals[b];
-                    }
-        }
+        sweep([&](int64_t sl, Index k, Float w) {
+            const int64_t d = nx[sl]++;
+            p.w_col[d] = k;
+            p.w_val[d] = w;
+        });
     }
-    p.slot_pos.resize(static_cast<size_t>(p.nslots));
-    p.slot_i.resize(static_cast<size_t>(p.nslots));
-    p.slot_j.resize(static_cast<size_t>(p.nslots));
-    auto fpos = [&](Index i, Index j) -> int64_t {
-        const int t = p.sn_of_col[j];
-        const Index* b = p.rows.data() + p.sn_rows_off[t];
-        const Index* e = b + p.sn_nrows[t];
-        const Index* it = std::lower_bound(b + (j - p.sn_first[t]), e, i);
-        if (it == e || *it != i) throw std::runtime_error("front plan: M entry outside the factor structure");
-        return p.sn_F_off[t] + (it - b) + static_cast<int64_t>(j - p.sn_first[t]) * p.sn_lda[t];
-    };
-    for (Index i = 0; i < p.M; ++i) {
-        p.slot_i[i] = i;
-        p.slot_j[i] = i;
-        p.slot_pos[i] = fpos(i, i);
-    }
-    for (Index i = 0; i < p.M; ++i)
-        for (Index q = rp[i]; q < rp[i + 1]; ++q) {
-            const int64_t sl = p.M + q;
-            p.slot_i[sl] = i;
-            p.slot_j[sl] = ci[q];
-            p.slot_pos[sl] = fpos(i, ci[q]);
-        }
-    // 9. off-diagonal slots in front-position order: the assembly runs one thread per
-    // slot, so consecutive threads then store consecutive entries of a front column
-    // (coalesced) instead of entries one leading dimension apart. Each slot keeps its
-    // own W entries in their order, so every value is summed exactly as before.
-    {
-        const int64_t noff_s = p.nslots - p.M;
-        std::vector<std::pair<int64_t, int64_t>> key(static_cast<size_t>(noff_s));   // (front position, slot)
-        for (int64_t k = 0; k < noff_s; ++k) key[k] = {p.slot_pos[p.M + k], p.M + k};
-        std::sort(key.begin(), key.end());        // positions are distinct
-        std::vector<int64_t> ord(static_cast<size_t>(noff_s));
-        for (int64_t k = 0; k < noff_s; ++k) ord[k] = key[k].second;
-        std::vector<std::pair<int64_t, int64_t>>().swap(key);
-        std::vector<int64_t> wp(static_cast<size_t>(p.nslots) + 1), sp(static_cast<size_t>(p.nslots));
-        std::vector<Index> si(static_cast<size_t>(p.nslots)), sj(static_cast<size_t>(p.nslots));
-        std::vector<Index> wc(p.w_col.size());
-        std::vector<Float> wv(p.w_val.size());
-        int64_t at = 0;
-        auto take = [&](int64_t dst, int64_t src) {
-            wp[dst] = at;
-            for (int64_t t = p.w_ptr[src]; t < p.w_ptr[src + 1]; ++t, ++at) {
-                wc[at] = p.w_col[t];
-                wv[at] = p.w_val[t];
-            }
-            sp[dst] = p.slot_pos[src];
-            si[dst] = p.slot_i[src];
-            sj[dst] = p.slot_j[src];
-        };
-        for (int64_t s0 = 0; s0 < p.M; ++s0) take(s0, s0);
-        for (int64_t k = 0; k < noff_s; ++k) take(p.M + k, ord[k]);
-        wp[p.nslots] = at;
-        p.w_ptr.swap(wp);
-        p.w_col.swap(wc);
-        p.w_val.swap(wv);
-        p.slot_pos.swap(sp);
-        p.slot_i.swap(si);
-        p.slot_j.swap(sj);
-    }
+    p.w_ptr.swap(cnt);
 }
 
 }  // namespace ipm
