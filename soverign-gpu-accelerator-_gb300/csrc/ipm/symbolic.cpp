@@ -8,7 +8,6 @@
 #include <exception>
 #include <mutex>
 #include <thread>
-#include <unordered_map>
 #include <vector>
 
 namespace sankhya {
@@ -229,24 +228,29 @@ std::vector<Index> fill_reducing_ordering(const core::CSRMatrix& A) {
     for (Index r = 0; r < m; ++r)
         if (!last[r]) members[comp[r]].push_back(r);
     std::vector<std::vector<Index>> part(static_cast<size_t>(ncomp));
-    auto order_component = [&](Index c) {
+    // local numbering of a component's subgraph: a dense map per worker thread (reset
+    // after each component), rows first in index order, then linking rows as met
+    auto order_component = [&](Index c, std::vector<Index>& local) {
         const auto& rows = members[c];
-        std::unordered_map<Index, Index> local;
-        local.reserve(rows.size() * 2);
         std::vector<Index> verts(rows.begin(), rows.end());
-        for (size_t q = 0; q < rows.size(); ++q) local.emplace(rows[q], static_cast<Index>(q));
+        for (size_t q = 0; q < rows.size(); ++q) local[rows[q]] = static_cast<Index>(q);
         const Index nrows = static_cast<Index>(rows.size());
         for (Index r : rows)
             for (Index v : adj[r])
-                if (last[v] && local.emplace(v, static_cast<Index>(verts.size())).second) verts.push_back(v);
+                if (last[v] && local[v] < 0) {
+                    local[v] = static_cast<Index>(verts.size());
+                    verts.push_back(v);
+                }
         std::vector<std::vector<Index>> g(verts.size());
         for (Index q = 0; q < nrows; ++q) {
+            g[q].reserve(adj[rows[q]].size());
             for (Index v : adj[rows[q]]) {
-                const Index lv = local.at(v);
+                const Index lv = local[v];
                 g[q].push_back(lv);
                 if (lv >= nrows) g[lv].push_back(q);
             }
         }
+        for (Index v : verts) local[v] = -1;
         for (auto& nb : g) std::sort(nb.begin(), nb.end());
         std::vector<char> lastl(verts.size(), 0);
         for (size_t q = static_cast<size_t>(nrows); q < verts.size(); ++q) lastl[q] = 1;
@@ -263,7 +267,8 @@ std::vector<Index> fill_reducing_ordering(const core::CSRMatrix& A) {
     for (Index t = 0; t < nthreads; ++t)
         pool.emplace_back([&, t]() {
             try {
-                for (Index c = t; c < ncomp; c += nthreads) order_component(c);
+                std::vector<Index> local(static_cast<size_t>(m), -1);
+                for (Index c = t; c < ncomp; c += nthreads) order_component(c, local);
             } catch (...) {
                 std::lock_guard<std::mutex> lk(err_mu);
                 if (!err) err = std::current_exception();
