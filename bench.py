@@ -134,7 +134,8 @@ def batch_comparison(sk, nlps):
     """LPs/s on the first `nlps` members of the 512-LP uneven batch (family 3),
     solved as one batch: mixed precision + learned start (falling back per LP to
     Mehrotra's start), mixed precision + Mehrotra's start, and the plain FP64 IPM
-    (unit start). Device time of the second of two runs of each."""
+    (unit start); device time of the second of two runs of each. Then the plain
+    FP64 IPM on the same LPs one at a time (sequential solves)."""
     lps = [sk.generate(3, k) for k in range(nlps)]
     net = None
     if os.path.exists(WEIGHTS):
@@ -165,6 +166,24 @@ def batch_comparison(sk, nlps):
     for name in ("mixed_learned", "mixed_mehrotra"):
         if name in out:
             out[name]["speedup_vs_plain_fp64"] = out[name]["lps_per_s"] / base
+    # the same LPs solved one after another by the plain FP64 IPM, one LP per solver (how the
+    # reference's device IPM is used); device time of the second of two runs of each
+    try:
+        seq_ms, seq_ok = 0.0, True
+        for lp in lps:
+            s = sk.Solver([lp], precision=sk.PREC_FP64, start=sk.START_UNIT)
+            s.run()
+            s.run()
+            info, *_ = s.result(0, want_vectors=False)
+            s.close()
+            seq_ms += info["device_ms"]
+            seq_ok = seq_ok and info["status"] == 0
+        out["sequential_plain_fp64"] = {"ms": seq_ms, "lps_per_s": 1000.0 * nlps / seq_ms, "all_optimal": seq_ok}
+        for name in ("mixed_learned", "mixed_mehrotra", "plain_fp64"):
+            if name in out:
+                out[name]["speedup_vs_sequential_plain_fp64"] = out[name]["lps_per_s"] / (1000.0 * nlps / seq_ms)
+    except Exception as e:          # the comparison is auxiliary: report, do not lose the bench line
+        out["sequential_plain_fp64"] = {"error": "%s: %s" % (type(e).__name__, e)}
     return out
 
 
