@@ -130,42 +130,61 @@ def count_kernel_launches(fn):
 WEIGHTS = os.path.join(ROOT, "soverign-gpu-accelerator-_gb300", "weights", "learned_start_family3.npy")
 
 
-def batch_comparison(sk, nlps):
+def batch_comparison(sk, nlps, dist=None, rank=0, world=1):
     """LPs/s on the first `nlps` members of the 512-LP uneven batch (family 3),
     solved as one batch: mixed precision + learned start (falling back per LP to
     Mehrotra's start), mixed precision + Mehrotra's start, and the plain FP64 IPM
     (unit start); device time of the second of two runs of each. Then the plain
-    FP64 IPM on the same LPs one at a time (sequential solves)."""
-    lps = [sk.generate(3, k) for k in range(nlps)]
+    FP64 IPM on the same LPs one at a time (sequential solves). With several ranks
+    the LPs are sharded (sharding.shard_lps): each rank solves its own LPs as one
+    batch, the time is the slowest rank's and the per-LP results are gathered to
+    rank 0 once per arm; no other communication."""
+    import sharding
+    lps_all = [sk.generate(3, k) for k in range(nlps)]
+    shards = sharding.shard_lps([sharding.lp_cost(lp.m, lp.n, lp.nnz) for lp in lps_all], world)
+    mine = shards[rank]
+    lps = [lps_all[k] for k in mine]
     net = None
     if os.path.exists(WEIGHTS):
         net = sk.Gnn(1)
         net.load(WEIGHTS)
     out = {"lps": nlps, "members": "family-3 instances 0..%d (m %d..%d)" % (
-        nlps - 1, min(lp.m for lp in lps), max(lp.m for lp in lps))}
+        nlps - 1, min(lp.m for lp in lps_all), max(lp.m for lp in lps_all))}
+    if world > 1:
+        out["sharding"] = {"ranks": world, "lps_per_rank": [len(sh) for sh in shards]}
     arms = [("mixed_learned", sk.PREC_MIXED, sk.START_LEARNED), ("mixed_mehrotra", sk.PREC_MIXED, sk.START_MEHROTRA),
             ("plain_fp64", sk.PREC_FP64, sk.START_UNIT)]
     for name, prec, start in arms:
-        if start == sk.START_LEARNED and net is None:
+        if start == sk.START_LEARNED and net is None:   # the same weights file on every rank
             continue
-        s = sk.Solver(lps, precision=prec, start=start)
+        infos, ms = [], 0.0
+        if lps:
+            s = sk.Solver(lps, precision=prec, start=start)
+            if start == sk.START_LEARNED:
+                s.set_gnn(net)
+            s.run()
+            s.run()
+            infos = [s.result(k, want_vectors=False)[0] for k in range(len(lps))]
+            s.close()
+            ms = infos[0]["device_ms"]
+        ms = barrier_max(dist, ms)
+        per_lp = sharding.gather_results({mine[q]: {"status": i["status"], "iterations": i["iterations"],
+                                                    "learned_start": i["learned_start"]}
+                                          for q, i in enumerate(infos)}, dist, rank, world)
+        if per_lp is None:
+            continue
+        vals = [per_lp[k] for k in range(nlps)]
+        out[name] = {"ms": ms, "lps_per_s": 1000.0 * nlps / ms, "all_optimal": all(v["status"] == 0 for v in vals),
+                     "mean_iterations": sum(v["iterations"] for v in vals) / nlps}
         if start == sk.START_LEARNED:
-            s.set_gnn(net)
-        s.run()
-        s.run()
-        infos = [s.result(k, want_vectors=False)[0] for k in range(nlps)]
-        s.close()
-        ms = infos[0]["device_ms"]
-        out[name] = {"ms": ms, "lps_per_s": 1000.0 * nlps / ms, "all_optimal": all(i["status"] == 0 for i in infos),
-                     "mean_iterations": sum(i["iterations"] for i in infos) / nlps}
-        if start == sk.START_LEARNED:
-            out[name]["learned_used"] = sum(i["learned_start"] for i in infos)
+            out[name]["learned_used"] = sum(v["learned_start"] for v in vals)
     if net is not None:
         net.close()
-    base = out["plain_fp64"]["lps_per_s"]
-    for name in ("mixed_learned", "mixed_mehrotra"):
-        if name in out:
-            out[name]["speedup_vs_plain_fp64"] = out[name]["lps_per_s"] / base
+    if "plain_fp64" in out:
+        base = out["plain_fp64"]["lps_per_s"]
+        for name in ("mixed_learned", "mixed_mehrotra"):
+            if name in out:
+                out[name]["speedup_vs_plain_fp64"] = out[name]["lps_per_s"] / base
     # the same LPs solved one after another by the plain FP64 IPM, one LP per solver (how the
     # reference's device IPM is used); device time of the second of two runs of each
     try:
@@ -178,10 +197,14 @@ def batch_comparison(sk, nlps):
             s.close()
             seq_ms += info["device_ms"]
             seq_ok = seq_ok and info["status"] == 0
-        out["sequential_plain_fp64"] = {"ms": seq_ms, "lps_per_s": 1000.0 * nlps / seq_ms, "all_optimal": seq_ok}
-        for name in ("mixed_learned", "mixed_mehrotra", "plain_fp64"):
-            if name in out:
-                out[name]["speedup_vs_sequential_plain_fp64"] = out[name]["lps_per_s"] / (1000.0 * nlps / seq_ms)
+        seq_ms = barrier_max(dist, seq_ms)
+        oks = sharding.gather_results({rank: seq_ok}, dist, rank, world)
+        if oks is not None:
+            out["sequential_plain_fp64"] = {"ms": seq_ms, "lps_per_s": 1000.0 * nlps / seq_ms,
+                                            "all_optimal": all(oks.values())}
+            for name in ("mixed_learned", "mixed_mehrotra", "plain_fp64"):
+                if name in out:
+                    out[name]["speedup_vs_sequential_plain_fp64"] = out[name]["lps_per_s"] / (1000.0 * nlps / seq_ms)
     except Exception as e:          # the comparison is auxiliary: report, do not lose the bench line
         out["sequential_plain_fp64"] = {"error": "%s: %s" % (type(e).__name__, e)}
     return out
@@ -367,10 +390,12 @@ def dist_setup(args):
 
 
 def barrier_max(dist, v):
+    """Max of v over all ranks (v itself without a process group)."""
     if dist is None:
         return v
     import torch
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -425,7 +450,7 @@ def run_ours(args):
     info64b, *_ = fp64.result(0, want_vectors=False)
     prof64 = fp64.profile(fp32=False)
     fp64.close()
-    batch = batch_comparison(sk, args.batch_lps) if args.batch_lps > 0 else None
+    batch = batch_comparison(sk, args.batch_lps, dist, rank, world) if args.batch_lps > 0 else None
     family2 = None if args.no_family2 else family2_comparison(sk, args.family2_unit_start)
     # end to end through the C ABI (host arrays in, host solution out)
     e2e_t = []
