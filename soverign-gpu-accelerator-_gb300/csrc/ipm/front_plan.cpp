@@ -3,6 +3,7 @@
 
 #include <algorithm>
 #include <future>
+#include <thread>
 #include <numeric>
 #include <stdexcept>
 
@@ -565,9 +566,10 @@ void build_front_plan(const std::vector<LpView>& lps, const core::CSRMatrix& A, 
     std::vector<int> col_lp(static_cast<size_t>(p.N), 0);
     for (int L = 0; L < p.nlp; ++L)
         for (Index k = p.col_off[L]; k < p.col_off[L + 1]; ++k) col_lp[k] = L;
-    std::vector<int64_t> slot_of_col(static_cast<size_t>(p.M), -1);
-    auto sweep = [&](auto&& visit) {
-        for (Index i = 0; i < p.M; ++i) {
+    // Rows only touch their own slots (slot (i, j) belongs to row i), so both sweeps split
+    // over row ranges on worker threads, each with its own column-to-slot scratch.
+    auto sweep_rows = [&](Index i0, Index i1, std::vector<int64_t>& slot_of_col, auto&& visit) {
+        for (Index i = i0; i < i1; ++i) {
             for (Index q = rp[i]; q < rp[i + 1]; ++q) slot_of_col[ci[q]] = sid_row[q];
             slot_of_col[i] = i;
             const Index r = p.perm[i];
@@ -586,14 +588,28 @@ void build_front_plan(const std::vector<LpView>& lps, const core::CSRMatrix& A, 
             }
         }
     };
+    const int nthreads = p.M >= 4096 ? static_cast<int>(std::max(1u, std::min(16u, std::thread::hardware_concurrency())))
+                                     : 1;
+    auto parallel_rows = [&](auto&& visit) {
+        auto body = [&](int t) {
+            std::vector<int64_t> slot_of_col(static_cast<size_t>(p.M), -1);
+            const Index i0 = static_cast<Index>(static_cast<int64_t>(p.M) * t / nthreads);
+            const Index i1 = static_cast<Index>(static_cast<int64_t>(p.M) * (t + 1) / nthreads);
+            sweep_rows(i0, i1, slot_of_col, visit);
+        };
+        if (nthreads == 1) { body(0); return; }
+        std::vector<std::thread> pool;
+        for (int t = 0; t < nthreads; ++t) pool.emplace_back(body, t);
+        for (auto& th : pool) th.join();
+    };
     std::vector<int64_t> cnt(static_cast<size_t>(p.nslots) + 1, 0);
-    sweep([&](int64_t sl, Index, Float) { cnt[sl + 1]++; });
+    parallel_rows([&](int64_t sl, Index, Float) { cnt[sl + 1]++; });
     for (int64_t sl = 0; sl < p.nslots; ++sl) cnt[sl + 1] += cnt[sl];
     p.w_col.resize(static_cast<size_t>(cnt.back()));
     p.w_val.resize(static_cast<size_t>(cnt.back()));
     {
         std::vector<int64_t> nx(cnt.begin(), cnt.end() - 1);
-        sweep([&](int64_t sl, Index k, Float w) {
+        parallel_rows([&](int64_t sl, Index k, Float w) {
             const int64_t d = nx[sl]++;
             p.w_col[d] = k;
             p.w_val[d] = w;

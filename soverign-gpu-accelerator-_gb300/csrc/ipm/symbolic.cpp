@@ -34,18 +34,32 @@ std::vector<std::vector<Index>> aat_graph(const core::CSRMatrix& A) {
     std::vector<Index> cptr, crow;
     column_rows(A, cptr, crow);
     std::vector<std::vector<Index>> adj(static_cast<size_t>(A.rows));
-    std::vector<Index> mark(static_cast<size_t>(A.rows), -1);
-    for (Index i = 0; i < A.rows; ++i) {
-        auto& ai = adj[static_cast<size_t>(i)];
-        mark[i] = i;
-        for (Index k = A.row_ptrs[i]; k < A.row_ptrs[i + 1]; ++k) {
-            const Index j = A.col_indices[k];
-            for (Index q = cptr[j]; q < cptr[j + 1]; ++q) {
-                const Index r = crow[q];
-                if (mark[r] != i) { mark[r] = i; ai.push_back(r); }
+    // rows are independent: ranges of rows on worker threads, each with its own marks
+    auto rows = [&](Index i0, Index i1) {
+        std::vector<Index> mark(static_cast<size_t>(A.rows), -1);
+        for (Index i = i0; i < i1; ++i) {
+            auto& ai = adj[static_cast<size_t>(i)];
+            mark[i] = i;
+            for (Index k = A.row_ptrs[i]; k < A.row_ptrs[i + 1]; ++k) {
+                const Index j = A.col_indices[k];
+                for (Index q = cptr[j]; q < cptr[j + 1]; ++q) {
+                    const Index r = crow[q];
+                    if (mark[r] != i) { mark[r] = i; ai.push_back(r); }
+                }
             }
+            std::sort(ai.begin(), ai.end());
         }
-        std::sort(ai.begin(), ai.end());
+    };
+    const int nt = A.rows >= 4096 ? static_cast<int>(std::max(1u, std::min(16u, std::thread::hardware_concurrency())))
+                                  : 1;
+    if (nt == 1) {
+        rows(0, A.rows);
+    } else {
+        std::vector<std::thread> pool;
+        for (int t = 0; t < nt; ++t)
+            pool.emplace_back(rows, static_cast<Index>(static_cast<int64_t>(A.rows) * t / nt),
+                              static_cast<Index>(static_cast<int64_t>(A.rows) * (t + 1) / nt));
+        for (auto& th : pool) th.join();
     }
     return adj;
 }
