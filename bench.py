@@ -58,8 +58,9 @@ def cpu_sample(sk):
 class Clocks:
     def __init__(self):
         self.p = None
-        self.path = os.path.join(ROOT, "gpurun_out", "bench_clocks.csv") if os.path.isdir(
-            os.path.join(ROOT, "gpurun_out")) else "/tmp/bench_clocks.csv"
+        import tempfile
+        # nvidia-smi samples of the timed region (path overridable for keeping the record)
+        self.path = os.environ.get("SK_BENCH_CLOCKS", os.path.join(tempfile.gettempdir(), "sk_bench_clocks.csv"))
 
     def start(self):
         try:

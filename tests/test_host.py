@@ -121,3 +121,39 @@ def test_invalid_lp_arrays_rejected_before_device(sk):
     bad.col_ptrs[0] = 1
     with pytest.raises(RuntimeError):
         sk.solve(bad)
+
+
+def _cuda_visible():
+    try:
+        rt = ctypes.CDLL("libcudart.so")
+        n = ctypes.c_int(0)
+        return rt.cudaGetDeviceCount(ctypes.byref(n)) == 0 and n.value > 0
+    except OSError:
+        return False
+
+
+def test_spmv_plan_rejects_bad_arguments_before_the_device(sk):
+    L = sk.lib()
+    out = ctypes.c_void_p()
+    vp = ctypes.c_void_p
+    # negative sizes, missing row pointers, missing output handle: SK_ERR_INVALID (1)
+    assert L.sk_spmv_plan_create(-1, 5, 0, vp(8), None, None, None, ctypes.byref(out)) == 1
+    assert L.sk_spmv_plan_create(5, 5, 3, None, vp(8), vp(8), None, ctypes.byref(out)) == 1
+    assert L.sk_spmv_plan_create(5, 5, 3, vp(8), vp(8), vp(8), None, None) == 1
+    assert L.sk_spmv_plan_execute(None, vp(8), 1.0, 0.0, vp(8), None) == 1
+    assert L.sk_spmv_plan_set_group(None, 4, 0) == 1
+    # a well-formed empty plan (no rows: no device memory is read): SK_ERR_NO_DEVICE (4) without a
+    # device, no fallback; with a device it is created and destroyed
+    rc = L.sk_spmv_plan_create(0, 5, 0, vp(8), None, None, None, ctypes.byref(out))
+    if _cuda_visible():
+        assert rc == 0
+        L.sk_spmv_plan_destroy(out)
+    else:
+        assert rc == 4
+
+
+def test_presolve_and_spmv_plan_symbols_declared(sk):
+    names = declared_symbols()
+    for n in ("sk_presolve_ruiz", "sk_spmv_plan_create", "sk_spmv_plan_execute", "sk_spmv_plan_info",
+              "sk_spmv_plan_set_group", "sk_spmv_plan_destroy"):
+        assert n in names
