@@ -6,6 +6,7 @@
 #include <numeric>
 #include <stdexcept>
 #include <exception>
+#include <functional>
 #include <mutex>
 #include <thread>
 #include <vector>
@@ -103,27 +104,46 @@ void permuted_lower_pattern(const core::CSRMatrix& A, const std::vector<Index>& 
     for (Index i = 0; i < m; ++i) P[P_inv[i]] = i;
     rowptr.assign(static_cast<size_t>(m) + 1, 0);
     colidx.clear();
-    std::vector<Index> mark(static_cast<size_t>(m), -1);
-    std::vector<Index> row;
-    for (Index k = 0; k < m; ++k) {
-        const Index i = P[k];
-        mark[i] = k;
-        row.clear();
-        for (Index q = A.row_ptrs[i]; q < A.row_ptrs[i + 1]; ++q) {
-            const Index j = A.col_indices[q];
-            for (Index t = cptr[j]; t < cptr[j + 1]; ++t) {
-                const Index r = crow[t];
-                if (mark[r] != k) {
-                    mark[r] = k;
-                    const Index pr = P_inv[r];
-                    if (pr < k) row.push_back(pr);
+    // rows are independent: contiguous ranges of permuted rows on worker threads, each
+    // building its part of the pattern, joined in row order
+    struct Part { std::vector<Index> ci; };
+    auto rows = [&](Index k0, Index k1, Part& out) {
+        std::vector<Index> mark(static_cast<size_t>(m), -1);
+        std::vector<Index> row;
+        for (Index k = k0; k < k1; ++k) {
+            const Index i = P[k];
+            mark[i] = k;
+            row.clear();
+            for (Index q = A.row_ptrs[i]; q < A.row_ptrs[i + 1]; ++q) {
+                const Index j = A.col_indices[q];
+                for (Index t = cptr[j]; t < cptr[j + 1]; ++t) {
+                    const Index r = crow[t];
+                    if (mark[r] != k) {
+                        mark[r] = k;
+                        const Index pr = P_inv[r];
+                        if (pr < k) row.push_back(pr);
+                    }
                 }
             }
+            std::sort(row.begin(), row.end());
+            out.ci.insert(out.ci.end(), row.begin(), row.end());
+            rowptr[k + 1] = static_cast<Index>(row.size());
         }
-        std::sort(row.begin(), row.end());
-        colidx.insert(colidx.end(), row.begin(), row.end());
-        rowptr[k + 1] = static_cast<Index>(colidx.size());
+    };
+    const int nt = m >= 4096 ? static_cast<int>(std::max(1u, std::min(16u, std::thread::hardware_concurrency()))) : 1;
+    std::vector<Part> parts(static_cast<size_t>(nt));
+    if (nt == 1) {
+        rows(0, m, parts[0]);
+    } else {
+        std::vector<std::thread> pool;
+        for (int t = 0; t < nt; ++t)
+            pool.emplace_back(rows, static_cast<Index>(static_cast<int64_t>(m) * t / nt),
+                              static_cast<Index>(static_cast<int64_t>(m) * (t + 1) / nt), std::ref(parts[t]));
+        for (auto& th : pool) th.join();
     }
+    for (Index k = 0; k < m; ++k) rowptr[k + 1] += rowptr[k];
+    colidx.reserve(static_cast<size_t>(rowptr[m]));
+    for (auto& pt : parts) colidx.insert(colidx.end(), pt.ci.begin(), pt.ci.end());
 }
 
 std::vector<Index> elimination_tree(Index m, const std::vector<Index>& rowptr,
