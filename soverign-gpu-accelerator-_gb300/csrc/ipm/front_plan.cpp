@@ -2,6 +2,7 @@
 #include "ipm/front_plan.hpp"
 
 #include <algorithm>
+#include <functional>
 #include <future>
 #include <thread>
 #include <numeric>
@@ -361,14 +362,34 @@ void build_front_plan(const std::vector<LpView>& lps, const core::CSRMatrix& A, 
     // 3. column counts by row-subtree traversal
     std::vector<int64_t> colcount(static_cast<size_t>(p.M), 1);
     {
-        std::vector<Index> mark(static_cast<size_t>(p.M), -1);
-        for (Index i = 0; i < p.M; ++i) {
-            mark[i] = i;
-            for (Index q = rp[i]; q < rp[i + 1]; ++q)
-                for (Index j = ci[q]; j != -1 && mark[j] != i; j = parent[j]) {
-                    mark[j] = i;
-                    colcount[j]++;
-                }
+        // row i adds one to every column on the paths from its entries up the tree; the
+        // rows split into ranges on worker threads with their own marks and counts,
+        // summed afterwards (integer counts: the same result in any order)
+        auto count_rows = [&](Index i0, Index i1, std::vector<int64_t>& cc) {
+            std::vector<Index> mark(static_cast<size_t>(p.M), -1);
+            for (Index i = i0; i < i1; ++i) {
+                mark[i] = i;
+                for (Index q = rp[i]; q < rp[i + 1]; ++q)
+                    for (Index j = ci[q]; j != -1 && mark[j] != i; j = parent[j]) {
+                        mark[j] = i;
+                        cc[j]++;
+                    }
+            }
+        };
+        const int nt = p.M >= 16384 ? static_cast<int>(std::max(1u, std::min(16u, std::thread::hardware_concurrency())))
+                                    : 1;
+        if (nt == 1) {
+            count_rows(0, p.M, colcount);
+        } else {
+            std::vector<std::vector<int64_t>> part(static_cast<size_t>(nt),
+                                                   std::vector<int64_t>(static_cast<size_t>(p.M), 0));
+            std::vector<std::thread> pool;
+            for (int t = 0; t < nt; ++t)
+                pool.emplace_back(count_rows, static_cast<Index>(static_cast<int64_t>(p.M) * t / nt),
+                                  static_cast<Index>(static_cast<int64_t>(p.M) * (t + 1) / nt), std::ref(part[t]));
+            for (auto& th : pool) th.join();
+            for (const auto& cc : part)
+                for (Index j = 0; j < p.M; ++j) colcount[j] += cc[j];
         }
     }
     std::vector<Index> nchild(static_cast<size_t>(p.M), 0);
