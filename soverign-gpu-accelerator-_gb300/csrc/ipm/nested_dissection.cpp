@@ -32,7 +32,7 @@ constexpr Index kUnset = -1;
 constexpr int kMinSideDiv = 5;      // each side of a separator holds at least 1/5 of the part
 constexpr Index kSlackNum = 11, kSlackDen = 10;   // a separator up to 10% wider wins when better balanced
 constexpr int kNoGain = 2;          // ball radii tried after the last narrower cut
-constexpr int kParallelDepth = 3;   // separators whose sides are dissected concurrently: 2^3 threads at most
+constexpr int kParallelDepth = 4;   // separators whose sides are dissected concurrently: 2^4 threads at most
 constexpr Index kParallelRows = 20000;
 
 // Minimum vertex cut through a band of vertices 0..nb-1 (adjacency inside the band
@@ -46,8 +46,26 @@ public:
     Index run(Index nb, const std::vector<Index>& ptr, const std::vector<Index>& adj, const std::vector<char>& src,
               const std::vector<char>& snk, std::vector<char>& side) {
         const Index N = 2 * nb + 2, S = 2 * nb, T = 2 * nb + 1;
-        head_.assign(static_cast<size_t>(N), kUnset);
-        to_.clear(); cap_.clear(); next_.clear();
+        // arcs in CSR form (each with its reverse residual arc): count, place, fill
+        off_.assign(static_cast<size_t>(N) + 1, 0);
+        auto count = [&](Index u, Index v) { off_[u + 1]++; off_[v + 1]++; };
+        for (Index b = 0; b < nb; ++b) {
+            count(2 * b, 2 * b + 1);
+            for (Index q = ptr[b]; q < ptr[b + 1]; ++q) count(2 * b + 1, 2 * adj[q]);
+            if (src[b]) count(S, 2 * b);
+            if (snk[b]) count(2 * b + 1, T);
+        }
+        for (Index u = 0; u < N; ++u) off_[u + 1] += off_[u];
+        const Index E = off_[N];
+        to_.resize(static_cast<size_t>(E));
+        cap_.resize(static_cast<size_t>(E));
+        rev_.resize(static_cast<size_t>(E));
+        it_.assign(off_.begin(), off_.end() - 1);
+        auto arc = [&](Index u, Index v, Index c) {
+            const Index e = it_[u]++, r = it_[v]++;
+            to_[e] = v; cap_[e] = c; rev_[e] = r;
+            to_[r] = u; cap_[r] = 0; rev_[r] = e;
+        };
         for (Index b = 0; b < nb; ++b) {
             arc(2 * b, 2 * b + 1, 1);
             for (Index q = ptr[b]; q < ptr[b + 1]; ++q) arc(2 * b + 1, 2 * adj[q], kBig);
@@ -58,10 +76,12 @@ public:
         it_.resize(static_cast<size_t>(N));
         Index flow = 0;
         while (levels(S, T, N)) {
-            for (Index u = 0; u < N; ++u) it_[u] = head_[u];
+            std::copy(off_.begin(), off_.end() - 1, it_.begin());
             while (augment(S, T)) ++flow;
         }
-        levels(S, T, N);   // reachability in the final residual graph
+        // reachability from S in the final residual graph: the source side of the
+        // minimum cut closest to S, the same for every maximum flow
+        levels(S, T, N);
         side.resize(static_cast<size_t>(nb));
         for (Index b = 0; b < nb; ++b)
             side[b] = lvl_[2 * b] < 0 ? 2 : (lvl_[2 * b + 1] < 0 ? 1 : 0);
@@ -70,12 +90,7 @@ public:
 
 private:
     static constexpr Index kBig = 0x3fffffff;
-    std::vector<Index> head_, to_, cap_, next_, lvl_, it_, queue_, path_;
-
-    void arc(Index u, Index v, Index c) {
-        to_.push_back(v); cap_.push_back(c); next_.push_back(head_[u]); head_[u] = static_cast<Index>(to_.size()) - 1;
-        to_.push_back(u); cap_.push_back(0); next_.push_back(head_[v]); head_[v] = static_cast<Index>(to_.size()) - 1;
-    }
+    std::vector<Index> off_, to_, cap_, rev_, lvl_, it_, queue_, path_;
 
     // Breadth-first distances from S over arcs with residual capacity; true if T is reached.
     bool levels(Index S, Index T, Index N) {
@@ -85,7 +100,7 @@ private:
         lvl_[S] = 0;
         for (size_t h = 0; h < queue_.size(); ++h) {
             const Index u = queue_[h];
-            for (Index e = head_[u]; e != kUnset; e = next_[e])
+            for (Index e = off_[u]; e < off_[u + 1]; ++e)
                 if (cap_[e] > 0 && lvl_[to_[e]] < 0) { lvl_[to_[e]] = lvl_[u] + 1; queue_.push_back(to_[e]); }
         }
         return lvl_[T] >= 0;
@@ -98,18 +113,18 @@ private:
         Index u = S;
         for (;;) {
             if (u == T) {
-                for (Index e : path_) { cap_[e] -= 1; cap_[e ^ 1] += 1; }
+                for (Index e : path_) { cap_[e] -= 1; cap_[rev_[e]] += 1; }
                 return true;
             }
             Index& e = it_[u];
-            while (e != kUnset && !(cap_[e] > 0 && lvl_[to_[e]] == lvl_[u] + 1)) e = next_[e];
-            if (e == kUnset) {
+            while (e < off_[u + 1] && !(cap_[e] > 0 && lvl_[to_[e]] == lvl_[u] + 1)) ++e;
+            if (e >= off_[u + 1]) {
                 lvl_[u] = kUnset;            // dead end for this phase
                 if (path_.empty()) return false;
                 const Index back = path_.back();
                 path_.pop_back();
-                u = to_[back ^ 1];
-                it_[u] = next_[it_[u]];
+                u = to_[rev_[back]];
+                ++it_[u];
                 continue;
             }
             path_.push_back(e);
