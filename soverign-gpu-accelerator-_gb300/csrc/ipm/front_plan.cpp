@@ -240,14 +240,29 @@ double factor_flops(const core::CSRMatrix& A, const std::vector<Index>& perm) {
     permuted_lower_pattern(A, iperm, rp, ci);
     const std::vector<Index> parent = elimination_tree(M, rp, ci);
     std::vector<int64_t> cc(static_cast<size_t>(M), 1);
-    std::vector<Index> mark(static_cast<size_t>(M), -1);
-    for (Index i = 0; i < M; ++i) {
-        mark[i] = i;
-        for (Index q = rp[i]; q < rp[i + 1]; ++q)
-            for (Index j = ci[q]; j != -1 && mark[j] != i; j = parent[j]) {
-                mark[j] = i;
-                cc[j]++;
-            }
+    auto count_rows = [&](Index i0, Index i1, std::vector<int64_t>& out) {
+        std::vector<Index> mark(static_cast<size_t>(M), -1);
+        for (Index i = i0; i < i1; ++i) {
+            mark[i] = i;
+            for (Index q = rp[i]; q < rp[i + 1]; ++q)
+                for (Index j = ci[q]; j != -1 && mark[j] != i; j = parent[j]) {
+                    mark[j] = i;
+                    out[j]++;
+                }
+        }
+    };
+    const int nt = M >= 16384 ? static_cast<int>(std::max(1u, std::min(16u, std::thread::hardware_concurrency()))) : 1;
+    if (nt == 1) {
+        count_rows(0, M, cc);
+    } else {      // per-thread integer counts, summed: the same counts as one sweep
+        std::vector<std::vector<int64_t>> part(static_cast<size_t>(nt), std::vector<int64_t>(static_cast<size_t>(M), 0));
+        std::vector<std::thread> pool;
+        for (int t = 0; t < nt; ++t)
+            pool.emplace_back(count_rows, static_cast<Index>(static_cast<int64_t>(M) * t / nt),
+                              static_cast<Index>(static_cast<int64_t>(M) * (t + 1) / nt), std::ref(part[t]));
+        for (auto& th : pool) th.join();
+        for (const auto& c : part)
+            for (Index j = 0; j < M; ++j) cc[j] += c[j];
     }
     double f = 0.0;
     for (Index j = 0; j < M; ++j) f += static_cast<double>(cc[j]) * static_cast<double>(cc[j]);
