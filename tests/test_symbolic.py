@@ -152,3 +152,13 @@ def test_family1_ordering_flops(sk):
     st = sk.plan_stats(lp)
     assert st["consistent"] == 1.0
     assert st["flops_factor"] <= 2.121e10 * 1.0001
+
+
+def test_family1_plan_is_pinned(sk):
+    # The automatic plan of the family-1 LP as the GB300 runs were measured with (constrained
+    # minimum degree, relaxed supernodes, Khatri-Rao map): the parallel host analysis must give
+    # exactly these integers whatever the thread count.
+    st = sk.plan_stats(sk.generate(1, 0))
+    want = {"supernodes": 2222, "levels": 8, "nnz_factor": 19714304, "flops_factor": 20996637444,
+            "front_entries": 170729700, "slots": 718906, "khatri_rao_entries": 1008000, "max_front_rows": 2000}
+    assert {k: int(st[k]) for k in want} == want
