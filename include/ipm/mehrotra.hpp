@@ -32,6 +32,7 @@ struct MehrotraOptions {
     int strict = 0;
     double delta32 = 1e-8;
     double delta64 = 1e-14;
+    int fp64_update = SK_FP64_UPDATE_AUTO;
     // false (default, as the reference): lb / ub of the model are ignored and x >= 0
     // is solved; true: the model's bounds are honoured through the host standard form
     // (core/standard_form.hpp).

@@ -71,6 +71,8 @@ void check_options(const sk_options& o) {
     if (o.criteria != SK_CRIT_RELATIVE && o.criteria != SK_CRIT_REFERENCE) throw std::invalid_argument("bad criteria");
     if (!(o.tol > 0.0) || o.max_iter < 0 || o.ruiz_passes < 0) throw std::invalid_argument("bad tolerance / limits");
     if (!(o.learned_accept >= 0.0)) throw std::invalid_argument("bad learned_accept");
+    if (o.fp64_update < SK_FP64_UPDATE_AUTO || o.fp64_update > SK_FP64_UPDATE_TENSOR)
+        throw std::invalid_argument("bad fp64_update");
     if (o.ordering < SK_ORDER_AUTO || o.ordering > SK_ORDER_DISSECTION) throw std::invalid_argument("bad ordering");
 }
 
@@ -396,6 +398,13 @@ int sk_kkt_get_factor(sk_kkt* k, double* L_dense, double* D) {
     } catch (...) {
         return api::status_of_current_exception();
     }
+}
+
+int sk_kkt_set_fp64_update(sk_kkt* k, int mode) {
+    api::clear_error();
+    if (!k || mode < SK_FP64_UPDATE_AUTO || mode > SK_FP64_UPDATE_TENSOR) return SK_ERR_INVALID;
+    k->eng->set_fp64_emulation(mode == SK_FP64_UPDATE_TENSOR);
+    return SK_OK;
 }
 
 void sk_kkt_destroy(sk_kkt* k) { delete k; }

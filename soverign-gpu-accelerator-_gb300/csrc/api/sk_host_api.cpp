@@ -91,6 +91,7 @@ void sk_options_default(sk_options* opt) {
     opt->delta32 = 1e-8;
     opt->delta64 = 1e-14;
     opt->learned_accept = 0.5;
+    opt->fp64_update = SK_FP64_UPDATE_AUTO;
 }
 
 int sk_lp_generate(int family, int instance, sk_lp** out) {

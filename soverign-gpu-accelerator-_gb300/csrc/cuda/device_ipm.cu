@@ -401,8 +401,14 @@ struct DeviceIPM::Impl {
     std::vector<LpResult> res;
     std::vector<char> active, user_start;
     std::vector<double> rp0, rd0, mu0;
-    int factorizations = 0, solves = 0, refine_steps = 0, precision_path = 0, last_pcg = 0, max_pcg_iter = 0;
+    int factorizations = 0, solves = 0, refine_steps = 0, precision_path = 0, last_pcg = 0;
     bool switched = false, used_fp32 = false;
+    // Per-LP precision of a mixed solve: sw[k] once LP k has moved to FP64 fronts for
+    // good; sw_now[k] the fronts LP k uses in the current factorisation (a start-point
+    // factorisation can fall back to FP64 without a permanent switch); pcg_k[k] the
+    // most PCG steps of LP k's solves in the current iteration.
+    std::vector<char> sw, sw_now;
+    std::vector<int> pcg_k;
     double solve_ms = 0.0, device_ms = 0.0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::vector<double> hx0, hy0, hs0;      // user start (scaled)
@@ -703,6 +709,9 @@ void DeviceIPM::run() {
     I.used_fp32 = false;
     I.res.assign(nlp, LpResult());
     I.active.assign(nlp, 1);
+    I.sw.assign(nlp, o.precision == SK_PREC_FP64 ? 1 : 0);
+    I.sw_now = I.sw;
+    I.pcg_k.assign(nlp, 0);
     K.set_active(I.active);
     I.rp0.assign(nlp, 1.0);
     I.rd0.assign(nlp, 1.0);
@@ -767,6 +776,7 @@ void DeviceIPM::run() {
         std::vector<double> rn = resid_norm(rhs, out);
         std::vector<char> done(nlp, 0), stag(nlp, 0);
         I.last_pcg = 0;
+        std::vector<int> steps(nlp, 0);
         for (int k = 0; k < nlp; ++k) done[k] = !I.active[k] || rn[k] <= tol[k];
         if (o.strict) {
             for (int it = 0; it < 10; ++it) {
@@ -797,7 +807,9 @@ void DeviceIPM::run() {
             bool any = false;
             for (int k = 0; k < nlp; ++k) any |= !done[k];
             if (any) {
-                const int max_it = K.last_fp32() ? 30 : 60;
+                // PCG steps per LP: 30 on FP32 fronts, 60 on FP64 fronts
+                auto limit = [&](int k) { return I.sw_now[k] ? 60 : 30; };
+                const int max_it = 60;
                 std::vector<double> best = rn, rz(nlp, 0.0), al(nlp, 0.0), be(nlp, 0.0), imp(nlp, 0.0);
                 SK_CUDA(cudaMemcpyAsync(I.bak.ptr, out, sizeof(double) * M, cudaMemcpyDeviceToDevice, st));
                 K.apply_inverse(I.r.ptr, I.pz.ptr);
@@ -814,7 +826,9 @@ void DeviceIPM::run() {
                     for (int k = 0; k < nlp; ++k) {
                         al[k] = 0.0;
                         if (done[k] || stag[k]) continue;
+                        if (it >= limit(k)) { stag[k] = 1; continue; }
                         if (!(pq[k] > 0.0) || !(rz[k] > 0.0) || !std::isfinite(pq[k])) { stag[k] = 1; continue; }
+                        steps[k] = it + 1;
                         al[k] = rz[k] / pq[k];
                         run = true;
                     }
@@ -851,6 +865,7 @@ void DeviceIPM::run() {
                 SK_CUDA(cudaMemcpyAsync(out, I.bak.ptr, sizeof(double) * M, cudaMemcpyDeviceToDevice, st));
                 rn = resid_norm(rhs, out);
                 I.last_pcg = last_best_it + 1;
+                for (int k = 0; k < nlp; ++k) I.pcg_k[k] = std::max(I.pcg_k[k], steps[k]);
                 if (o.verbose > 1)
                     std::fprintf(stderr, "[sk]   pcg steps %d resid %.3e tol %.3e\n", last_best_it + 1, rn[0], tol[0]);
             }
@@ -867,8 +882,12 @@ void DeviceIPM::run() {
     // FP32 trailing updates run on the tensor cores (TF32 x3) while mu >= kTensorMu; the
     // last FP32 iterations, whose directions decide the FP64 switch, use exact FP32.
     bool tensor_now = true;
-    auto factor = [&](bool want_fp32) -> bool {
+    // One precision's fronts (the LPs of that precision's mask) through the delta ladder.
+    const bool emulate64 = o.fp64_update == SK_FP64_UPDATE_TENSOR ||
+                           (o.fp64_update == SK_FP64_UPDATE_AUTO && o.precision == SK_PREC_MIXED);
+    auto ladder = [&](bool want_fp32) -> bool {
         K.set_tensor_update(tensor_now);
+        K.set_fp64_emulation(emulate64);
         double delta = want_fp32 ? o.delta32 : (o.strict ? 1e-9 : o.delta64);
         for (int retry = 0; retry < (o.strict ? 5 : 6); ++retry, delta *= 10.0) {
             ++I.factorizations;
@@ -878,6 +897,65 @@ void DeviceIPM::run() {
             }
         }
         return false;
+    };
+    auto any_of = [&](const std::vector<char>& v) {
+        for (char c : v) if (c) return true;
+        return false;
+    };
+    auto masks_now = [&](std::vector<char>& on32, std::vector<char>& on64) {
+        on32.assign(nlp, 0);
+        on64.assign(nlp, 0);
+        for (int k = 0; k < nlp; ++k) if (I.active[k]) (I.sw_now[k] ? on64 : on32)[k] = 1;
+    };
+    auto mark_switch = [&](int k, int it) {
+        I.sw[k] = I.sw_now[k] = 1;
+        I.switched = true;
+        if (I.res[k].switch_iteration < 0) I.res[k].switch_iteration = it;
+    };
+    // Factors every active LP: FP32 fronts for the LPs not (yet) switched, FP64 fronts
+    // for the others. When the FP32 ladder fails, the LP whose pivot failed moves to
+    // FP64 fronts (up to four LPs one by one, then all that remain); with `sticky`
+    // false that move lasts for this factorisation only (start points). Returns false
+    // when the FP64 ladder fails.
+    auto factor_all = [&](int it, bool sticky) -> bool {
+        I.sw_now = I.sw;
+        std::vector<char> on32, on64;
+        masks_now(on32, on64);
+        const std::vector<char> none(nlp, 0);
+        int single = 0;
+        while (any_of(on32)) {
+            K.set_masks(on32, none);
+            if (ladder(true)) break;
+            const int k = K.failed_lp();
+            std::vector<char> move(nlp, 0);
+            if (k >= 0 && k < nlp && on32[k] && single < 4) { move[k] = 1; ++single; }
+            else move = on32;
+            for (int q = 0; q < nlp; ++q) {
+                if (!move[q]) continue;
+                if (o.verbose) std::fprintf(stderr, "[sk] lp %d: FP32 factorisation failed, FP64 fronts\n", q);
+                if (sticky) mark_switch(q, it);
+                else I.sw_now[q] = 1;
+                on32[q] = 0;
+            }
+        }
+        masks_now(on32, on64);
+        if (any_of(on64)) {
+            K.set_masks(on32, on64);
+            if (!ladder(false)) return false;
+        }
+        K.set_masks(on32, on64);
+        return true;
+    };
+    // Moves the LPs in `which` to FP64 fronts now and factors them alone (the other
+    // LPs' factors stay as they are).
+    auto switch_lps = [&](const std::vector<char>& which, int it) -> bool {
+        for (int k = 0; k < nlp; ++k) if (which[k]) mark_switch(k, it);
+        std::vector<char> on32, on64;
+        masks_now(on32, on64);
+        K.set_masks(on32, which);
+        const bool ok = ladder(false);
+        K.set_masks(on32, on64);
+        return ok;
     };
     // ---- direction: solve for rkkt -> (dx, dy, ds) and check it (mehrotra_device.cu:494-587).
     // acc[k]: the solve met its tolerance and e1, e2, e3 <= 1e-8 (the reference's test);
@@ -914,7 +992,7 @@ void DeviceIPM::run() {
                 if (I.active[k])
                     std::fprintf(stderr, "[sk]   dir lp %d solved %d e1 %.2e e2 %.2e e3 %.2e ratio_x %.3e ratio_s %.3e tol %.2e %s\n",
                                  k, (int)solved[k], ds_.e1[k], ds_.e2[k], ds_.e3[k], ds_.rx[k], ds_.rs[k], tol[k],
-                                 K.last_fp32() ? "fp32" : "fp64");
+                                 I.sw_now[k] ? "fp64" : "fp32");
         for (int k = 0; k < nlp; ++k) {
             const double e = std::max(ds_.e1[k], std::max(ds_.e2[k], ds_.e3[k]));
             const bool fin = std::isfinite(ds_.e1[k]) && std::isfinite(ds_.e2[k]) && std::isfinite(ds_.e3[k]) &&
@@ -922,15 +1000,6 @@ void DeviceIPM::run() {
             acc[k] = solved[k] && fin && e <= 1e-8;
             use[k] = o.strict ? acc[k] : (fin && e <= kUseDir);
         }
-    };
-    auto any_active_missing = [&](const std::vector<char>& v) {
-        for (int k = 0; k < nlp; ++k) if (I.active[k] && !v[k]) return true;
-        return false;
-    };
-    auto switch_to_fp64 = [&](int it) -> bool {
-        I.switched = true;
-        for (int k = 0; k < nlp; ++k) if (I.active[k] && I.res[k].switch_iteration < 0) I.res[k].switch_iteration = it;
-        return factor(false);
     };
 
     if (o.start == SK_START_MEHROTRA || o.start == SK_START_LEARNED) {
@@ -940,8 +1009,7 @@ void DeviceIPM::run() {
         std::vector<double> one(nlp, 1.0);
         I.put_scalars(0, one);
         k_fill<<<nblk(N), 256, 0, st>>>(N, I.theta.ptr, 1.0);
-        const bool f32 = o.precision == SK_PREC_MIXED;
-        if (!factor(f32) && !(f32 && factor(false)))
+        if (!factor_all(0, false))
             throw api::sk_exception(SK_ERR_NUMERICAL, "heuristic start: A A^T could not be factored");
         for (int k = 0; k < nlp; ++k) tol[k] = 1e-10;
         std::vector<char> ok;
@@ -990,8 +1058,7 @@ void DeviceIPM::run() {
             std::vector<double> one(nlp, 1.0);
             I.put_scalars(0, one);
             k_theta<<<nblk(N), 256, 0, st>>>(N, I.x.ptr, I.s.ptr, I.col_lp.ptr, d_mask, I.theta.ptr);
-            const bool f32 = o.precision == SK_PREC_MIXED;
-            if (!factor(f32) && !(f32 && factor(false)))
+            if (!factor_all(0, false))
                 throw api::sk_exception(SK_ERR_NUMERICAL, "learned start: A Theta A^T could not be factored");
             for (int k = 0; k < nlp; ++k) tol[k] = 1e-8;
             std::vector<char> ok;
@@ -1111,7 +1178,7 @@ void DeviceIPM::run() {
             }
             if (o.verbose)
                 std::fprintf(stderr, "[sk] lp %d iter %d rp %.3e rd %.3e mu %.3e gap %.3e %s\n", k, iter, nrp[k],
-                             nrd[k], mu[k], r.rel_gap, I.switched || o.precision == SK_PREC_FP64 ? "fp64" : "fp32");
+                             nrd[k], mu[k], r.rel_gap, I.sw[k] ? "fp64" : "fp32");
             if (I.capture_mu > 0.0 && !I.captured[k] && (conv || mu[k] < I.capture_mu)) {
                 const int co = I.col_off[k], nk = I.col_off[k + 1] - co;
                 const int ro = I.row_off[k], mk = I.row_off[k + 1] - ro;
@@ -1127,24 +1194,23 @@ void DeviceIPM::run() {
         if (!any) break;
         for (int k = 0; k < nlp; ++k) mask[k] = I.active[k] ? 1.0 : 0.0;
         I.put_scalars(0, mask);
-        K.set_active(I.active);   // converged LPs' fronts are no longer factored or solved
+        // converged LPs' fronts are no longer factored or solved (factor_all sets the masks)
         k_theta<<<nblk(N), 256, 0, st>>>(N, I.x.ptr, I.s.ptr, I.col_lp.ptr, d_mask, I.theta.ptr);
-        // precision for this iteration
-        tensor_now = mumax >= kTensorMu;
-        bool fp32 = o.precision == SK_PREC_MIXED && !I.switched && mumax >= o.mu_switch;
-        if (o.precision == SK_PREC_MIXED && !I.switched && !fp32) {
-            if (o.verbose) std::fprintf(stderr, "[sk] FP64 fronts from iter %d: mu below mu_switch\n", iter);
-            I.switched = true;
-            for (int k = 0; k < nlp; ++k) if (I.active[k]) I.res[k].switch_iteration = iter;
+        // precision of each LP for this iteration: FP64 fronts once its mu is below mu_switch
+        (void)mumax;
+        double mu32 = 0.0;
+        for (int k = 0; k < nlp; ++k) {
+            if (!I.active[k] || I.sw[k]) continue;
+            if (mu[k] < o.mu_switch) {
+                if (o.verbose) std::fprintf(stderr, "[sk] lp %d: FP64 fronts from iter %d (mu below mu_switch)\n", k, iter);
+                mark_switch(k, iter);
+                continue;
+            }
+            mu32 = std::max(mu32, mu[k]);
         }
-        bool ok_fac = factor(fp32);
-        if (!ok_fac && fp32) {
-            if (o.verbose) std::fprintf(stderr, "[sk] FP64 fronts from iter %d: FP32 factorisation failed\n", iter);
-            I.switched = true;
-            for (int k = 0; k < nlp; ++k) if (I.active[k]) I.res[k].switch_iteration = iter;
-            fp32 = false;
-            ok_fac = factor(false);
-        }
+        tensor_now = mu32 >= kTensorMu;
+        std::fill(I.pcg_k.begin(), I.pcg_k.end(), 0);
+        const bool ok_fac = factor_all(iter, true);
         if (!ok_fac) {   // the reference throws here (kkt.cu:600-602); report a numerical stop
             for (int k = 0; k < nlp; ++k) if (I.active[k]) { I.res[k].status = SK_STATUS_ITERATION_LIMIT; I.active[k] = 0; }
             break;
@@ -1153,28 +1219,39 @@ void DeviceIPM::run() {
         // ---------------- predictor
         DirStats pd;
         std::vector<char> acc_p, use_p;
-        bool fac_ok = true, tightened = false;
+        bool fac_ok = true;
         // An FP32 direction that misses the check is first recomputed with the same
-        // factor and a 100x tighter PCG target; only a second miss moves to FP64 fronts.
-        auto tighten = [&](const std::vector<char>& acc) {
-            if (tightened) return false;
-            tightened = true;
-            for (int k = 0; k < nlp; ++k) if (I.active[k] && !acc[k]) tol[k] *= 0.01;
-            return true;
+        // factor and a 100x tighter PCG target; an LP whose direction misses again moves
+        // to FP64 fronts (alone: the other LPs keep their precision).
+        std::vector<char> tightened(nlp, 0);
+        auto retry_fp32_misses = [&](const std::vector<char>& acc, const char* what) -> int {
+            // returns 0: nothing to redo; 1: redo the direction; -1: FP64 factorisation failed
+            std::vector<char> now(nlp, 0);
+            bool redo = false, any_now = false;
+            for (int k = 0; k < nlp; ++k) {
+                if (!I.active[k] || I.sw[k] || acc[k]) continue;
+                redo = true;
+                if (!tightened[k]) { tightened[k] = 1; tol[k] *= 0.01; }
+                else { now[k] = 1; any_now = true; }
+            }
+            if (any_now) {
+                if (o.verbose)
+                    for (int k = 0; k < nlp; ++k)
+                        if (now[k])
+                            std::fprintf(stderr, "[sk] lp %d: FP64 fronts from iter %d (FP32 %s missed the accuracy, "
+                                         "pcg %d)\n", k, iter, what, I.pcg_k[k]);
+                if (!switch_lps(now, iter)) return -1;
+            }
+            return redo ? 1 : 0;
         };
         for (int attempt = 0; attempt < 3; ++attempt) {
             k_rhs<<<nblk(N), 256, 0, st>>>(N, I.x.ptr, I.s.ptr, I.theta.ptr, I.rd.ptr, nullptr, nullptr, nullptr,
                                           I.col_lp.ptr, I.rxs.ptr, I.v.ptr);
             direction(I.dxa.ptr, I.dya.ptr, I.dsa.ptr, I.rxs.ptr, acc_p, use_p, pd);
-            I.max_pcg_iter = std::max(tightened ? I.max_pcg_iter : 0, I.last_pcg);
-            if (!fp32 || !any_active_missing(acc_p)) break;
-            if (tighten(acc_p)) continue;
-            // an FP32 direction missed the reference accuracy: FP64 factor from here on
-            if (o.verbose)
-                std::fprintf(stderr, "[sk] FP64 fronts from iter %d: FP32 predictor missed the accuracy (pcg %d)\n",
-                             iter, I.last_pcg);
-            fp32 = false;
-            if (!(fac_ok = switch_to_fp64(iter))) break;
+            if (attempt == 2) break;
+            const int r = retry_fp32_misses(acc_p, "predictor");
+            if (r < 0) { fac_ok = false; break; }
+            if (r == 0) break;
         }
         if (!fac_ok) {
             for (int k = 0; k < nlp; ++k) if (I.active[k]) { I.res[k].status = SK_STATUS_ITERATION_LIMIT; I.active[k] = 0; }
@@ -1200,21 +1277,17 @@ void DeviceIPM::run() {
             k_rhs<<<nblk(N), 256, 0, st>>>(N, I.x.ptr, I.s.ptr, I.theta.ptr, I.rd.ptr, I.dxa.ptr, I.dsa.ptr, d_tgt,
                                           I.col_lp.ptr, I.rxs.ptr, I.v.ptr);
             direction(I.dx.ptr, I.dy.ptr, I.ds.ptr, I.rxs.ptr, acc_c, okc, cd);
-            I.max_pcg_iter = std::max(I.max_pcg_iter, I.last_pcg);
-            if (!fp32 || !any_active_missing(acc_c)) break;
-            if (tighten(acc_c)) continue;
-            if (o.verbose)
-                std::fprintf(stderr, "[sk] FP64 fronts from iter %d: FP32 corrector missed the accuracy (pcg %d)\n",
-                             iter, I.last_pcg);
-            fp32 = false;
-            if (!switch_to_fp64(iter)) { okc.assign(nlp, 0); break; }
+            if (attempt == 2) break;
+            const int r = retry_fp32_misses(acc_c, "corrector");
+            if (r < 0) { okc.assign(nlp, 0); break; }
+            if (r == 0) break;
         }
         // FP32 fronts that needed many PCG steps are not worth keeping: FP64 from the next iteration
-        if (fp32 && I.max_pcg_iter > 20) {
+        for (int k = 0; k < nlp; ++k) {
+            if (!I.active[k] || I.sw[k] || I.pcg_k[k] <= 20) continue;
             if (o.verbose)
-                std::fprintf(stderr, "[sk] FP64 fronts from iter %d: %d PCG steps\n", iter + 1, I.max_pcg_iter);
-            I.switched = true;
-            for (int k = 0; k < nlp; ++k) if (I.active[k] && I.res[k].switch_iteration < 0) I.res[k].switch_iteration = iter + 1;
+                std::fprintf(stderr, "[sk] lp %d: FP64 fronts from iter %d (%d PCG steps)\n", k, iter + 1, I.pcg_k[k]);
+            mark_switch(k, iter + 1);
         }
         const double eta = 0.995, armijo = 1e-4;
         std::vector<int> dir(nlp, 0), bt(nlp, 0);

@@ -51,6 +51,8 @@ struct StepArgs {
     int tp_off;   // trsm prefix offset
     int up_off;   // update prefix offset (64x64 tiles)
     int up2_off;  // update prefix offset (128x128 blocks, tensor-core path)
+    int up3_off;  // update prefix offset (128x64 blocks, emulated FP64 path)
+    int dr_off;   // digit-row offsets of the items (emulated FP64 path)
 };
 
 
@@ -97,15 +99,18 @@ __global__ void __launch_bounds__(256) k_asm_diag_sparse(int M, const int64_t* _
     }
 }
 
+// Slots of LPs whose fronts are not being factored (lp_on 0) are left alone.
 template <class T>
 __global__ void k_asm_slots_sparse(int64_t nslots, int M, const int64_t* __restrict__ w_ptr,
                                    const int* __restrict__ w_col, const double* __restrict__ w_val,
                                    const double* __restrict__ theta, const int* __restrict__ si,
                                    const int* __restrict__ sj, const int64_t* __restrict__ pos,
                                    const double* __restrict__ Mdiag, const double* __restrict__ D,
-                                   const double* __restrict__ params, T* __restrict__ F) {
+                                   const double* __restrict__ params, const int* __restrict__ q_lp,
+                                   const int* __restrict__ lp_on, T* __restrict__ F) {
     const int64_t s = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (s >= nslots) return;
+    if (!lp_on[q_lp[s < M ? static_cast<int>(s) : si[s]]]) return;
     double v;
     if (s < M) {
         v = Mdiag[s] * D[s] * D[s] + params[0];
@@ -176,6 +181,7 @@ __global__ void k_asm_cols_dense(int M, const int* __restrict__ rp, const int* _
     if (warp >= M) return;
     const int j = warp;
     const int s = row_lp[j];
+    if (!pd.lp_on[s]) return;            // dense mode: front s is LP s
     const int first = pd.sn_first[s];
     const int N = pd.sn_nrows[s];
     T* col = F + pd.F_off[s] + static_cast<int64_t>(j - first) * pd.sn_lda[s] - first;
@@ -615,6 +621,15 @@ __global__ void __launch_bounds__(256, 1) k_update_tc(StepArgs a, const int* __r
         if (!done) {
             *fail = 1;
             atomicExch(err + 2, 1);
+            // Before the TMEM columns are freed below, give MMAs still in flight a
+            // second bounded wait: a CTA must free its TMEM before it exits, and
+            // freeing columns an MMA still writes could hand them to another CTA
+            // mid-write. The host turns err[2] into an error either way.
+            for (int spin = 0; spin < kTcSpin && !done; ++spin) {
+                asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n"
+                             " selp.u32 %0, 1, 0, p;\n}\n" : "=r"(done) : "r"(smem_addr(bar)) : "memory");
+                if (!done) __nanosleep(20);
+            }
         }
     }
     __syncthreads();
@@ -654,6 +669,286 @@ __global__ void __launch_bounds__(256, 1) k_update_tc(StepArgs a, const int* __r
     }
 }
 
+// ---- emulated FP64 trailing update on the tensor cores (BF16 digits) --------
+// FP64 fronts of the late iterations of a mixed-precision solve. Each trailing
+// row of the step's panel (its 64 L entries a_k) is written as
+//     a_k = sum_{i=0..6} d_ik 2^(E - 7 - 8 i),   E = floor(log2 max_k |a_k|),
+// with balanced base-256 digits (d_0 in [-256, 256], d_i in [-128, 127] for
+// i >= 1): 56 bits, the row to 2^-56 of its largest entry. Every digit is an
+// integer of at most 8 significant bits, exact in BF16 (k_oz_digits, once per
+// panel row). C -= A B^T is then the sum over digit pairs (i, j); the pairs of
+// one level L = i + j share the scale 2^(E_a + E_b - 14 - 8 L) and accumulate in
+// one FP32 TMEM accumulator. With K <= 64 each level sum is an integer below
+// 9 * 2^20 in magnitude (|d_0 e_0| <= 2^16, |d_0 e_j| <= 2^15, |d_i e_j| <= 2^14,
+// at most L + 1 pairs of 64 products), so the tensor cores add it exactly. Levels
+// 0..6 (28 pairs; the pairs beyond level 6 weigh below 2^-56 and are left out)
+// are combined in 64-bit integers, hi = levels 0..2 and lo = levels 3..6, and
+// applied with two FP64 FMAs per entry: C - hi 2^(Ea+Eb-30) - lo 2^(Ea+Eb-62).
+// This is the error-free splitting of Ozaki, Ogita, Oishi and Rump (2012) with
+// BF16 digits, exact FP32 tensor-core sums and an integer epilogue; the result
+// agrees with an FP64 product to about 2^-53 of sum_k |a_k| |b_k|.
+//
+// Digit layout (global and shared alike): per digit plane i, row q, column k at
+// byte i * plane + (q >> 3) * 1024 + (k >> 3) * 128 + (q & 7) * 16 + (k & 7) * 2:
+// the canonical K-major no-swizzle layout of 8-row x 16-byte core matrices, so a
+// block's 128 (or 64) consecutive rows are one contiguous bulk copy.
+
+constexpr int kOzDigits = 7;
+constexpr uint32_t kOzLbo = 128;                       // bytes between K-adjacent core matrices
+constexpr uint32_t kOzSbo = 1024;                      // bytes between 8-row groups (64 bf16 per row)
+constexpr size_t kOzA = 128 * 128;                     // one digit plane of 128 rows: 16 KB
+constexpr size_t kOzB = 64 * 128;                      // one digit plane of 64 rows: 8 KB
+constexpr size_t kOzSmem = kOzDigits * (kOzA + kOzB) + 64;
+constexpr int kOzSpin = 1 << 22;
+// instruction descriptor (kind::f16): D = F32 (bits 4-5 = 1), A = B = BF16 (bits 7-9, 10-12 = 1),
+// both K-major, N >> 3 at bits 17-22 (N = 64), M >> 4 at bits 24-28 (M = 128)
+constexpr uint32_t kOzIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
+
+__device__ __forceinline__ uint64_t oz_sdesc(uint32_t saddr) {
+    uint64_t d = static_cast<uint64_t>((saddr & 0x3FFFFu) >> 4);
+    d |= static_cast<uint64_t>(kOzLbo >> 4) << 16;
+    d |= static_cast<uint64_t>(kOzSbo >> 4) << 32;
+    d |= static_cast<uint64_t>(1) << 46;
+    return d;
+}
+__device__ __forceinline__ double oz_pow2(int p) {       // 2^p, 0 below the normal range
+    if (p < -1022) return 0.0;
+    return __longlong_as_double(static_cast<long long>(p + 1023) << 52);
+}
+__device__ __forceinline__ uint32_t oz_bf16(int d) {     // |d| <= 256: exact
+    return __float_as_uint(static_cast<float>(d)) >> 16;
+}
+__device__ __forceinline__ bool oz_wait(uint32_t bar) {
+    uint32_t done = 0;
+    for (int spin = 0; spin < kOzSpin && !done; ++spin) {
+        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n"
+                     " selp.u32 %0, 1, 0, p;\n}\n" : "=r"(done) : "r"(bar) : "memory");
+        if (!done) __nanosleep(20);
+    }
+    return done != 0;
+}
+
+// Digits of the step's trailing panel rows: one block per 64-row tile (the trsm
+// tiles), four threads per row with 16 columns each.
+__global__ void __launch_bounds__(256) k_oz_digits(StepArgs a, const int* __restrict__ items,
+                                                   const int* __restrict__ prefix, PlanDev pd,
+                                                   const double* __restrict__ F, unsigned char* __restrict__ dig,
+                                                   int* __restrict__ dexp, int64_t plane) {
+    __shared__ double smax[4][64];
+    const int i = find_item(prefix + a.tp_off, a.nitems, blockIdx.x);
+    const int s = items[a.item_off + i];
+    if (!pd.lp_on[pd.sn_lp[s]]) return;
+    const int lt = blockIdx.x - prefix[a.tp_off + i];
+    const int N = pd.sn_nrows[s], K = pd.sn_ncols[s], LD = pd.sn_lda[s];
+    const int k0 = a.k * T64;
+    const int w = min(T64, K - k0);
+    const int t0 = k0 + w;
+    const int r = threadIdx.x & 63, cg = threadIdx.x >> 6;
+    const int row = t0 + lt * T64 + r;
+    const bool rin = row < N;
+    const double* Fs = F + pd.F_off[s];
+    double v[16];
+    double mx = 0.0;
+#pragma unroll
+    for (int t = 0; t < 16; ++t) {
+        const int k = cg * 16 + t;
+        v[t] = (rin && k < w) ? Fs[row + static_cast<int64_t>(k0 + k) * LD] : 0.0;
+        mx = fmax(mx, fabs(v[t]));
+    }
+    smax[cg][r] = mx;
+    __syncthreads();
+    mx = fmax(fmax(smax[0][r], smax[1][r]), fmax(smax[2][r], smax[3][r]));
+    // E is held at -968 or above so that 2^(55 - E) stays a normal double (rows whose
+    // largest entry is below 2^-967 keep fewer digits; they do not matter next to 1)
+    const int E = mx > 0.0 ? max(ilogb(mx), -968) : 0;
+    const double mul = oz_pow2(55 - E);             // |v mul| < 2^56
+    uint32_t pk[kOzDigits][8];                      // 16 BF16 digits per plane, packed in pairs
+#pragma unroll
+    for (int t = 0; t < 16; t += 2) {
+        int d0[kOzDigits], d1[kOzDigits];
+        long long f0 = llrint(v[t] * mul), f1 = llrint(v[t + 1] * mul);
+#pragma unroll
+        for (int j = kOzDigits - 1; j >= 1; --j) {
+            int l0 = static_cast<int>(f0 & 255), l1 = static_cast<int>(f1 & 255);
+            f0 >>= 8;
+            f1 >>= 8;
+            if (l0 >= 128) { l0 -= 256; f0 += 1; }
+            if (l1 >= 128) { l1 -= 256; f1 += 1; }
+            d0[j] = l0;
+            d1[j] = l1;
+        }
+        d0[0] = static_cast<int>(f0);
+        d1[0] = static_cast<int>(f1);
+#pragma unroll
+        for (int j = 0; j < kOzDigits; ++j) pk[j][t >> 1] = oz_bf16(d0[j]) | (oz_bf16(d1[j]) << 16);
+    }
+    const int q = prefix[a.dr_off + i] + lt * T64 + r;
+    unsigned char* base = dig + static_cast<int64_t>(q >> 3) * 1024 + (q & 7) * 16;
+#pragma unroll
+    for (int j = 0; j < kOzDigits; ++j)
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+            *reinterpret_cast<uint4*>(base + j * plane + (cg * 2 + h) * 128) =
+                make_uint4(pk[j][4 * h], pk[j][4 * h + 1], pk[j][4 * h + 2], pk[j][4 * h + 3]);
+    if (cg == 0) dexp[q] = E;
+}
+
+// C(128 x 64) -= A B^T from the digit planes (one block of 256 threads per
+// 128-row x 64-column block of the trailing lower part; row block bi holds
+// column blocks 0..2bi+1). One thread stages the 14 planes with bulk copies and
+// issues the 112 MMAs (M=128, N=64, K=16; level L accumulates in TMEM columns
+// 64L..64L+63); every thread loads its C values meanwhile, then reads its row's
+// 7 accumulators for 32 columns and applies them. Every wait is bounded: on a
+// time-out the block records err[2], waits once more for what it issued, frees
+// its TMEM and leaves C untouched.
+__global__ void __launch_bounds__(256, 1) k_update_oz(StepArgs a, const int* __restrict__ items,
+                                                      const int* __restrict__ prefix, PlanDev pd, double* F,
+                                                      double* __restrict__ Linv, const int64_t* __restrict__ inv_off,
+                                                      const unsigned char* __restrict__ dig,
+                                                      const int* __restrict__ dexp, int64_t plane, int* err) {
+    extern __shared__ __align__(1024) unsigned char smraw[];
+    unsigned char* As = smraw;
+    unsigned char* Bs = smraw + kOzDigits * kOzA;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(Bs + kOzDigits * kOzB);   // [0] planes loaded, [1] MMAs done
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 2);
+    int* fail = reinterpret_cast<int*>(bar + 3);
+    const int i = find_item(prefix + a.up3_off, a.nitems, blockIdx.x);
+    const int s = items[a.item_off + i];
+    if (!pd.lp_on[pd.sn_lp[s]]) return;
+    const int lb = blockIdx.x - prefix[a.up3_off + i];
+    int bi = static_cast<int>((sqrt(4.0 * lb + 1.0) - 1.0) * 0.5);
+    while ((bi + 1) * (bi + 2) <= lb) ++bi;
+    while (bi * (bi + 1) > lb) --bi;
+    const int bj = lb - bi * (bi + 1);
+    const int N = pd.sn_nrows[s], K = pd.sn_ncols[s], LD = pd.sn_lda[s];
+    const int k0 = a.k * T64;
+    const int w = min(T64, K - k0);
+    const int t0 = k0 + w;
+    const int r0 = t0 + bi * 128, c0 = t0 + bj * T64;
+    if (c0 >= N) return;                              // the whole block: column block past the front
+    const int nra = min(128, N - r0), ncb = min(T64, N - c0);
+    const int qa = prefix[a.dr_off + i] + bi * 128, qb = prefix[a.dr_off + i] + bj * T64;
+    double* Fs = F + pd.F_off[s];
+    const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_addr(bar)));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_addr(bar + 1)));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        *fail = 0;
+    }
+    if (wid == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" :: "r"(smem_addr(tslot)));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tslot;
+    if (tid == 0) {
+        const uint32_t b0 = smem_addr(bar);
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                     :: "r"(b0), "r"(static_cast<uint32_t>(kOzDigits * (kOzA + kOzB))) : "memory");
+        for (int j = 0; j < kOzDigits; ++j) {
+            const unsigned char* ga = dig + j * plane + static_cast<int64_t>(qa >> 3) * 1024;
+            const unsigned char* gb = dig + j * plane + static_cast<int64_t>(qb >> 3) * 1024;
+            asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                         :: "r"(smem_addr(As + j * kOzA)), "l"(ga), "r"(static_cast<uint32_t>(kOzA)), "r"(b0)
+                         : "memory");
+            asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                         :: "r"(smem_addr(Bs + j * kOzB)), "l"(gb), "r"(static_cast<uint32_t>(kOzB)), "r"(b0)
+                         : "memory");
+        }
+        bool ok = oz_wait(b0);
+        if (ok) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t sa = smem_addr(As), sb = smem_addr(Bs);
+            for (int L = 0; L < kOzDigits; ++L) {
+                uint32_t acc = 0;
+                for (int da = (L > kOzDigits - 1 ? L - kOzDigits + 1 : 0); da <= L && da < kOzDigits; ++da) {
+                    const int db = L - da;
+                    for (int ks = 0; ks < T64 / 16; ++ks) {
+                        const uint64_t adesc = oz_sdesc(sa + da * static_cast<uint32_t>(kOzA) + ks * 2 * kOzLbo);
+                        const uint64_t bdesc = oz_sdesc(sb + db * static_cast<uint32_t>(kOzB) + ks * 2 * kOzLbo);
+                        asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                                     " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+                                     :: "r"(tmem + static_cast<uint32_t>(64 * L)), "l"(adesc), "l"(bdesc),
+                                        "r"(kOzIdesc), "r"(acc));
+                        acc = 1;
+                    }
+                }
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                         :: "r"(smem_addr(bar + 1)) : "memory");
+            ok = oz_wait(smem_addr(bar + 1));
+            if (!ok) oz_wait(smem_addr(bar + 1));     // a second bounded wait before TMEM is freed
+        } else {
+            oz_wait(b0);                               // copies still in flight: a second bounded wait
+        }
+        if (!ok) {
+            *fail = 1;
+            atomicExch(err + 2, 1);
+        }
+    }
+    // this thread's row (TMEM lane) and 32 columns, and its C values, loaded while the MMAs run
+    const int row = 32 * (wid & 3) + lane, ch = 32 * (wid >> 2);
+    const bool rok = row < nra;
+    double cv[32];
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+        const int col = ch + j;
+        const bool in = rok && col < ncb && r0 + row >= c0 + col;
+        cv[j] = in ? Fs[(r0 + row) + static_cast<int64_t>(c0 + col) * LD] : 0.0;
+    }
+    const int ea = rok ? dexp[qa + row] : 0;
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const bool ok = *fail == 0;
+    if (ok) {
+#pragma unroll
+        for (int c16 = 0; c16 < 2; ++c16) {
+            uint32_t v[kOzDigits][16];
+#pragma unroll
+            for (int L = 0; L < kOzDigits; ++L) {
+                const uint32_t taddr = tmem + (static_cast<uint32_t>(32 * (wid & 3)) << 16) +
+                                       static_cast<uint32_t>(64 * L + ch + 16 * c16);
+                asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                             : "=r"(v[L][0]), "=r"(v[L][1]), "=r"(v[L][2]), "=r"(v[L][3]), "=r"(v[L][4]),
+                               "=r"(v[L][5]), "=r"(v[L][6]), "=r"(v[L][7]), "=r"(v[L][8]), "=r"(v[L][9]),
+                               "=r"(v[L][10]), "=r"(v[L][11]), "=r"(v[L][12]), "=r"(v[L][13]), "=r"(v[L][14]),
+                               "=r"(v[L][15])
+                             : "r"(taddr));
+            }
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+                const int j = 16 * c16 + q, col = ch + j;
+                if (!(rok && col < ncb && r0 + row >= c0 + col)) continue;
+                long long lv[kOzDigits];
+#pragma unroll
+                for (int L = 0; L < kOzDigits; ++L) lv[L] = __float2int_rn(__uint_as_float(v[L][q]));
+                const long long hi = lv[0] * 65536LL + lv[1] * 256LL + lv[2];
+                const long long lo = lv[3] * 16777216LL + lv[4] * 65536LL + lv[5] * 256LL + lv[6];
+                const int eb = dexp[qb + col];
+                const double shi = oz_pow2(ea + eb - 30), slo = oz_pow2(ea + eb - 62);
+                Fs[(r0 + row) + static_cast<int64_t>(c0 + col) * LD] =
+                    fma(-static_cast<double>(hi), shi, fma(-static_cast<double>(lo), slo, cv[j]));
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (wid == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" :: "r"(tmem));
+    }
+    if (!ok) return;
+    // the block holding the first trailing diagonal tile factors it (as in k_update)
+    if (lb == 0 && t0 < K) {
+        __syncthreads();
+        potrf_tile<double>(s, a.k + 1, pd, F, Linv, inv_off, err, smraw);
+    }
+}
+
 template <class T>
 __global__ void k_extend_add(int item_off, int nitems, int prefix_off, const int* __restrict__ items,
                              const int* __restrict__ prefix, PlanDev pd, T* F) {
@@ -690,16 +985,35 @@ __global__ void k_permute_scale(int M, const int* __restrict__ perm, const doubl
     if (q < M) zp[q] = static_cast<T>(D[q] * src[perm[q]]);
 }
 
-// Rows of LPs whose fronts were skipped get 0.
+// Rows of the LPs in `own` receive D xp; rows of the LPs in `other` (the set the
+// other precision's pass serves; may be null) are left as they are; all other
+// rows get 0.
 template <class T>
 __global__ void k_unpermute_scale(int M, const int* __restrict__ perm, const double* __restrict__ D,
                                   const T* __restrict__ xp, const int* __restrict__ row_lp,
-                                  const int* __restrict__ lp_on, double* __restrict__ dst) {
+                                  const int* __restrict__ own, const int* __restrict__ other,
+                                  double* __restrict__ dst) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q < M) {
         const int r = perm[q];
-        dst[r] = lp_on[row_lp[r]] ? D[q] * static_cast<double>(xp[q]) : 0.0;
+        const int k = row_lp[r];
+        if (own[k]) dst[r] = D[q] * static_cast<double>(xp[q]);
+        else if (!other || !other[k]) dst[r] = 0.0;
     }
+}
+
+// Zeroes the fronts of the LPs being factored, one chunk of a front per block
+// (the fronts of other LPs keep their factors).
+constexpr int kZeroChunk = 8192;
+template <class T>
+__global__ void __launch_bounds__(256) k_zero_fronts(const int* __restrict__ zc_sn, const int* __restrict__ zc_len,
+                                                     const int64_t* __restrict__ zc_off, PlanDev pd,
+                                                     T* __restrict__ F) {
+    const int s = zc_sn[blockIdx.x];
+    if (!pd.lp_on[pd.sn_lp[s]]) return;
+    T* p = F + zc_off[blockIdx.x];
+    const int len = zc_len[blockIdx.x];
+    for (int i = threadIdx.x; i < len; i += blockDim.x) p[i] = T(0);
 }
 
 // Frontal right-hand sides of one level: one thread per front row, the row's own
@@ -1060,6 +1374,9 @@ static void set_smem_attrs() {
                                  static_cast<int>(2 * T64 * T64 * sizeof(T))));
     SK_CUDA(cudaFuncSetAttribute(k_update<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  static_cast<int>(potrf_smem(sizeof(T)))));
+    if (std::is_same<T, double>::value)
+        SK_CUDA(cudaFuncSetAttribute(k_update_oz, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     static_cast<int>(kOzSmem)));
 }
 
 KktEngine::KktEngine(const ipm::FrontPlan& plan, const DeviceLP& lp, cudaStream_t stream)
@@ -1132,7 +1449,27 @@ KktEngine::KktEngine(const ipm::FrontPlan& plan, const DeviceLP& lp, cudaStream_
         const Index r = p.perm[p.sn_first[s]];
         sn_lp[s] = static_cast<int>(std::upper_bound(p.row_off.begin(), p.row_off.end(), r) - p.row_off.begin()) - 1;
     }
-    lp_on_h_.assign(static_cast<size_t>(std::max(1, p.nlp)), 1);
+    sn_lp_h_ = sn_lp;
+    on32_h_.assign(static_cast<size_t>(std::max(1, p.nlp)), 1);
+    on64_h_ = on32_h_;
+    // LP of each permuted row
+    std::vector<int> q_lp(static_cast<size_t>(std::max<Index>(1, p.M)), 0);
+    for (Index q = 0; q < p.M; ++q)
+        q_lp[q] = static_cast<int>(std::upper_bound(p.row_off.begin(), p.row_off.end(), p.perm[q]) -
+                                   p.row_off.begin()) - 1;
+    // front-zeroing chunks (front, start, length), kZeroChunk entries at most
+    std::vector<int> zc_sn, zc_len;
+    std::vector<int64_t> zc_off;
+    for (int s = 0; s < p.ns; ++s) {
+        const int64_t size = static_cast<int64_t>(p.sn_lda[s]) * p.sn_nrows[s];
+        for (int64_t o = 0; o < size; o += kZeroChunk) {
+            zc_sn.push_back(s);
+            zc_off.push_back(p.sn_F_off[s] + o);
+            zc_len.push_back(static_cast<int>(std::min<int64_t>(kZeroChunk, size - o)));
+        }
+    }
+    nzc_ = static_cast<int64_t>(zc_sn.size());
+    if (zc_sn.empty()) { zc_sn.push_back(0); zc_off.push_back(0); zc_len.push_back(0); }
     auto rsv = [&](auto& slot, const auto& vec) { reserve(arena_, slot, vec.size()); };
     rsv(sn_first_, p.sn_first); rsv(sn_ncols_, p.sn_ncols); rsv(sn_nrows_, p.sn_nrows); rsv(sn_lda_, p.sn_lda); rsv(sn_parent_, p.sn_parent);
     rsv(rows_, p.rows); rsv(ea_map_, p.ea_map); rsv(ch_ptr_, p.ch_ptr); rsv(ch_list_, p.ch_list);
@@ -1143,7 +1480,8 @@ KktEngine::KktEngine(const ipm::FrontPlan& plan, const DeviceLP& lp, cudaStream_
     rsv(w_col_, p.w_col); rsv(w_val_, p.w_val); rsv(inv_off_, inv_off); rsv(blk_off_, blk_off);
     rsv(fwd_tasks_, ftask); rsv(bwd_tasks_, btask);
     rsv(g_dst_, g_dst); rsv(g_zp_, g_zp); rsv(g_ptr_, g_ptr); rsv(g_src_, g_src);
-    rsv(sn_lp_, sn_lp); rsv(lp_on_, lp_on_h_);
+    rsv(sn_lp_, sn_lp); rsv(on32_, on32_h_); rsv(on64_, on64_h_); rsv(q_lp_, q_lp);
+    rsv(zc_sn_, zc_sn); rsv(zc_len_, zc_len); rsv(zc_off_, zc_off);
     reserve(arena_, flags_, static_cast<size_t>(std::max(1, nflags_)));
     reserve(arena_, counters_, static_cast<size_t>(2 * std::max(1, p.nlevels)));
     reserve(arena_, solve_err_, 1);
@@ -1162,7 +1500,7 @@ KktEngine::KktEngine(const ipm::FrontPlan& plan, const DeviceLP& lp, cudaStream_
     bnd(ch_list_); bnd(perm_); bnd(sn_F_off_); bnd(sn_f_off_); bnd(sn_rows_off_); bnd(ea_off_); bnd(step_items_);
     bnd(step_prefix_); bnd(round_items_); bnd(round_prefix_); bnd(level_sn_); bnd(slot_pos_); bnd(w_ptr_);
     bnd(slot_i_); bnd(slot_j_); bnd(w_col_); bnd(w_val_); bnd(inv_off_); bnd(blk_off_); bnd(fwd_tasks_);
-    bnd(bwd_tasks_); bnd(g_dst_); bnd(g_zp_); bnd(g_ptr_); bnd(g_src_); bnd(sn_lp_); bnd(lp_on_); bnd(flags_); bnd(counters_); bnd(solve_err_); bnd(D_); bnd(Mdiag_);
+    bnd(bwd_tasks_); bnd(g_dst_); bnd(g_zp_); bnd(g_ptr_); bnd(g_src_); bnd(sn_lp_); bnd(on32_); bnd(on64_); bnd(q_lp_); bnd(zc_sn_); bnd(zc_len_); bnd(zc_off_); bnd(flags_); bnd(counters_); bnd(solve_err_); bnd(D_); bnd(Mdiag_);
     bnd(zp_); bnd(xp_); bnd(zsol_); bnd(fvec_); bnd(tn_); bnd(params_); bnd(err_);
     upload(sn_first_, p.sn_first, st_); upload(sn_ncols_, p.sn_ncols, st_); upload(sn_nrows_, p.sn_nrows, st_);
     upload(sn_lda_, p.sn_lda, st_);
@@ -1176,7 +1514,8 @@ KktEngine::KktEngine(const ipm::FrontPlan& plan, const DeviceLP& lp, cudaStream_
     upload(w_val_, p.w_val, st_); upload(inv_off_, inv_off, st_); upload(blk_off_, blk_off, st_);
     upload(fwd_tasks_, ftask, st_); upload(bwd_tasks_, btask, st_);
     upload(g_dst_, g_dst, st_); upload(g_zp_, g_zp, st_); upload(g_ptr_, g_ptr, st_); upload(g_src_, g_src, st_);
-    upload(sn_lp_, sn_lp, st_); upload(lp_on_, lp_on_h_, st_);
+    upload(sn_lp_, sn_lp, st_); upload(on32_, on32_h_, st_); upload(on64_, on64_h_, st_); upload(q_lp_, q_lp, st_);
+    upload(zc_sn_, zc_sn, st_); upload(zc_len_, zc_len, st_); upload(zc_off_, zc_off, st_);
     SK_CUDA(cudaMemsetAsync(solve_err_.ptr, 0, sizeof(int), st_));
     SK_CUDA(cudaStreamSynchronize(st_));
     set_smem_attrs<float>();
@@ -1184,16 +1523,16 @@ KktEngine::KktEngine(const ipm::FrontPlan& plan, const DeviceLP& lp, cudaStream_
 }
 
 KktEngine::~KktEngine() {
-    for (int q = 0; q < 3; ++q)
+    for (int q = 0; q < 4; ++q)
         if (gfac_[q]) cudaGraphExecDestroy(gfac_[q]);
     for (int q = 0; q < 2; ++q)
         if (gsol_[q]) cudaGraphExecDestroy(gsol_[q]);
 }
 
-PlanDev KktEngine::pd() const {
+PlanDev KktEngine::pd(bool fp32) const {
     return PlanDev{sn_first_.ptr, sn_ncols_.ptr, sn_nrows_.ptr, sn_lda_.ptr, sn_F_off_.ptr, sn_f_off_.ptr, sn_rows_off_.ptr,
                    rows_.ptr, ea_off_.ptr, ea_map_.ptr, ch_ptr_.ptr, ch_list_.ptr, sn_parent_.ptr, sn_lp_.ptr,
-                   lp_on_.ptr};
+                   fp32 ? on32_.ptr : on64_.ptr};
 }
 
 template <class T>
@@ -1202,8 +1541,9 @@ void KktEngine::launch_factor(T* F, T* Linv, Prof* prof) {
         if (prof) prof->timed(cls, f); else f();
     };
     const auto& p = plan_;
-    const PlanDev pdv = pd();
-    SK_CUDA(cudaMemsetAsync(F, 0, sizeof(T) * static_cast<size_t>(p.F_size), st_));
+    const PlanDev pdv = pd(std::is_same<T, float>::value);
+    if (nzc_ > 0)
+        k_zero_fronts<T><<<static_cast<int>(nzc_), 256, 0, st_>>>(zc_sn_.ptr, zc_len_.ptr, zc_off_.ptr, pdv, F);
     SK_CUDA(cudaMemsetAsync(err_.ptr, 0, 4 * sizeof(int), st_));
     const double* theta = theta_bound_;
     run(0, [&] {
@@ -1218,13 +1558,14 @@ void KktEngine::launch_factor(T* F, T* Linv, Prof* prof) {
                                     Mdiag_.ptr, D_.ptr);
             k_asm_slots_sparse<T><<<blocks_for(p.nslots, 256), 256, 0, st_>>>(
                 p.nslots, p.M, w_ptr_.ptr, w_col_.ptr, w_val_.ptr, theta, slot_i_.ptr, slot_j_.ptr, slot_pos_.ptr,
-                Mdiag_.ptr, D_.ptr, params_.ptr, F);
+                Mdiag_.ptr, D_.ptr, params_.ptr, q_lp_.ptr, pdv.lp_on, F);
         }
     });
     for (int l = 0; l < p.nlevels; ++l) {
         for (int q = p.step_level_ptr[l]; q < p.step_level_ptr[l + 1]; ++q) {
             const auto& st = p.steps[q];
-            StepArgs a{st.k, st.item_off, st.nitems, st.trsm_prefix_off, st.upd_prefix_off, st.upd2_prefix_off};
+            StepArgs a{st.k,           st.item_off,         st.nitems,           st.trsm_prefix_off,
+                       st.upd_prefix_off, st.upd2_prefix_off, st.upd3_prefix_off, st.digit_row_off};
             if (st.k == 0)   // later diagonal tiles are factored by the previous step's update
                 run(1, [&] {
                     k_potrf<T><<<st.nitems, 256, potrf_smem(sizeof(T)), st_>>>(a, step_items_.ptr, pdv, F, Linv,
@@ -1243,6 +1584,16 @@ void KktEngine::launch_factor(T* F, T* Linv, Prof* prof) {
                             tc = true;
                             k_update_tc<<<static_cast<int>(st.upd2_blocks), 256, kTcSmem, st_>>>(
                                 a, step_items_.ptr, step_prefix_.ptr, pdv, F, Linv, inv_off_.ptr, err_.ptr);
+                        }
+                    } else {
+                        if (emulate64_) {
+                            tc = true;
+                            const int64_t plane = plan_.max_digit_rows * 128;
+                            k_oz_digits<<<static_cast<int>(st.trsm_tiles), 256, 0, st_>>>(
+                                a, step_items_.ptr, step_prefix_.ptr, pdv, F, dig_.ptr, dexp_.ptr, plane);
+                            k_update_oz<<<static_cast<int>(st.upd3_blocks), 256, kOzSmem, st_>>>(
+                                a, step_items_.ptr, step_prefix_.ptr, pdv, F, Linv, inv_off_.ptr, dig_.ptr,
+                                dexp_.ptr, plane, err_.ptr);
                         }
                     }
                     if (!tc)
@@ -1277,7 +1628,7 @@ void KktEngine::launch_solve(const T* F, const T* Linv, Prof* prof) {
         if (prof) prof->timed(cls, f); else f();
     };
     const auto& p = plan_;
-    const PlanDev pdv = pd();
+    const PlanDev pdv = pd(std::is_same<T, float>::value);
     T* zp = reinterpret_cast<T*>(zp_.ptr);
     T* xp = reinterpret_cast<T*>(xp_.ptr);
     T* zs = reinterpret_cast<T*>(zsol_.ptr);
@@ -1333,9 +1684,20 @@ void KktEngine::ensure_fronts(bool fp32) {
     }
 }
 
+void KktEngine::ensure_digits() {
+    if (dig_.ptr || plan_.max_digit_rows <= 0) return;
+    dig_arena_.reset();
+    reserve(dig_arena_, dig_, static_cast<size_t>(kOzDigits) * static_cast<size_t>(plan_.max_digit_rows) * 128);
+    reserve(dig_arena_, dexp_, static_cast<size_t>(plan_.max_digit_rows));
+    dig_arena_.commit();
+    bind(dig_arena_, dig_);
+    bind(dig_arena_, dexp_);
+}
+
 bool KktEngine::factor(const double* d_theta, double delta, bool fp32) {
-    const int q = fp32 ? (tensor_ ? 2 : 1) : 0;
+    const int q = fp32 ? (tensor_ ? 2 : 1) : (emulate64_ ? 3 : 0);
     ensure_fronts(fp32);
+    if (!fp32 && emulate64_) ensure_digits();
     fp32_ = fp32;
     double hp[4] = {delta, 0, 0, 0};
     SK_CUDA(cudaMemcpyAsync(params_.ptr, hp, sizeof(hp), cudaMemcpyHostToDevice, st_));
@@ -1354,40 +1716,85 @@ bool KktEngine::factor(const double* d_theta, double delta, bool fp32) {
     int herr[3];
     SK_CUDA(cudaMemcpyAsync(herr, err_.ptr, sizeof(herr), cudaMemcpyDeviceToHost, st_));
     SK_CUDA(cudaStreamSynchronize(st_));
-    if (herr[2]) throw std::runtime_error("tensor-core update: an MMA did not complete in time");
+    if (herr[2]) throw std::runtime_error("tensor-core update: a copy or an MMA did not complete in time");
     failed_sn_ = herr[0] ? herr[1] : -1;
     return herr[0] == 0;
 }
 
-void KktEngine::apply_inverse(const double* d_src, double* d_dst) {
+// One precision's solve: permute and scale src, the level-scheduled triangular
+// solves of that precision's fronts (graph `graph`), unscale and unpermute into
+// dst. Rows of LPs in `other` keep their dst values (see k_unpermute_scale).
+template <class T>
+void KktEngine::solve_pass(const T* F, const T* Linv, const int* mask, bool keep, const double* d_src,
+                           double* d_dst, int graph) {
     const auto& p = plan_;
-    const int q = fp32_ ? 1 : 0;
-    if (fp32_) k_permute_scale<float><<<blocks_for(p.M, 256), 256, 0, st_>>>(p.M, perm_.ptr, D_.ptr, d_src,
-                                                                             reinterpret_cast<float*>(zp_.ptr));
-    else k_permute_scale<double><<<blocks_for(p.M, 256), 256, 0, st_>>>(p.M, perm_.ptr, D_.ptr, d_src, zp_.ptr);
-    if (!gsol_[q]) {
+    k_permute_scale<T><<<blocks_for(p.M, 256), 256, 0, st_>>>(p.M, perm_.ptr, D_.ptr, d_src,
+                                                              reinterpret_cast<T*>(zp_.ptr));
+    if (!gsol_[graph]) {
         cudaGraph_t g;
         SK_CUDA(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
-        if (fp32_) launch_solve<float>(F32_.ptr, Linv32_.ptr); else launch_solve<double>(F64_.ptr, Linv64_.ptr);
+        launch_solve<T>(F, Linv);
         SK_CUDA(cudaStreamEndCapture(st_, &g));
-        SK_CUDA(cudaGraphInstantiate(&gsol_[q], g, 0));
+        SK_CUDA(cudaGraphInstantiate(&gsol_[graph], g, 0));
         cudaGraphDestroy(g);
     }
-    SK_CUDA(cudaGraphLaunch(gsol_[q], st_));
-    if (fp32_) k_unpermute_scale<float><<<blocks_for(p.M, 256), 256, 0, st_>>>(
-        p.M, perm_.ptr, D_.ptr, reinterpret_cast<const float*>(xp_.ptr), lp_.row_lp, lp_on_.ptr, d_dst);
-    else k_unpermute_scale<double><<<blocks_for(p.M, 256), 256, 0, st_>>>(p.M, perm_.ptr, D_.ptr, xp_.ptr,
-                                                                           lp_.row_lp, lp_on_.ptr, d_dst);
+    SK_CUDA(cudaGraphLaunch(gsol_[graph], st_));
+    const int* other = keep ? (std::is_same<T, float>::value ? on64_.ptr : on32_.ptr) : nullptr;
+    k_unpermute_scale<T><<<blocks_for(p.M, 256), 256, 0, st_>>>(
+        p.M, perm_.ptr, D_.ptr, reinterpret_cast<const T*>(xp_.ptr), lp_.row_lp, mask, other, d_dst);
     SK_CUDA(cudaGetLastError());
 }
 
-void KktEngine::set_active(const std::vector<char>& on) {
-    bool same = on.size() == lp_on_h_.size();
-    for (size_t k = 0; same && k < on.size(); ++k) same = (on[k] != 0) == (lp_on_h_[k] != 0);
+void KktEngine::apply_inverse(const double* d_src, double* d_dst) {
+    if (!mixed_) {
+        if (fp32_) solve_pass<float>(F32_.ptr, Linv32_.ptr, on32_.ptr, false, d_src, d_dst, 1);
+        else solve_pass<double>(F64_.ptr, Linv64_.ptr, on64_.ptr, false, d_src, d_dst, 0);
+        return;
+    }
+    bool any32 = false, any64 = false;
+    for (size_t k = 0; k < on32_h_.size(); ++k) { any32 |= on32_h_[k] != 0; any64 |= on64_h_[k] != 0; }
+    // The FP32 pass writes only the rows of on32 (and zeroes the inactive ones); the FP64
+    // pass then reads the rows of on64 from src, which the first pass left alone, so src
+    // and dst may still alias.
+    if (!any32 && !any64) {          // no LP left: every row is 0
+        SK_CUDA(cudaMemsetAsync(d_dst, 0, sizeof(double) * static_cast<size_t>(plan_.M), st_));
+        return;
+    }
+    if (any32) {
+        ensure_fronts(true);
+        solve_pass<float>(F32_.ptr, Linv32_.ptr, on32_.ptr, true, d_src, d_dst, 1);
+    }
+    if (any64) {
+        ensure_fronts(false);
+        solve_pass<double>(F64_.ptr, Linv64_.ptr, on64_.ptr, true, d_src, d_dst, 0);
+    }
+}
+
+void KktEngine::upload_mask(Slot<int>& dev, std::vector<int>& host, const std::vector<char>& on) {
+    if (on.size() != host.size()) throw std::invalid_argument("set_active: one flag per LP");
+    bool same = true;
+    for (size_t k = 0; same && k < on.size(); ++k) same = (on[k] != 0) == (host[k] != 0);
     if (same) return;
-    if (on.size() != lp_on_h_.size()) throw std::invalid_argument("set_active: one flag per LP");
-    for (size_t k = 0; k < on.size(); ++k) lp_on_h_[k] = on[k] ? 1 : 0;
-    SK_CUDA(cudaMemcpyAsync(lp_on_.ptr, lp_on_h_.data(), sizeof(int) * lp_on_h_.size(), cudaMemcpyHostToDevice, st_));
+    for (size_t k = 0; k < on.size(); ++k) host[k] = on[k] ? 1 : 0;
+    SK_CUDA(cudaMemcpyAsync(dev.ptr, host.data(), sizeof(int) * host.size(), cudaMemcpyHostToDevice, st_));
+}
+
+void KktEngine::set_active(const std::vector<char>& on) {
+    mixed_ = false;
+    upload_mask(on32_, on32_h_, on);
+    upload_mask(on64_, on64_h_, on);
+}
+
+void KktEngine::set_masks(const std::vector<char>& on32, const std::vector<char>& on64) {
+    for (size_t k = 0; k < on32.size() && k < on64.size(); ++k)
+        if (on32[k] && on64[k]) throw std::invalid_argument("set_masks: an LP in both precisions");
+    mixed_ = true;
+    upload_mask(on32_, on32_h_, on32);
+    upload_mask(on64_, on64_h_, on64);
+}
+
+int KktEngine::failed_lp() const {
+    return failed_sn_ >= 0 && failed_sn_ < static_cast<int>(sn_lp_h_.size()) ? sn_lp_h_[failed_sn_] : -1;
 }
 
 void KktEngine::apply_normal(const double* d_theta, const double* d_src, double* d_dst) {
@@ -1412,12 +1819,13 @@ void KktEngine::profile(const double* d_theta, double delta, bool fp32, const do
                                                                           reinterpret_cast<float*>(zp_.ptr));
         launch_solve<float>(F32_.ptr, Linv32_.ptr, &pr);
         k_unpermute_scale<float><<<blocks_for(plan_.M, 256), 256, 0, st_>>>(
-            plan_.M, perm_.ptr, D_.ptr, reinterpret_cast<const float*>(xp_.ptr), lp_.row_lp, lp_on_.ptr, d_out);
+            plan_.M, perm_.ptr, D_.ptr, reinterpret_cast<const float*>(xp_.ptr), lp_.row_lp, on32_.ptr, nullptr,
+            d_out);
     } else {
         k_permute_scale<double><<<blocks_for(plan_.M, 256), 256, 0, st_>>>(plan_.M, perm_.ptr, D_.ptr, d_rhs, zp_.ptr);
         launch_solve<double>(F64_.ptr, Linv64_.ptr, &pr);
         k_unpermute_scale<double><<<blocks_for(plan_.M, 256), 256, 0, st_>>>(plan_.M, perm_.ptr, D_.ptr, xp_.ptr,
-                                                                             lp_.row_lp, lp_on_.ptr, d_out);
+                                                                             lp_.row_lp, on64_.ptr, nullptr, d_out);
     }
     SK_CUDA(cudaStreamSynchronize(st_));
     for (int q = 0; q < 16; ++q) out[q] = 0.0;

@@ -31,6 +31,11 @@ public:
     // FP32 fronts: trailing updates on the tensor cores (tcgen05, TF32 x3; default) or
     // as exact FP32 SIMT arithmetic. Applies to the next factor() call.
     void set_tensor_update(bool on) { tensor_ = on; }
+    // FP64 fronts: trailing updates as FP64-accurate products on the tensor cores
+    // (BF16 digits, exact FP32 sums, integer epilogue; see k_update_oz) or on the
+    // FP64 pipe (default). Applies to the next factor() call.
+    void set_fp64_emulation(bool on) { emulate64_ = on; }
+    bool fp64_emulation() const { return emulate64_; }
     // dst = D L^{-T} L^{-1} D src (batch row order), using the last factor. src
     // and dst may alias. Asynchronous on the engine stream.
     void apply_inverse(const double* d_src, double* d_dst);
@@ -38,7 +43,18 @@ public:
     void apply_normal(const double* d_theta, const double* d_src, double* d_dst);
     // Which LPs of the batch are still being solved: factorisation and solves skip
     // the fronts of the others (their solve output rows are 0). All on initially.
+    // apply_inverse then uses the last factor's precision for every LP.
     void set_active(const std::vector<char>& on);
+    // Per-LP precision: LPs flagged in on32 use the FP32 fronts, those in on64 the
+    // FP64 fronts (disjoint sets). factor(.., fp32) assembles and factors only the
+    // fronts of its own set, leaving the other fronts of that precision as they
+    // are, so an LP can be moved from on32 to on64 and factored alone. apply_inverse
+    // applies the FP32 factor to the rows of on32 and the FP64 factor to the rows
+    // of on64 (rows of neither get 0). Both sets must have been factored with the
+    // current theta before apply_inverse.
+    void set_masks(const std::vector<char>& on32, const std::vector<char>& on64);
+    // LP of the front whose pivot failed in the last factor() (-1 if none).
+    int failed_lp() const;
 
     // Diagnostics: one factorisation + one solve (of d_rhs) without graphs, with
     // CUDA events around every launch; fills out[17] as sk_solver_profile documents.
@@ -66,7 +82,11 @@ private:
     template <class T> void launch_factor(T* F, T* Linv, Prof* prof = nullptr);
     template <class T> void launch_solve(const T* F, const T* Linv, Prof* prof = nullptr);
     void ensure_fronts(bool fp32);
-    PlanDev pd() const;
+    void ensure_digits();
+    PlanDev pd(bool fp32) const;
+    void upload_mask(Slot<int>& dev, std::vector<int>& host, const std::vector<char>& on);
+    template <class T> void solve_pass(const T* F, const T* Linv, const int* mask, bool keep, const double* d_src,
+                                       double* d_dst, int graph);
 
     ipm::FrontPlan plan_;
     const DeviceLP& lp_;
@@ -85,8 +105,12 @@ private:
         solve_err_;
     Slot<int2> fwd_tasks_, bwd_tasks_;
     Slot<int> g_dst_, g_zp_, g_ptr_, g_src_;   // forward right-hand-side gather lists
-    Slot<int> sn_lp_, lp_on_;
-    std::vector<int> lp_on_h_;
+    Slot<int> sn_lp_, on32_, on64_, q_lp_;    // LP of each front; per-precision LP masks; LP of each permuted row
+    std::vector<int> on32_h_, on64_h_, sn_lp_h_;
+    bool mixed_ = false;                        // set_masks in force (else one precision for all)
+    Slot<int> zc_sn_, zc_len_;                  // front-zeroing chunks: front, length and start offset
+    Slot<int64_t> zc_off_;
+    int64_t nzc_ = 0;
     Slot<int64_t> inv_off_;
     Slot<int64_t> slot_pos_, w_ptr_;
     Slot<int> slot_i_, slot_j_, w_col_;
@@ -98,9 +122,14 @@ private:
     int failed_sn_ = -1;
     const double* theta_bound_ = nullptr;
     bool tensor_ = true;
-    cudaGraphExec_t gfac_[3] = {nullptr, nullptr, nullptr};   // FP64, FP32 SIMT update, FP32 tensor-core update
+    bool emulate64_ = false;
+    Arena dig_arena_;                           // digit planes and row exponents of the emulated FP64 update
+    Slot<unsigned char> dig_;
+    Slot<int> dexp_;
+    // FP64, FP32 SIMT update, FP32 tensor-core update, FP64 emulated on the tensor cores
+    cudaGraphExec_t gfac_[4] = {nullptr, nullptr, nullptr, nullptr};
     cudaGraphExec_t gsol_[2] = {nullptr, nullptr};
-    const double* gfac_theta_[3] = {nullptr, nullptr, nullptr};
+    const double* gfac_theta_[4] = {nullptr, nullptr, nullptr, nullptr};
 };
 
 }  // namespace dev

@@ -83,6 +83,7 @@ static void build_schedule(FrontPlan& p) {
     p.steps.clear();
     p.step_items.clear();
     p.step_prefix.clear();
+    p.max_digit_rows = 0;
     p.step_level_ptr.assign(static_cast<size_t>(p.nlevels) + 1, 0);
     for (int l = 0; l < p.nlevels; ++l) {
         int kmax = 0;
@@ -131,6 +132,30 @@ static void build_schedule(FrontPlan& p) {
                 p.step_prefix.push_back(static_cast<int>(acc));
             }
             st.upd2_blocks = acc;
+            st.upd3_prefix_off = static_cast<int>(p.step_prefix.size());
+            acc = 0;
+            p.step_prefix.push_back(0);
+            for (int s : items) {
+                const int64_t w = std::min<int64_t>(kTile, p.sn_ncols[s] - static_cast<int64_t>(k) * kTile);
+                const int64_t t = p.sn_nrows[s] - static_cast<int64_t>(k) * kTile - w;
+                const int64_t nbr = ceil_div(t, 2 * kTile);
+                acc += nbr * (nbr + 1);
+                if (acc > INT32_MAX) throw std::runtime_error("front plan: too many blocks in one step");
+                p.step_prefix.push_back(static_cast<int>(acc));
+            }
+            st.upd3_blocks = acc;
+            st.digit_row_off = static_cast<int>(p.step_prefix.size());
+            acc = 0;
+            p.step_prefix.push_back(0);
+            for (int s : items) {
+                const int64_t w = std::min<int64_t>(kTile, p.sn_ncols[s] - static_cast<int64_t>(k) * kTile);
+                const int64_t t = p.sn_nrows[s] - static_cast<int64_t>(k) * kTile - w;
+                acc += ceil_div(t, 2 * kTile) * 2 * kTile;
+                if (acc > INT32_MAX) throw std::runtime_error("front plan: too many digit rows in one step");
+                p.step_prefix.push_back(static_cast<int>(acc));
+            }
+            st.digit_rows = acc;
+            p.max_digit_rows = std::max(p.max_digit_rows, acc);
             p.steps.push_back(st);
         }
         p.step_level_ptr[l + 1] = static_cast<int>(p.steps.size());
@@ -277,12 +302,19 @@ void build_front_plan(const std::vector<LpView>& lps, const core::CSRMatrix& A, 
     p.nlp = static_cast<int>(lps.size());
     p.row_off.assign(static_cast<size_t>(p.nlp) + 1, 0);
     p.col_off.assign(static_cast<size_t>(p.nlp) + 1, 0);
-    bool all_dense = true;
+    // A batch runs in dense mode when its LPs prefer dense fronts, or when the LPs that
+    // do not are a negligible part of the batch's dense factorisation work (their
+    // sum of m^3 at most 2% of the batch's): one dense front each then costs little
+    // extra and spares the whole batch the sparse analysis.
+    double cube_all = 0.0, cube_sparse = 0.0;
     for (int k = 0; k < p.nlp; ++k) {
         p.row_off[k + 1] = p.row_off[k] + lps[k].m;
         p.col_off[k + 1] = p.col_off[k] + lps[k].n;
-        all_dense = all_dense && prefer_dense_front(lps[k]);
+        const double c = static_cast<double>(lps[k].m) * lps[k].m * lps[k].m;
+        cube_all += c;
+        if (!prefer_dense_front(lps[k])) cube_sparse += c;
     }
+    const bool all_dense = cube_sparse == 0.0 || (p.nlp > 1 && cube_sparse <= 0.02 * cube_all);
     p.M = p.row_off[p.nlp];
     p.N = p.col_off[p.nlp];
     p.nnzA = A.row_ptrs.empty() ? 0 : A.row_ptrs.back();

@@ -49,6 +49,13 @@ struct PlanStep {            // one tile step of one level
     int64_t upd_tiles = 0;
     int upd2_prefix_off = 0; // into step_prefix: nitems+1 entries (lower 128x128 blocks of the trailing part)
     int64_t upd2_blocks = 0;
+    // emulated FP64 update: 128-row x 64-column blocks of the trailing lower part
+    // (row block i holds column blocks 0..2i+1), and each item's first row in the
+    // digit buffer (its trailing rows padded to a multiple of 128)
+    int upd3_prefix_off = 0; // into step_prefix: nitems+1 entries
+    int64_t upd3_blocks = 0;
+    int digit_row_off = 0;   // into step_prefix: nitems+1 entries
+    int64_t digit_rows = 0;
 };
 
 struct PlanRound {           // one extend-add round after a level
@@ -66,6 +73,7 @@ struct FrontPlan {
     std::vector<Index> row_off, col_off;   // nlp+1 each
     bool dense_mode = false;
     int ordering_used = 0;
+    int64_t max_digit_rows = 0;            // largest PlanStep::digit_rows of any step
 
     std::vector<Index> perm, iperm;        // perm[k] = batch row at elimination position k
 

@@ -27,6 +27,7 @@ sk_options to_c(const MehrotraOptions& o) {
     c.strict = o.strict;
     c.delta32 = o.delta32;
     c.delta64 = o.delta64;
+    c.fp64_update = o.fp64_update;
     return c;
 }
 
