@@ -77,7 +77,15 @@ typedef struct sk_options {
     double learned_accept;/* SK_START_LEARNED: the network's start is used for an LP when its distance to
                            * the stopping test is below learned_accept x that of Mehrotra's start
                            * (default 0.5); otherwise that LP starts from Mehrotra's start */
+    int fp64_update;      /* trailing updates of FP64 fronts: SK_FP64_UPDATE_AUTO (default: FP64-accurate
+                           * products on the tensor cores in SK_PREC_MIXED, the FP64 pipe in SK_PREC_FP64),
+                           * SK_FP64_UPDATE_NATIVE (FP64 pipe) or SK_FP64_UPDATE_TENSOR (tensor cores:
+                           * BF16 digits of the FP64 panel, exact FP32 sums, results within about
+                           * 2^-53 of sum |a||b|) */
 } sk_options;
+#define SK_FP64_UPDATE_AUTO 0
+#define SK_FP64_UPDATE_NATIVE 1
+#define SK_FP64_UPDATE_TENSOR 2
 
 typedef struct sk_info {
     int status;               /* SK_STATUS_* */
@@ -210,6 +218,11 @@ int sk_kkt_solve(sk_kkt* k, double* rhs, double tol);                        /* 
 /* Copies the factor of D (P M0 P^T) D + delta I as a dense lower-triangular m x m
  * row-major matrix in the elimination order, plus D (m), for inspection. */
 int sk_kkt_get_factor(sk_kkt* k, double* L_dense, double* D);
+/* Trailing updates of the FP64 factorisation (sk_kkt_create with SK_PREC_FP64):
+ * SK_FP64_UPDATE_NATIVE / _AUTO (FP64 pipe, default) or SK_FP64_UPDATE_TENSOR
+ * (FP64-accurate products on the tensor cores). No counterpart in the reference
+ * (its factorisation is scalar FP64). Applies from the next factorisation. */
+int sk_kkt_set_fp64_update(sk_kkt* k, int mode);
 void sk_kkt_destroy(sk_kkt* k);
 
 /* ---- Symbolic analysis (host) ----
@@ -268,13 +281,58 @@ int sk_crossover(int m, int n, const int* col_ptrs, const int* row_idx, const do
  * synchronisation allowed). All work lives in one fixed device array of
  * 542,976 bytes, which limits m to SK_KKT_NOALLOC_MAX_ROWS; a larger m returns
  * SK_ERR_TOO_LARGE. The first call on each device fetches that array's address
- * (set-up), so make it before any stream capture. Every call on a device uses
+ * and loads the kernel (set-up; loading the module may allocate driver memory),
+ * so make it before any stream capture. Every call on a device uses
  * the same array: calls that overlap in time (two host threads, or two streams
  * without ordering between them) race and corrupt each other's results. The
- * call synchronises `stream` (NULL = legacy default stream) before it returns. */
+ * call synchronises `stream` (NULL = legacy default stream) before it returns.
+ * d_row_ptrs[m] must equal the length of d_col_idx and d_vals: the kernel reads
+ * up to that entry and cannot check it against the arrays' sizes. Malformed
+ * row pointers, unsorted or out-of-range columns, a negative or non-finite theta
+ * and non-finite values of A or rhs return SK_ERR_INVALID with d_rhs untouched;
+ * a solve that misses tol (for example a row of A without entries) returns
+ * SK_ERR_NUMERICAL with d_rhs holding the last iterate. */
 #define SK_KKT_NOALLOC_MAX_ROWS 256
 int sk_kkt_solve_noalloc(int m, int n, const int* d_row_ptrs, const int* d_col_idx, const double* d_vals,
                          const double* d_theta, double* d_rhs, double tol, void* stream);
+
+/* ---- Convex QP on the device ----
+ * Replaces: qp::QPSolver::solve_with_diagnostics (src/qp/qp_solver.hpp:47-66,
+ * src/qp/qp_solver.cpp:151-560; C++ interface kept in include/qp/qp_solver.hpp).
+ * min 1/2 x^T H x + c^T x subject to A x = b and lb <= x <= ub. A is m x n in CSC
+ * (m may be 0); H is n x n given by its lower triangle (diagonal included) in CSC;
+ * lb / ub may be NULL (0 and +inf); a bound beyond 1e15 in magnitude is absent.
+ * convexity: SK_QP_CONVEX_PSD solves; SK_QP_CONVEXITY_UNKNOWN and SK_QP_NONCONVEX
+ * give status UnsupportedNonconvex, as the reference does. opts may be NULL
+ * (sk_qp_options_default: 1e-6, 1e-6, 1e-6, 200). The reference's iteration runs
+ * on the GPU with W = H + D diagonal (a non-diagonal H is lifted through a
+ * pivoted Cholesky H = F^T F into free variables w = F x; dense, n <= 4096).
+ * *status receives the QPSolverStatus (SK_QP_OPTIMAL ...); x (n), y (m) and
+ * z = zl - zu (n) are written when it is Optimal or IterationLimit; info (may be
+ * NULL) receives {objective, iterations, primal_residual, dual_residual,
+ * complementarity}. Returns SK_OK, SK_ERR_INVALID (bad pointers or entries, an
+ * entry of H above the diagonal), SK_ERR_NO_DEVICE or SK_ERR_CUDA. */
+#define SK_QP_CONVEXITY_UNKNOWN 0
+#define SK_QP_CONVEX_PSD 1
+#define SK_QP_NONCONVEX 2
+#define SK_QP_OPTIMAL 0
+#define SK_QP_INFEASIBLE 1
+#define SK_QP_UNBOUNDED 2
+#define SK_QP_ITERATION_LIMIT 3
+#define SK_QP_NUMERICAL_FAILURE 4
+#define SK_QP_UNSUPPORTED_NONCONVEX 5
+#define SK_QP_INVALID_MODEL 6
+typedef struct sk_qp_options {
+    double feasibility_tol;   /* ||A x - b||_inf below this */
+    double dual_tol;          /* ||H x + c - A^T y - zl + zu||_inf below this */
+    double grad_tol;          /* complementarity mu below this */
+    int max_iterations;
+} sk_qp_options;
+void sk_qp_options_default(sk_qp_options* opts);
+int sk_qp_solve(int m, int n, const int* a_col_ptrs, const int* a_row_idx, const double* a_vals, const double* b,
+                const double* c, const double* lb, const double* ub, const int* h_col_ptrs, const int* h_row_idx,
+                const double* h_vals, int convexity, const sk_qp_options* opts, double* x, double* y, double* z,
+                int* status, double* info);
 
 /* ---- Presolve: Ruiz equilibration of a model (host) ----
  * Replaces: presolve::apply_ruiz_scaling(core::Model&, int max_iterations)

@@ -2,6 +2,7 @@
 // sources where they lie (see Makefile target `ref`). TEST INFRASTRUCTURE ONLY:
 // the reference is used here as a checker (symbolic analysis, simplex objective,
 // certificate) and as the timed CPU baseline; nothing in the product links it.
+#include <cmath>
 #include <cstring>
 #include <vector>
 
@@ -10,6 +11,8 @@
 #include "ipm/symbolic.hpp"
 #include "numerics/sparse_lu.hpp"
 #include "presolve/scaling.hpp"
+#include "qp/qp_model.hpp"
+#include "qp/qp_solver.hpp"
 #include "simplex/phase1.hpp"
 #include "verifier/certificate.hpp"
 
@@ -136,6 +139,65 @@ int ref_ruiz_scaling(int m, int n, const int* cp, const int* ri, const double* v
         std::memcpy(row_scale, model.row_scale.data(), sizeof(double) * static_cast<size_t>(m));
         std::memcpy(col_scale, model.col_scale.data(), sizeof(double) * static_cast<size_t>(n));
         return 0;
+    } catch (...) {
+        return -1;
+    }
+}
+
+// The reference's qp::QPSolver::solve_with_diagnostics on a QP given densely
+// (H n x n row-major, symmetric; A m x n row-major), modelled as the reference's
+// own QP tests model it (H's lower triangle in CSC, entries above 1e-15 in
+// magnitude; convexity ConvexPSD). Writes x, y, z (when the solver returns them)
+// and info = {objective, iterations, primal_residual, dual_residual,
+// complementarity}; returns the QPSolverStatus as int (-1 on an exception).
+int ref_qp_solve(int n, int m, const double* H, const double* c, const double* A, const double* b,
+                 const double* lb, const double* ub, int max_iter, double* x_out, double* y_out, double* z_out,
+                 double* info) {
+    try {
+        qp::QPModel qp;
+        qp.lp_part.sense = OptimizationSense::Minimize;
+        qp.lp_part.obj.assign(c, c + n);
+        qp.lp_part.lb.assign(lb, lb + n);
+        qp.lp_part.ub.assign(ub, ub + n);
+        qp.lp_part.rhs.assign(b, b + m);
+        qp.lp_part.vtype.assign(static_cast<size_t>(n), VariableType::Continuous);
+        std::vector<Index> cp(static_cast<size_t>(n) + 1, 0), ri;
+        std::vector<Float> va;
+        for (int j = 0; j < n; ++j) {
+            cp[static_cast<size_t>(j)] = static_cast<Index>(ri.size());
+            for (int i = 0; i < m; ++i) {
+                const double v = A[static_cast<size_t>(i) * n + j];
+                if (std::abs(v) > 1e-15) { ri.push_back(i); va.push_back(v); }
+            }
+        }
+        cp[static_cast<size_t>(n)] = static_cast<Index>(ri.size());
+        qp.lp_part.A = core::CSCMatrix(m, n, va, ri, cp);
+        std::vector<Index> hp(static_cast<size_t>(n) + 1, 0), hr;
+        std::vector<Float> hv;
+        for (int j = 0; j < n; ++j) {
+            hp[static_cast<size_t>(j)] = static_cast<Index>(hr.size());
+            for (int i = j; i < n; ++i) {
+                const double v = H[static_cast<size_t>(i) * n + j];
+                if (std::abs(v) > 1e-15) { hr.push_back(i); hv.push_back(v); }
+            }
+        }
+        hp[static_cast<size_t>(n)] = static_cast<Index>(hr.size());
+        qp.H = core::CSCMatrix(n, n, hv, hr, hp);
+        qp.convexity = qp::QPConvexityStatus::ConvexPSD;
+        qp::QPSolver::Options opts;
+        opts.max_iterations = max_iter;
+        qp::QPSolver solver(opts);
+        std::vector<Float> x, y, z;
+        auto r = solver.solve_with_diagnostics(qp, x, y, z);
+        if (x.size() == static_cast<size_t>(n)) std::memcpy(x_out, x.data(), sizeof(double) * static_cast<size_t>(n));
+        if (y.size() == static_cast<size_t>(m) && m > 0) std::memcpy(y_out, y.data(), sizeof(double) * static_cast<size_t>(m));
+        if (z.size() == static_cast<size_t>(n)) std::memcpy(z_out, z.data(), sizeof(double) * static_cast<size_t>(n));
+        info[0] = r.objective_value;
+        info[1] = r.iterations;
+        info[2] = r.primal_residual;
+        info[3] = r.dual_residual;
+        info[4] = r.complementarity;
+        return static_cast<int>(r.status);
     } catch (...) {
         return -1;
     }
