@@ -85,6 +85,28 @@ void oracle_kkt_measures(int m, int n, const int* col_ptrs, const int* row_idx, 
                          const double* b, const double* c, const double* x, const double* y,
                          const double* s, double* out);
 
+/* A generated LP in standard form (CSC with rows increasing in each column). */
+typedef struct oracle_lp {
+    int m, n, nnz;
+    int* col_ptrs;     /* n + 1 */
+    int* row_idx;      /* nnz */
+    double* vals;      /* nnz */
+    double* b;         /* m */
+    double* c;         /* n */
+} oracle_lp;
+
+/* Seeded LP families of the benchmark (lpgen_oracle.c): the same arrays as the
+ * product's generator for the same seed, built without it, so that the CPU
+ * baselines load nothing of the product. Return 0 on success; release with
+ * oracle_lp_free. family: 0, 1 or 3. */
+int oracle_lp_family(int family, int instance, oracle_lp* lp);
+int oracle_lp_random(int m, int n, double density, unsigned long long seed, oracle_lp* lp);
+int oracle_lp_block_angular(unsigned long long seed, int blocks, int block_rows, int block_cols, int link_rows,
+                            int nnz_per_block_col, oracle_lp* lp);
+void oracle_lp_free(oracle_lp* lp);
+/* Rows, columns and density of family-3 member `instance` without building it. */
+int oracle_lp_family3_shape(int instance, int* m, int* n, double* density);
+
 #ifdef __cplusplus
 }
 #endif

@@ -33,10 +33,13 @@ class IpmResult(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
-def build(reference_root="/root/reference"):
-    """Builds the oracle library, and oracle/_ref when the reference sources exist."""
+def build(reference_root=None):
+    """Builds the oracle library, and oracle/_ref when the reference sources are
+    given (argument, else the SK_REFERENCE_ROOT environment variable: the
+    directory that holds the reference's src/ and include/)."""
     subprocess.run(["make", "-s", "-C", HERE], check=True)
-    if os.path.isdir(os.path.join(reference_root, "src")):
+    reference_root = reference_root or os.environ.get("SK_REFERENCE_ROOT")
+    if reference_root and os.path.isdir(os.path.join(reference_root, "src")):
         subprocess.run(["make", "-s", "-C", HERE, "ref", "REF=" + reference_root], check=True)
 
 
@@ -58,8 +61,71 @@ def oracle():
                                        _f64p, _f64p, _f64p, C.POINTER(IpmResult)]
         L.oracle_kkt_measures.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p, _f64p, _f64p, _f64p, _f64p, _f64p,
                                           _f64p]
+        L.oracle_lp_family.argtypes = [C.c_int, C.c_int, C.c_void_p]
+        L.oracle_lp_random.argtypes = [C.c_int, C.c_int, C.c_double, C.c_ulonglong, C.c_void_p]
+        L.oracle_lp_block_angular.argtypes = [C.c_ulonglong] + [C.c_int] * 5 + [C.c_void_p]
+        L.oracle_lp_free.argtypes = [C.c_void_p]
+        L.oracle_lp_family3_shape.argtypes = [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                              C.POINTER(C.c_double)]
         _o = L
     return _o
+
+
+class OracleLP(C.Structure):
+    _fields_ = [("m", C.c_int), ("n", C.c_int), ("nnz", C.c_int), ("col_ptrs", C.POINTER(C.c_int)),
+                ("row_idx", C.POINTER(C.c_int)), ("vals", C.POINTER(C.c_double)), ("b", C.POINTER(C.c_double)),
+                ("c", C.POINTER(C.c_double))]
+
+
+class LP:
+    """A generated LP (min c^T x, A x = b, x >= 0; A in CSC) as numpy arrays, built by
+    the oracle's restatement of the seeded generator (no product code involved)."""
+
+    def __init__(self, m, n, col_ptrs, row_idx, vals, b, c, name="lp"):
+        self.m, self.n = int(m), int(n)
+        self.col_ptrs, self.row_idx, self.vals, self.b, self.c = col_ptrs, row_idx, vals, b, c
+        self.name = name
+
+    @property
+    def nnz(self):
+        return int(self.col_ptrs[-1])
+
+
+def _take_lp(h, name):
+    def arr(p, k, dt):
+        return np.ctypeslib.as_array(p, shape=(k,)).astype(dt, copy=True) if k > 0 else np.zeros(0, dtype=dt)
+    lp = LP(h.m, h.n, arr(h.col_ptrs, h.n + 1, np.int32), arr(h.row_idx, h.nnz, np.int32),
+            arr(h.vals, h.nnz, np.float64), arr(h.b, h.m, np.float64), arr(h.c, h.n, np.float64), name)
+    oracle().oracle_lp_free(C.byref(h))
+    return lp
+
+
+def generate(family, instance=0):
+    """Seeded LP of family 0, 1 or 3, identical to the product's generator."""
+    h = OracleLP()
+    assert oracle().oracle_lp_family(family, instance, C.byref(h)) == 0, (family, instance)
+    return _take_lp(h, "family%d/%d" % (family, instance))
+
+
+def generate_dims(family, instance):
+    """(m, n) of a family-3 member without building it."""
+    assert family == 3
+    m, n, d = C.c_int(), C.c_int(), C.c_double()
+    oracle().oracle_lp_family3_shape(instance, C.byref(m), C.byref(n), C.byref(d))
+    return m.value, n.value
+
+
+def random_lp(m, n, density, seed):
+    h = OracleLP()
+    assert oracle().oracle_lp_random(m, n, density, seed, C.byref(h)) == 0
+    return _take_lp(h, "random%dx%d" % (m, n))
+
+
+def block_angular(seed, blocks, block_rows=500, block_cols=1200, link_rows=2000, nnz_per_col=5):
+    h = OracleLP()
+    assert oracle().oracle_lp_block_angular(seed, blocks, block_rows, block_cols, link_rows, nnz_per_col,
+                                            C.byref(h)) == 0
+    return _take_lp(h, "block_angular%dx%d" % (blocks, link_rows))
 
 
 def have_reference():
@@ -75,6 +141,8 @@ def reference():
         L.ref_simplex_solve.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p, _f64p, _f64p, _f64p,
                                         C.POINTER(C.c_double)]
         L.ref_verify_optimal.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p, _f64p, _f64p, _f64p, _f64p]
+        if hasattr(L, "ref_qp_solve"):
+            L.ref_qp_solve.argtypes = [C.c_int, C.c_int] + [_f64p] * 6 + [C.c_int] + [_f64p] * 4
         if hasattr(L, "ref_ruiz_scaling"):
             _u8p = np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")
             L.ref_ruiz_scaling.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p, _f64p, _f64p, _f64p, _f64p, _u8p,
@@ -167,3 +235,18 @@ def ref_ruiz(lp, lb, ub, integer, max_iter=10):
                             out["lb"], out["ub"], out["row_scale"], out["col_scale"])
     assert rc == 0, rc
     return out
+
+
+def ref_qp(H, c, A, b, lb, ub, max_iter=200):
+    """The reference's qp::QPSolver on a dense QP: dict(status, objective, iterations,
+    primal_residual, dual_residual, complementarity, x, y, z)."""
+    H = np.ascontiguousarray(H, dtype=np.float64)
+    n = H.shape[0]
+    A = np.ascontiguousarray(np.asarray(A, dtype=np.float64).reshape(-1, n))
+    m = A.shape[0]
+    f = lambda v: np.ascontiguousarray(v, dtype=np.float64)
+    x, y, z, info = np.zeros(n), np.zeros(max(m, 1)), np.zeros(n), np.zeros(5)
+    st = reference().ref_qp_solve(n, m, H.ravel(), f(c), A.ravel() if m else np.zeros(1), f(b) if m else np.zeros(1),
+                                  f(lb), f(ub), max_iter, x, y, z, info)
+    return {"status": st, "objective": info[0], "iterations": int(info[1]), "primal_residual": info[2],
+            "dual_residual": info[3], "complementarity": info[4], "x": x, "y": y[:m], "z": z}

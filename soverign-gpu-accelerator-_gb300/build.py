@@ -58,7 +58,9 @@ def compile_one(src, force, hdr_t):
     if src.endswith(".cu"):
         cmd = [NVCC] + NVFLAGS + INC + ["-c", src, "-o", obj]
     else:
-        cmd = ["g++"] + CXXFLAGS + INC + ["-c", src, "-o", obj]
+        # the seeded LP generator gives the same bits on every host (no FMA contraction)
+        extra = ["-ffp-contract=off"] if os.path.basename(src) == "lpgen.cpp" else []
+        cmd = ["g++"] + CXXFLAGS + extra + INC + ["-c", src, "-o", obj]
     p = subprocess.run(cmd, capture_output=True, text=True)
     if p.returncode != 0:
         raise RuntimeError("compile failed: %s\n%s\n%s" % (" ".join(cmd), p.stdout, p.stderr))
