@@ -215,7 +215,9 @@ std::mutex g_setup_mu;
 double* g_scratch[kMaxDevices] = {};
 
 // Address of the scratch array on the current device, fetched on the first call
-// made with that device current.
+// made with that device current. The same set-up also loads the kernel itself
+// (with lazy module loading a kernel is otherwise loaded at its first launch,
+// which may allocate), so later calls launch an already loaded kernel.
 cudaError_t scratch_for_current_device(double** out) {
     int dev = 0;
     cudaError_t rc = cudaGetDevice(&dev);
@@ -223,6 +225,9 @@ cudaError_t scratch_for_current_device(double** out) {
     if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
     std::lock_guard<std::mutex> lock(g_setup_mu);
     if (!g_scratch[dev]) {
+        cudaFuncAttributes attr;
+        rc = cudaFuncGetAttributes(&attr, k_kkt_noalloc);
+        if (rc != cudaSuccess) return rc;
         void* p = nullptr;
         rc = cudaGetSymbolAddress(&p, g_kkt_noalloc_scratch);
         if (rc != cudaSuccess) return rc;
