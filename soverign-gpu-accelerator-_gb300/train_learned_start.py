@@ -3,15 +3,18 @@ it on held-out seeds.
 
 Family: family 3 of the generator (m ~ logUniform[200, 5000], n = ceil(m U[2, 3]),
 density U[0.5%, 2%], feasible and bounded by construction). Training targets are
-iterates of the plain FP64 IPM (Mehrotra's start): each LP's (log x, log s, y)
-in its Ruiz-scaled space the first time mu drops below --capture-mu. Training
-runs on the GPU through the engine's own BF16 forward / backward kernels and
-Adam (sk_gnn_train_step). Evaluation solves held-out LPs in mixed precision from
+IPM iterates from Mehrotra's start: each LP's (log x, log s, y) in its Ruiz-scaled
+space the first time mu drops below --capture-mu (the target solves stop after
+--target-iters iterations: the iterate is captured long before convergence).
+Training runs on the GPU through the engine's own BF16 forward / backward kernels
+and Adam (sk_gnn_train_step), one step per batch of --batch LPs. Evaluation solves
+held-out LPs as batched solves of --eval-batch LPs in mixed precision from
 Mehrotra's start and from the learned start (which falls back per LP to
-Mehrotra's start) and reports iterations, fallback rate and device time.
+Mehrotra's start) and reports iterations, fallback rate and time-to-1e-8.
 
 usage: python train_learned_start.py [--train 1024] [--heldout 128] [--batch 16]
-           [--epochs 30] [--lr 2e-3] [--capture-mu 1.0] [--out weights/learned_start_family3.npy]
+           [--epochs 30] [--lr 2e-3] [--capture-mu 1.0] [--eval-batch 512]
+           [--out weights/learned_start_family3.npy]
 Writes the FP32 master weights (.npy) and a JSON report next to them.
 """
 import argparse
@@ -32,21 +35,24 @@ HELDOUT_BASE = 200100   # ... and of the held-out set (the benchmark batch uses 
                         # were used to choose the capture level and the acceptance rule)
 
 
-def solve_for_targets(instances, batch, capture_mu):
-    """Plain FP64 IPM over the instances in batches; returns device-resident
-    training batches (scaled LP + captured iterate) and per-LP iteration counts."""
-    out, iters, t0 = [], [], time.perf_counter()
+def solve_for_targets(instances, batch, capture_mu, target_iters):
+    """IPM from Mehrotra's start over the instances in batches, each stopped after
+    target_iters iterations; returns device-resident training batches (scaled LP +
+    captured iterate) of the batches whose every LP was captured, and the number
+    of LPs kept."""
+    out, kept, t0 = [], 0, time.perf_counter()
     for i in range(0, len(instances), batch):
         lps = [sk.generate(3, k) for k in instances[i:i + batch]]
-        s = sk.Solver(lps, precision=sk.PREC_FP64, start=sk.START_MEHROTRA)
+        s = sk.Solver(lps, precision=sk.PREC_MIXED, start=sk.START_MEHROTRA, max_iter=target_iters)
         s.set_capture(capture_mu)
         s.run()
-        infos = [s.result(k, want_vectors=False)[0] for k in range(len(lps))]
-        if all(inf["status"] == 0 for inf in infos):
+        try:
             out.append(sk.GnnBatch.from_solver(s))
-        iters += [inf["iterations"] for inf in infos]
+            kept += len(lps)
+        except RuntimeError:       # some LP did not reach mu < capture_mu in time: batch left out
+            pass
         s.close()
-    return out, iters, time.perf_counter() - t0
+    return out, kept, time.perf_counter() - t0
 
 
 def run_batch(lps, start, net=None, precision=sk.PREC_MIXED):
@@ -66,6 +72,8 @@ def evaluate(net, instances, batch):
         lps = [sk.generate(3, k) for k in instances[i:i + batch]]
         base = run_batch(lps, sk.START_MEHROTRA)
         lrn = run_batch(lps, sk.START_LEARNED, net)
+        print("[eval] batch %d: %.1f s Mehrotra, %.1f s learned" % (i // batch, base[0]["device_ms"] / 1e3,
+                                                                   lrn[0]["device_ms"] / 1e3), flush=True)
         for k in range(len(lps)):
             b, l = base[k], lrn[k]
             rows.append({"m": lps[k].m, "n": lps[k].n, "it_mehrotra": b["iterations"], "it_learned": l["iterations"],
@@ -109,22 +117,24 @@ def main():
     ap.add_argument("--epochs", type=int, default=30)
     ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--capture-mu", type=float, default=1.0)
+    ap.add_argument("--target-iters", type=int, default=25)
+    ap.add_argument("--eval-batch", type=int, default=512)
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--out", default=os.path.join(HERE, "weights", "learned_start_family3.npy"))
     args = ap.parse_args()
-    tr, it_tr, t_solve = solve_for_targets(list(range(TRAIN_BASE, TRAIN_BASE + args.train)), args.batch,
-                                           args.capture_mu)
-    print("[data] %d training batches, plain FP64 solves %.1f s, mean iterations %.2f" %
-          (len(tr), t_solve, float(np.mean(it_tr))), flush=True)
+    tr, kept, t_solve = solve_for_targets(list(range(TRAIN_BASE, TRAIN_BASE + args.train)), args.batch,
+                                          args.capture_mu, args.target_iters)
+    print("[data] %d training batches (%d LPs), target solves %.1f s" % (len(tr), kept, t_solve), flush=True)
     net = sk.Gnn(args.seed)
     hist, t_train = train(net, tr, args.epochs, args.lr, args.seed)
     for b in tr:
         b.close()
-    summary, rows = evaluate(net, list(range(HELDOUT_BASE, HELDOUT_BASE + args.heldout)), args.batch)
+    summary, rows = evaluate(net, list(range(HELDOUT_BASE, HELDOUT_BASE + args.heldout)), args.eval_batch)
     print(json.dumps(summary), flush=True)
     os.makedirs(os.path.dirname(os.path.abspath(args.out)), exist_ok=True)
     net.save(args.out)
-    rep = {"family": 3, "train_instances": [TRAIN_BASE, TRAIN_BASE + args.train],
+    rep = {"family": 3, "train_instances": [TRAIN_BASE, TRAIN_BASE + args.train], "train_lps_kept": kept,
+           "target_iters": args.target_iters, "eval_batch": args.eval_batch,
            "heldout_instances": [HELDOUT_BASE, HELDOUT_BASE + args.heldout], "batch": args.batch,
            "epochs": args.epochs, "lr": args.lr, "capture_mu": args.capture_mu, "seed": args.seed,
            "target_solve_s": t_solve, "train_s": t_train, "loss_history": hist, "heldout": summary,
