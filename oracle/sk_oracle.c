@@ -559,13 +559,14 @@ int oracle_ipm_solve(int m, int n, const int* cp, const int* ri, const double* v
         double nrp = norm2(m, w.rp), nrd = norm2(n, w.rd), mu = dot(n, x, s) / n;
         if (iter == 0) { rp0 = fmax(1.0, nrp); rd0 = fmax(1.0, nrd); mu0 = fmax(1.0, mu); }
         int converged;
+        double pinf = 0.0, dinf = 0.0, cx = 0.0, by = 0.0;
         if (opts.criteria == 1) {
             converged = nrp < 1e-6 && nrd < 1e-6 && mu < 1e-6;
         } else {
-            double pinf = 0.0, dinf = 0.0;
             for (int i = 0; i < m; ++i) { double a = fabs(w.rp[i] / R[i]); if (a > pinf) pinf = a; }
             for (int j = 0; j < n; ++j) { double a = fabs(w.rd[j] / C[j]); if (a > dinf) dinf = a; }
-            double cx = dot(n, c, x), by = dot(m, b, y);
+            cx = dot(n, c, x);
+            by = dot(m, b, y);
             double gap = fabs(cx - by) / (1.0 + fabs(cx) + fabs(by));
             /* the gap is also held to tol (1 + |c^T x|): with the optimum between the primal
              * and dual objectives, c^T x is then within tol of it in relative terms */
@@ -613,6 +614,13 @@ int oracle_ipm_solve(int m, int n, const int* cp, const int* ri, const double* v
         double cap = fmin(1.0, eta * step_length(n, x, w.dx));
         double cad = fmin(1.0, eta * step_length(n, s, w.ds));
         double orig_merit = nrp / rp0 + nrd / rd0 + mu / mu0;
+        /* near-optimal (robust mode, relative criteria): primal and dual infeasibility within
+         * 0.1 tol; a trial that stays so and whose distance to the stopping test falls by the
+         * Armijo factor is accepted even when the merit rises (an inexact direction can add
+         * infeasibility far below the tolerance while it closes the gap) */
+        const int near = !opts.strict && opts.criteria != 1 && pinf / unscale_b <= 0.1 * opts.tol &&
+                         dinf / unscale_c <= 0.1 * opts.tol;
+        const double dist0 = fmax(fmax(pinf / unscale_b, dinf / unscale_c), fabs(cx - by) / (1.0 + fabs(cx)));
         int accepted = 0;
         for (int dir = corrector_valid ? 0 : 1; dir < 2 && !accepted; ++dir) {
             if (dir == 1) {
@@ -644,6 +652,17 @@ int oracle_ipm_solve(int m, int n, const int* cp, const int* ri, const double* v
                              isfinite(cad) && isfinite(norm2(m, w.by));
                 int positive = minx > 0.0 && mins > 0.0 && mu2 > 0.0 && step > 0.0;
                 int progress = merit < orig_merit && merit <= (1.0 - armijo * step) * orig_merit;
+                if (!progress && near && finite && positive) {
+                    double tp = 0.0, td = 0.0;
+                    for (int i = 0; i < m; ++i) { double a = fabs(w.brp[i] / R[i]); if (a > tp) tp = a; }
+                    for (int j = 0; j < n; ++j) { double a = fabs(w.brd[j] / C[j]); if (a > td) td = a; }
+                    tp /= unscale_b;
+                    td /= unscale_c;
+                    const double tcx = dot(n, c, w.bx), tby = dot(m, b, w.by);
+                    const double tdist = fmax(fmax(tp, td), fabs(tcx - tby) / (1.0 + fabs(tcx)));
+                    progress = tp <= 0.1 * opts.tol && td <= 0.1 * opts.tol && isfinite(tdist) &&
+                               tdist <= (1.0 - armijo * step) * dist0;
+                }
                 if (finite && positive && progress) { accepted = 1; break; }
                 cap *= 0.5;
                 cad *= 0.5;

@@ -46,6 +46,7 @@ constexpr int kRestartWindow = 10;           // ... within the first iterations
 constexpr double kUseDir = 1e-4;
 constexpr double kTensorMu = 1e-4;           // FP32 fronts: tensor-core updates while mu >= this
 constexpr int kLooseIters = 3;               // stall acceptance of the relative tests (see the stopping rule)
+constexpr double kNearFeas = 0.1;            // near-optimal line-search rule: rel. pinf, dinf below this x tol
 constexpr int kProgressIter = 12;            // learned-start restart: by this iteration the distance to the
 constexpr double kProgress = 1e-3;           // stopping test must have fallen by this factor
 
@@ -190,22 +191,26 @@ struct RedDir {          // [e2^2, e3^2, rxs^2, ratio x, ratio s, x s, x ds, dx 
         v[8] = dx[j] * ds[j];
     }
 };
-struct RedTrialM {       // [sum rp^2, sum y^2]
-    const double *rp, *y;
-    __device__ static constexpr int op(int) { return OP_SUM; }
+struct RedTrialM {       // [sum rp^2, sum y^2, max |rp/R|, sum b y]
+    const double *rp, *y, *R, *b;
+    __device__ static constexpr int op(int r) { return r == 2 ? OP_MAX : OP_SUM; }
     __device__ void operator()(int i, double* v) const {
         v[0] = rp[i] * rp[i];
         v[1] = y[i] * y[i];
+        v[2] = fabs(rp[i] / R[i]);
+        v[3] = b[i] * y[i];
     }
 };
-struct RedTrialN {       // [sum rd^2, sum x s, min x, min s]
-    const double *rd, *x, *s;
-    __device__ static constexpr int op(int r) { return r >= 2 ? OP_MIN : OP_SUM; }
+struct RedTrialN {       // [sum rd^2, sum x s, min x, min s, max |rd/C|, sum c x]
+    const double *rd, *x, *s, *C, *c;
+    __device__ static constexpr int op(int r) { return (r == 2 || r == 3) ? OP_MIN : r == 4 ? OP_MAX : OP_SUM; }
     __device__ void operator()(int j, double* v) const {
         v[0] = rd[j] * rd[j];
         v[1] = x[j] * s[j];
         v[2] = x[j];
         v[3] = s[j];
+        v[4] = fabs(rd[j] / C[j]);
+        v[5] = c[j] * x[j];
     }
 };
 
@@ -1292,12 +1297,20 @@ void DeviceIPM::run() {
         const double eta = 0.995, armijo = 1e-4;
         std::vector<int> dir(nlp, 0), bt(nlp, 0);
         std::vector<char> decided(nlp, 1), accepted(nlp, 0);
-        std::vector<double> merit0(nlp, 0.0);
+        std::vector<double> merit0(nlp, 0.0), dist0(nlp, 0.0);
+        std::vector<char> near(nlp, 0);
         bool need_centred = false;
         for (int k = 0; k < nlp; ++k) {
             if (!I.active[k]) continue;
             decided[k] = 0;
             merit0[k] = nrp[k] / I.rp0[k] + nrd[k] / I.rd0[k] + mu[k] / I.mu0[k];
+            // near-optimal: primal and dual infeasibility already well inside the relative
+            // stopping test; progress may then also be judged by the test itself (below)
+            const LpResult& r = I.res[k];
+            near[k] = !o.strict && o.criteria == SK_CRIT_RELATIVE && r.rel_pinf <= kNearFeas * o.tol &&
+                      r.rel_dinf <= kNearFeas * o.tol;
+            dist0[k] = std::max({r.rel_pinf, r.rel_dinf,
+                                 std::fabs(r.objective - hm[k * 3 + 2]) / (1.0 + std::fabs(r.objective))});
             dir[k] = okc[k] ? 0 : 1;
             ap[k] = std::min(1.0, eta * cd.rx[k]);
             ad[k] = std::min(1.0, eta * cd.rs[k]);
@@ -1341,14 +1354,14 @@ void DeviceIPM::run() {
                                               I.xt.ptr, I.stt.ptr);
             k_trial_m<<<nblk(M), 256, 0, st>>>(M, I.y.ptr, I.dy.ptr, d_ad, I.row_lp.ptr, I.yt.ptr);
             residuals(I.xt.ptr, I.yt.ptr, I.stt.ptr, I.rpt.ptr, I.rdt.ptr);
-            I.reduce_rows<2>(RedTrialM{I.rpt.ptr, I.yt.ptr}, I.redout.ptr);
-            I.reduce_cols<4>(RedTrialN{I.rdt.ptr, I.xt.ptr, I.stt.ptr}, I.redout.ptr + nlp * 2);
-            std::vector<double> h = I.fetch(static_cast<size_t>(nlp) * 6);
+            I.reduce_rows<4>(RedTrialM{I.rpt.ptr, I.yt.ptr, I.R.ptr, I.b.ptr}, I.redout.ptr);
+            I.reduce_cols<6>(RedTrialN{I.rdt.ptr, I.xt.ptr, I.stt.ptr, I.C.ptr, I.c.ptr}, I.redout.ptr + nlp * 4);
+            std::vector<double> h = I.fetch(static_cast<size_t>(nlp) * 10);
             bool want_centred = false;
             for (int k = 0; k < nlp; ++k) {
                 if (decided[k]) continue;
-                const double rpn = std::sqrt(h[k * 2]), yn = std::sqrt(h[k * 2 + 1]);
-                const double* q = h.data() + nlp * 2 + k * 4;
+                const double rpn = std::sqrt(h[k * 4]), yn = std::sqrt(h[k * 4 + 1]);
+                const double* q = h.data() + nlp * 4 + k * 6;
                 const double rdn = std::sqrt(q[0]), mun = q[1] / nn[k], minx = q[2], mins = q[3];
                 const double merit = rpn / I.rp0[k] + rdn / I.rd0[k] + mun / I.mu0[k];
                 const double stp = std::min(ap[k], ad[k]);
@@ -1357,7 +1370,20 @@ void DeviceIPM::run() {
                                     std::isfinite(mins) && std::isfinite(ap[k]) && std::isfinite(ad[k]) &&
                                     std::isfinite(yn);
                 const bool positive = minx > 0.0 && mins > 0.0 && mun > 0.0 && stp > 0.0;
-                const bool progress = merit < merit0[k] && merit <= (1.0 - armijo * stp) * merit0[k];
+                bool progress = merit < merit0[k] && merit <= (1.0 - armijo * stp) * merit0[k];
+                if (!progress && near[k] && finite && positive) {
+                    // Near the optimum the merit's residual terms can outweigh its mu term
+                    // although the step closes the gap: an inexact FP64 direction (normal
+                    // equations beyond FP64's reach) adds primal infeasibility far below the
+                    // tolerance and the merit rejects every step (an LP stalled at rel. gap
+                    // 3e-8 that way). Such a trial is accepted when it stays near-feasible
+                    // and its distance to the stopping test falls by the Armijo factor.
+                    const double tp = h[k * 4 + 2] / (1.0 + I.binf[k]), td = q[4] / (1.0 + I.cinf[k]);
+                    const double tobj = q[5], tby = h[k * 4 + 3];
+                    const double tdist = std::max({tp, td, std::fabs(tobj - tby) / (1.0 + std::fabs(tobj))});
+                    progress = tp <= kNearFeas * o.tol && td <= kNearFeas * o.tol && std::isfinite(tdist) &&
+                               tdist <= (1.0 - armijo * stp) * dist0[k];
+                }
                 if (o.verbose > 1 && k < 4)
                     std::fprintf(stderr, "[sk]   trial lp %d dir %d bt %d ap %.3e ad %.3e merit %.6e -> %.6e minx %.2e mins %.2e %s\n",
                                  k, dir[k], bt[k], ap[k], ad[k], merit0[k], merit, minx, mins,
