@@ -1,19 +1,41 @@
-"""Benchmark of the device Mehrotra IPM on the block-angular LP (family 1:
-40 blocks of 500x1200 + 2000 linking rows, m=22000, n=48000, 288k nnz).
+"""Benchmark of the device Mehrotra IPM: mixed precision + learned start against the
+plain FP64 IPM, on one GB300.
 
-A step is one complete solve to 1e-8 relative primal / dual infeasibility and
-duality gap, mixed precision (FP32 fronts, FP64 residuals and refinement, FP64
-switch near convergence). value = LPs/s with the LP resident in device memory
-(CUDA events around sk_solver_run on the solver stream); e2e = LPs/s through the
-one-shot C ABI call sk_ipm_solve_csc from host arrays (analysis, upload, solve
-and download inside the timed region).
+Headline workload: the uneven batch of 512 independent LPs (family 3:
+m ~ logUniform[200, 5000], n = ceil(m U[2, 3]), density 0.5-2 %, instances
+0..511; 763,585 rows, 1,925,793 columns, 61 M nonzeros in all), solved as one
+batch to 1e-8 relative primal / dual infeasibility and duality gap per LP.
 
---impl reference times the CPU restatement of the reference algorithm (oracle/,
-plain C, FP64, dense Cholesky) on all host cores over a bounded sample of the
-same LP family (see cpu_sample()).
+A step is one complete batched solve of the 512 LPs in mixed precision (FP32
+fronts with TF32 x3 tensor-core updates while the directions pass the accuracy
+check, FP64 fronts after the switch with FP64-accurate tensor-core updates; FP64
+residuals, operator and PCG throughout) started from the learned point (the
+bipartite network's prediction, falling back per LP to Mehrotra's start).
+value = LPs/s with the batch resident in device memory (CUDA events around
+sk_solver_run on the solver stream); the A matrices of the batch (0.73 GB of CSR
+and CSC arrays) exceed the 129 MB L2 and a 256 MB buffer is written before every
+step. e2e = the same LPs/s through the C ABI from host arrays (sk_solver_create:
+host analysis and upload; sk_solver_run; sk_solver_result: download of x, y, s of
+every LP), all inside the timed region.
+
+The line also carries the plain FP64 IPM on the same batch (unit start, FP64
+fronts on the FP64 pipe: the comparison the metric names), the 512 LPs solved
+one at a time by the plain FP64 IPM (config 3's "sequential plain solves"), the
+precision-only gain (mixed vs FP64, both from the unit start), the family-2
+staircase LP's time-to-1e-8 (m=200000), the family-1 block-angular LP, the
+learned start on held-out seeds (config 4), kernel rooflines and a CPU baseline.
+The compact comparison blocks are printed last in the line.
+
+--impl reference times a CPU implementation of the path on the host cores over a
+bounded, stratified sample of the same 512-LP batch, built by the oracle's own copy
+of the generator (no product code is loaded): the reference's own CPU simplex
+(oracle/_ref, built from the reference sources) where that library exists, else the
+CPU restatement of the reference's Mehrotra IPM (oracle/sk_oracle.c, FP64 dense
+Cholesky); `kind` says which ran.
 """
 import argparse
 import json
+import multiprocessing as mp
 import os
 import statistics
 import subprocess
@@ -21,12 +43,18 @@ import sys
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
-sys.path.insert(0, os.path.join(ROOT, "soverign-gpu-accelerator-_gb300"))
-sys.path.insert(0, os.path.join(ROOT, "oracle"))
+PKG = os.path.join(ROOT, "soverign-gpu-accelerator-_gb300")
+ORACLE = os.path.join(ROOT, "oracle")
+for _p in (PKG, ORACLE):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
 
 METRIC = "time-to-1e-8 gap & LPs/sec: mixed+learned vs plain FP64 IPM, same GB300"
-WORKLOAD = "block-angular LP, 40 blocks of 500x1200 + 2000 linking rows (m=22000, n=48000, 6 nnz/col), seed 0xC1"
-FULL_NNZ = 288000
+BATCH = 512
+WORKLOAD = ("uneven batch of 512 independent LPs solved as one batch (family 3: m ~ logUniform[200,5000], "
+            "n = ceil(m U[2,3]), density 0.5-2%, instances 0..511; 763585 rows, 1925793 cols, 61.0 M nnz)")
+WEIGHTS = os.path.join(PKG, "weights", "learned_start_family3.npy")
+HELDOUT0 = 200100          # first held-out family-3 seed (training: 100000..; tuning: 200000..200099)
 
 
 def peaks():
@@ -37,22 +65,12 @@ def peaks():
         return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), "measured"
     return 6800.0, 1900.0, "fallback"
 
-
 def ensure_built():
     import sankhya_gb300 as sk
     if not os.path.exists(sk.LIB_PATH):
         import __graft_entry__ as g
         g.build()
     return sk
-
-
-def cpu_sample(sk):
-    """Bounded CPU sample of the workload: one block of the same family
-    (500x1200 block + 50 linking rows, m=550, n=1200, 7200 nnz = 1/40 of the full
-    LP's nonzeros). CPU LPs/s on the full LP is reported as the sample rate x
-    7200/288000 (linear in nnz, which favours the CPU: its dense factorisation
-    grows as m^3)."""
-    return sk.block_angular(0xC1, 1, 500, 1200, 50, 5)
 
 
 class Clocks:
@@ -128,148 +146,6 @@ def count_kernel_launches(fn):
         return None
 
 
-WEIGHTS = os.path.join(ROOT, "soverign-gpu-accelerator-_gb300", "weights", "learned_start_family3.npy")
-
-
-def batch_comparison(sk, nlps, dist=None, rank=0, world=1):
-    """LPs/s on the first `nlps` members of the 512-LP uneven batch (family 3),
-    solved as one batch: mixed precision + learned start (falling back per LP to
-    Mehrotra's start), mixed precision + Mehrotra's start, and the plain FP64 IPM
-    (unit start); device time of the second of two runs of each. Then the plain
-    FP64 IPM on the same LPs one at a time (sequential solves). With several ranks
-    the LPs are sharded (sharding.shard_lps): each rank solves its own LPs as one
-    batch, the time is the slowest rank's and the per-LP results are gathered to
-    rank 0 once per arm; no other communication."""
-    import sharding
-    lps_all = [sk.generate(3, k) for k in range(nlps)]
-    shards = sharding.shard_lps([sharding.lp_cost(lp.m, lp.n, lp.nnz) for lp in lps_all], world)
-    mine = shards[rank]
-    lps = [lps_all[k] for k in mine]
-    net = None
-    if os.path.exists(WEIGHTS):
-        net = sk.Gnn(1)
-        net.load(WEIGHTS)
-    out = {"lps": nlps, "members": "family-3 instances 0..%d (m %d..%d)" % (
-        nlps - 1, min(lp.m for lp in lps_all), max(lp.m for lp in lps_all))}
-    if world > 1:
-        out["sharding"] = {"ranks": world, "lps_per_rank": [len(sh) for sh in shards]}
-    arms = [("mixed_learned", sk.PREC_MIXED, sk.START_LEARNED), ("mixed_mehrotra", sk.PREC_MIXED, sk.START_MEHROTRA),
-            ("plain_fp64", sk.PREC_FP64, sk.START_UNIT)]
-    for name, prec, start in arms:
-        if start == sk.START_LEARNED and net is None:   # the same weights file on every rank
-            continue
-        infos, ms = [], 0.0
-        if lps:
-            s = sk.Solver(lps, precision=prec, start=start)
-            if start == sk.START_LEARNED:
-                s.set_gnn(net)
-            s.run()
-            s.run()
-            infos = [s.result(k, want_vectors=False)[0] for k in range(len(lps))]
-            s.close()
-            ms = infos[0]["device_ms"]
-        ms = barrier_max(dist, ms)
-        per_lp = sharding.gather_results({mine[q]: {"status": i["status"], "iterations": i["iterations"],
-                                                    "learned_start": i["learned_start"]}
-                                          for q, i in enumerate(infos)}, dist, rank, world)
-        if per_lp is None:
-            continue
-        vals = [per_lp[k] for k in range(nlps)]
-        out[name] = {"ms": ms, "lps_per_s": 1000.0 * nlps / ms, "all_optimal": all(v["status"] == 0 for v in vals),
-                     "mean_iterations": sum(v["iterations"] for v in vals) / nlps}
-        if start == sk.START_LEARNED:
-            out[name]["learned_used"] = sum(v["learned_start"] for v in vals)
-    if net is not None:
-        net.close()
-    if "plain_fp64" in out:
-        base = out["plain_fp64"]["lps_per_s"]
-        for name in ("mixed_learned", "mixed_mehrotra"):
-            if name in out:
-                out[name]["speedup_vs_plain_fp64"] = out[name]["lps_per_s"] / base
-    # the same LPs solved one after another by the plain FP64 IPM, one LP per solver (how the
-    # reference's device IPM is used); device time of the second of two runs of each
-    try:
-        seq_ms, seq_ok = 0.0, True
-        for lp in lps:
-            s = sk.Solver([lp], precision=sk.PREC_FP64, start=sk.START_UNIT)
-            s.run()
-            s.run()
-            info, *_ = s.result(0, want_vectors=False)
-            s.close()
-            seq_ms += info["device_ms"]
-            seq_ok = seq_ok and info["status"] == 0
-        seq_ms = barrier_max(dist, seq_ms)
-        oks = sharding.gather_results({rank: seq_ok}, dist, rank, world)
-        if oks is not None:
-            out["sequential_plain_fp64"] = {"ms": seq_ms, "lps_per_s": 1000.0 * nlps / seq_ms,
-                                            "all_optimal": all(oks.values())}
-            for name in ("mixed_learned", "mixed_mehrotra", "plain_fp64"):
-                if name in out:
-                    out[name]["speedup_vs_sequential_plain_fp64"] = out[name]["lps_per_s"] / (1000.0 * nlps / seq_ms)
-    except Exception as e:          # the comparison is auxiliary: report, do not lose the bench line
-        out["sequential_plain_fp64"] = {"error": "%s: %s" % (type(e).__name__, e)}
-    return out
-
-
-def family2_comparison(sk, unit_start_arm=False):
-    """Time-to-1e-8 on the family-2 staircase LP (m=200000, n=500000): mixed precision with
-    the learned start (falling back to Mehrotra's start), mixed precision with the plain
-    method's unit start, and the plain FP64 IPM. One solve per arm (each solve is tens of
-    seconds); host analysis (ordering, plan) is timed separately from the device solve."""
-    lp = sk.generate(2, 0)
-    ref = None
-    fixture = os.path.join(ROOT, "tests", "golden", "highs_large_objectives.json")
-    if os.path.exists(fixture):
-        with open(fixture) as f:
-            for c in json.load(f)["cases"]:
-                if c["name"] == "family2_0" and c["digest"]["nnz"] == lp.nnz:
-                    ref = c["objective"]
-    net = None
-    if os.path.exists(WEIGHTS):
-        net = sk.Gnn(1)
-        net.load(WEIGHTS)
-    out = {"workload": "staircase transportation LP, 50 stages (m=200000, n=500000, 4 nnz/col), seed 0xC2",
-           "objective_reference": "HiGHS (tests/golden/highs_large_objectives.json)" if ref is not None else None}
-    arms = [("mixed_learned", sk.PREC_MIXED, sk.START_LEARNED), ("mixed_unit_start", sk.PREC_MIXED, sk.START_UNIT),
-            ("plain_fp64", sk.PREC_FP64, sk.START_UNIT)]
-    if not unit_start_arm:
-        arms = [a for a in arms if a[0] != "mixed_unit_start"]
-    for name, prec, start in arms:
-        if start == sk.START_LEARNED and net is None:
-            continue
-        t0 = time.perf_counter()
-        s = sk.Solver([lp], precision=prec, start=start)
-        t1 = time.perf_counter()
-        if start == sk.START_LEARNED:
-            s.set_gnn(net)
-        s.run()
-        info, *_ = s.result(0, want_vectors=False)
-        t2 = time.perf_counter()
-        if name == "mixed_learned":
-            # instrumented replay of one FP32 factorisation at the final iterate (not part of the solve time)
-            out["profile_fp32"] = s.profile(fp32=True)
-        s.close()
-        arm = {"status": info["status"], "iterations": info["iterations"], "device_ms": info["device_ms"],
-               "analysis_s": t1 - t0, "wall_s": t2 - t0, "objective": info["objective"],
-               "rel_pinf": info["rel_pinf"], "rel_dinf": info["rel_dinf"], "rel_gap": info["rel_gap"],
-               "precision_path": info["precision_path"], "switch_iteration": info["switch_iteration"],
-               "factorizations": info["factorizations"], "solves": info["solves"],
-               "nnz_factor": info["nnz_factor"], "flops_per_factorization": info["flops_factor"]}
-        if start == sk.START_LEARNED:
-            arm["learned_used"] = info["learned_start"]
-        if ref is not None:
-            arm["rel_obj_err_vs_highs"] = abs(info["objective"] - ref) / (1.0 + abs(ref))
-        out[name] = arm
-    if net is not None:
-        net.close()
-    base = out["plain_fp64"]
-    for name in ("mixed_learned", "mixed_unit_start"):
-        if name in out:
-            out[name]["speedup_device_vs_plain_fp64"] = base["device_ms"] / out[name]["device_ms"]
-            out[name]["speedup_wall_vs_plain_fp64"] = base["wall_s"] / out[name]["wall_s"]
-    return out
-
-
 def _block_diag_csr(parts, col_offsets):
     """Concatenates per-LP CSR arrays (row_ptrs, col_idx, vals) into the CSR of the
     block-diagonal matrix, shifting each block's columns by its offset."""
@@ -287,7 +163,7 @@ def _block_diag_csr(parts, col_offsets):
             np.ascontiguousarray(np.concatenate(vs)))
 
 
-def spmv_rooflines(sk, hbm, src, nlps=512, warm=3, reps=10):
+def spmv_rooflines(sk, lps, hbm, src, warm=3, reps=10):
     """HBM roofline of the solver's SpMV kernel (autotuned plan, sk_spmv_plan_*) for
     y = A x and y = A^T x on the block-diagonal matrix of the family-3 batch (512
     LPs: 61 M nonzeros, 0.73 GB of CSR indices and values per product, several times
@@ -298,13 +174,12 @@ def spmv_rooflines(sk, hbm, src, nlps=512, warm=3, reps=10):
     is timed the same way for comparison, and the two results are compared."""
     import numpy as np
     import torch
-    lps = [sk.generate(3, k) for k in range(nlps)]
+    nlps = len(lps)
     roff = np.cumsum([0] + [lp.m for lp in lps])[:-1]
     coff = np.cumsum([0] + [lp.n for lp in lps])[:-1]
     M, N = sum(lp.m for lp in lps), sum(lp.n for lp in lps)
     mats = [("A x", M, N, _block_diag_csr([lp.csr() for lp in lps], coff)),
             ("A^T y", N, M, _block_diag_csr([(lp.col_ptrs, lp.row_idx, lp.vals) for lp in lps], roff))]
-    del lps
     stream = torch.cuda.current_stream()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     out = []
@@ -401,22 +276,191 @@ def barrier_max(dist, v):
     return float(t.item())
 
 
+def load_net(sk):
+    if not os.path.exists(WEIGHTS):
+        raise SystemExit("learned-start weights missing: %s" % WEIGHTS)
+    net = sk.Gnn(1)
+    net.load(WEIGHTS)
+    return net
+
+
+def batch_stats(solver, nlps):
+    infos = [solver.result(k, want_vectors=False)[0] for k in range(nlps)]
+    its = [i["iterations"] for i in infos]
+    return infos, {"all_optimal": all(i["status"] == 0 for i in infos),
+                   "optimal": sum(1 for i in infos if i["status"] == 0),
+                   "mean_iterations": sum(its) / nlps, "max_iterations": max(its),
+                   "max_rel_gap": max(i["rel_gap"] for i in infos),
+                   "max_rel_pinf": max(i["rel_pinf"] for i in infos),
+                   "max_rel_dinf": max(i["rel_dinf"] for i in infos)}
+
+
+def batch_arm(sk, lps, prec, start, net=None, runs=1, **opts):
+    """`runs` batched solves of `lps` on one solver; device time of the last run and
+    per-LP statistics of the last run (the kernels are already loaded and tuned by
+    earlier solves in the process, so one run is a warm measurement)."""
+    t0 = time.perf_counter()
+    s = sk.Solver(lps, precision=prec, start=start, **opts)
+    setup = time.perf_counter() - t0
+    if start == sk.START_LEARNED:
+        s.set_gnn(net)
+    ms = []
+    for _ in range(runs):
+        s.run()
+        ms.append(s.result(0, want_vectors=False)[0]["device_ms"])
+    infos, st = batch_stats(s, len(lps))
+    s.close()
+    out = {"ms": ms[-1], "lps_per_s": 1000.0 * len(lps) / ms[-1], "setup_s": setup}
+    out.update(st)
+    if start == sk.START_LEARNED:
+        used = sum(i["learned_start"] for i in infos)
+        out["learned_used"] = used
+        out["fallback_rate"] = 1.0 - used / len(lps)
+    return out, infos
+
+
+def sequential_plain(sk, lps):
+    """The LPs solved one after another by the plain FP64 IPM (unit start), one LP per
+    solver, as the reference's device IPM is used: sum of the device times of one
+    solve each (after a warm-up solve of the first LP); host set-up timed apart."""
+    w = sk.Solver([lps[0]], precision=sk.PREC_FP64, start=sk.START_UNIT)
+    w.run()
+    w.close()
+    tot, ok, setup, its = 0.0, 0, 0.0, 0
+    for lp in lps:
+        t = time.perf_counter()
+        s = sk.Solver([lp], precision=sk.PREC_FP64, start=sk.START_UNIT)
+        setup += time.perf_counter() - t
+        s.run()
+        info, *_ = s.result(0, want_vectors=False)
+        s.close()
+        tot += info["device_ms"]
+        ok += info["status"] == 0
+        its += info["iterations"]
+    return {"ms": tot, "lps_per_s": 1000.0 * len(lps) / tot, "optimal": ok, "all_optimal": ok == len(lps),
+            "mean_iterations": its / len(lps), "host_setup_s": setup}
+
+
+def family2_comparison(sk, net):
+    """Time-to-1e-8 on the family-2 staircase LP (m=200000, n=500000): mixed precision
+    with the learned start (falling back to Mehrotra's start) against the plain FP64
+    IPM (unit start); one solve per arm; host analysis (ordering, plan) timed apart
+    from the device solve."""
+    lp = sk.generate(2, 0)
+    out = {}
+    prof = None
+    for name, prec, start in (("mixed_learned", sk.PREC_MIXED, sk.START_LEARNED),
+                              ("plain_fp64", sk.PREC_FP64, sk.START_UNIT)):
+        t0 = time.perf_counter()
+        s = sk.Solver([lp], precision=prec, start=start)
+        t1 = time.perf_counter()
+        if start == sk.START_LEARNED:
+            s.set_gnn(net)
+        s.run()
+        info, *_ = s.result(0, want_vectors=False)
+        t2 = time.perf_counter()
+        if name == "mixed_learned":
+            prof = s.profile(fp32=True)      # instrumented replay, not part of the solve time
+        s.close()
+        out[name] = {"status": info["status"], "iterations": info["iterations"], "device_s": info["device_ms"] / 1e3,
+                     "analysis_s": t1 - t0, "wall_s": t2 - t0, "objective": info["objective"],
+                     "rel_gap": info["rel_gap"], "switch_iteration": info["switch_iteration"]}
+        if start == sk.START_LEARNED:
+            out[name]["learned_used"] = info["learned_start"]
+    m, p = out["mixed_learned"], out["plain_fp64"]
+    out["speedup_device"] = p["device_s"] / m["device_s"]
+    out["speedup_wall"] = p["wall_s"] / m["wall_s"]
+    out["rel_obj_diff"] = abs(m["objective"] - p["objective"]) / (1.0 + abs(p["objective"]))
+    return out, prof
+
+
+def family1_comparison(sk):
+    """Family-1 block-angular LP (m=22000, n=48000): mixed precision vs plain FP64, device
+    time of the second of two solves each."""
+    lp = sk.generate(1, 0)
+    out, profs = {}, {}
+    for name, prec in (("mixed", sk.PREC_MIXED), ("plain_fp64", sk.PREC_FP64)):
+        s = sk.Solver([lp], precision=prec, start=sk.START_UNIT)
+        s.run()
+        s.run()
+        info, *_ = s.result(0, want_vectors=False)
+        profs[name] = s.profile(fp32=(prec == sk.PREC_MIXED))
+        s.close()
+        out[name] = {"ms": info["device_ms"], "iterations": info["iterations"], "status": info["status"],
+                     "switch_iteration": info["switch_iteration"]}
+    out["speedup"] = out["plain_fp64"]["ms"] / out["mixed"]["ms"]
+    return out, profs
+
+
+def heldout_comparison(sk, net, count, batch):
+    """The learned start on held-out family-3 seeds (instances 200100.., never used in
+    training or tuning), solved in batches of `batch`: mixed + learned against mixed
+    + Mehrotra's start (the fallback); iterations, fallback rate and time-to-1e-8."""
+    agg = {"mixed_learned": [0.0, 0, 0, 0, 0], "mixed_mehrotra": [0.0, 0, 0, 0, 0]}   # ms, iters, optimal, used, n
+    for b0 in range(0, count, batch):
+        lps = [sk.generate(3, HELDOUT0 + k) for k in range(b0, min(count, b0 + batch))]
+        for name, start in (("mixed_learned", sk.START_LEARNED), ("mixed_mehrotra", sk.START_MEHROTRA)):
+            r, infos = batch_arm(sk, lps, sk.PREC_MIXED, start, net)
+            a = agg[name]
+            a[0] += r["ms"]
+            a[1] += sum(i["iterations"] for i in infos)
+            a[2] += r["optimal"]
+            a[3] += sum(i["learned_start"] for i in infos)
+            a[4] += len(lps)
+    out = {"lps": count, "seeds": "family-3 instances %d..%d" % (HELDOUT0, HELDOUT0 + count - 1),
+           "batch": batch}
+    for name, a in agg.items():
+        out[name] = {"s": a[0] / 1e3, "lps_per_s": 1000.0 * a[4] / a[0], "mean_iterations": a[1] / a[4],
+                     "optimal": a[2]}
+    out["mixed_learned"]["fallback_rate"] = 1.0 - agg["mixed_learned"][3] / count
+    out["iterations_saved"] = out["mixed_mehrotra"]["mean_iterations"] - out["mixed_learned"]["mean_iterations"]
+    out["time_ratio_learned_vs_mehrotra"] = out["mixed_learned"]["s"] / out["mixed_mehrotra"]["s"]
+    return out
+
+
+def update_roofline(prof, kernel, peak, src, workload):
+    u = prof["update"]
+    ach = prof["update_flops"] / (u["ms"] / 1000.0) / 1e12 if u["ms"] > 0 else 0.0
+    return {"kernel": "%s (%s)" % (kernel, workload), "bound": "tensor", "achieved": ach, "peak": peak,
+            "unit": "TFLOP/s", "frac": ach / peak,
+            "peak_source": "%s bf16 dense tensor peak (MEASURED_PEAKS.json bf16_tflops)" % src, "traffic": None,
+            "launches": u["launches"], "ms_total": u["ms"], "algorithmic_flops": prof["update_flops"],
+            "note": "FP64 flops of the trailing updates (sum over fronts of 2 w t(t+1)/2 per tile step) over the "
+                    "update class's event-timed duration in an instrumented replay of one factorisation"}
+
+
+def solve_roofline(prof, nnz_factor, elem, hbm, src, workload, kernel):
+    """Triangular solve (forward + backward) of an instrumented replay: each factor entry is
+    read once per direction (algorithmic bytes = 2 nnz(L) x element size)."""
+    ms = prof["fwd_solve"]["ms"] + prof["bwd_solve"]["ms"]
+    nbytes = 2.0 * nnz_factor * elem
+    ach = nbytes / (ms / 1000.0) / 1e9 if ms > 0 else 0.0
+    return {"kernel": "%s (%s)" % (kernel, workload), "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
+            "frac": ach / hbm, "peak_source": "%s copy bandwidth (MEASURED_PEAKS.json hbm_gbs)" % src,
+            "traffic": None, "ms_total": ms, "algorithmic_bytes": nbytes,
+            "launches": prof["fwd_solve"]["launches"] + prof["bwd_solve"]["launches"]}
+
+
 def run_ours(args):
     rank, world, dist = dist_setup(args)
     sk = ensure_built()
-    import numpy as np
+    import sharding
     import torch
-    dev = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(dev)
-    os.environ.setdefault("CUDA_VISIBLE_DEVICES", os.environ.get("CUDA_VISIBLE_DEVICES", ""))
-    lp = sk.generate(1, 0)
-    solver = sk.Solver([lp], precision=sk.PREC_MIXED)
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    lps_all = [sk.generate(3, k) for k in range(args.batch)]
+    shards = sharding.shard_lps([sharding.lp_cost(lp.m, lp.n, lp.nnz) for lp in lps_all], world)
+    lps = [lps_all[k] for k in shards[rank]]
+    net = load_net(sk)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")   # 256 MB > 129 MB L2
+    t0 = time.perf_counter()
+    solver = sk.Solver(lps, precision=sk.PREC_MIXED, start=sk.START_LEARNED)
+    setup_s = time.perf_counter() - t0
+    solver.set_gnn(net)
     for _ in range(args.warmup):
         solver.run()
-    info0, *_ = solver.result(0, want_vectors=False)
-    if info0["status"] != 0:
-        raise SystemExit("warm-up solve did not converge: %s" % info0)
+    _, st0 = batch_stats(solver, len(lps))
+    if not st0["all_optimal"]:
+        raise SystemExit("warm-up batch solve left LPs unsolved: %s" % st0)
     clocks = Clocks()
     if dist:
         dist.barrier()
@@ -428,179 +472,269 @@ def run_ours(args):
         flush.zero_()
         torch.cuda.synchronize()
         solver.run()
-        info, *_ = solver.result(0, want_vectors=False)
-        assert info["status"] == 0, info
-        dev_ms.append(info["device_ms"])
+        dev_ms.append(solver.result(0, want_vectors=False)[0]["device_ms"])
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
     clk = clocks.stop()
+    infos, st = batch_stats(solver, len(lps))
     total_ms = barrier_max(dist, sum(dev_ms))
-    value = world * args.steps / (total_ms / 1000.0)
-    # kernels per solve, counted on one more (untimed) run of the same solve
+    value = args.batch * args.steps / (total_ms / 1000.0)
     per_run = count_kernel_launches(solver.run)
     launches = per_run * args.steps if per_run is not None else None
-    # kernel-class breakdown (instrumented replay of one factorisation + solve at the final iterate)
-    prof = solver.profile(fp32=True)                 # tensor-core FP32 updates
-    prof_simt = solver.profile(fp32=True, tensor=False)
+    prof = solver.profile(fp32=True)                 # instrumented replay of one FP32 factorisation + solve
+    prof64 = solver.profile(fp32=False)              # same, FP64 fronts (tensor-core FP64 updates)
+    nnz_factor = infos[0]["nnz_factor"]
     solver.close()
-    # plain FP64 solve of the same LP for the comparison the metric names
-    fp64 = sk.Solver([lp], precision=sk.PREC_FP64)
-    fp64.run()
-    info64, *_ = fp64.result(0, want_vectors=False)
-    fp64.run()
-    info64b, *_ = fp64.result(0, want_vectors=False)
-    prof64 = fp64.profile(fp32=False)
-    fp64.close()
-    batch = batch_comparison(sk, args.batch_lps, dist, rank, world) if args.batch_lps > 0 else None
-    family2 = None if args.no_family2 else family2_comparison(sk, args.family2_unit_start)
-    # end to end through the C ABI (host arrays in, host solution out)
+    headline = {"ms_per_batch": total_ms / args.steps, "lps_per_s": value, "setup_s": setup_s,
+                "learned_used": sum(i["learned_start"] for i in infos),
+                "fallback_rate": 1.0 - sum(i["learned_start"] for i in infos) / len(lps)}
+    headline.update(st)
+
+    # the comparison the metric names: the plain FP64 IPM (unit start) on the same batch; the
+    # precision-only gain (mixed vs FP64 from the same unit start); Mehrotra's start in mixed precision
+    arms = {}
+    if not args.quick:
+        for name, prec, start in (("plain_fp64", sk.PREC_FP64, sk.START_UNIT),
+                                  ("mixed_unit_start", sk.PREC_MIXED, sk.START_UNIT),
+                                  ("mixed_mehrotra", sk.PREC_MIXED, sk.START_MEHROTRA)):
+            a, _ = batch_arm(sk, lps, prec, start)
+            a["ms"] = barrier_max(dist, a["ms"])
+            a["lps_per_s"] = 1000.0 * args.batch / a["ms"]
+            arms[name] = a
+    seq = sequential_plain(sk, lps) if (args.sequential and world == 1 and not args.quick) else None
+
+    # end to end through the C ABI: host arrays in, x, y, s of every LP out
+    e2e_steps = max(1, min(args.steps, args.e2e_steps))
     e2e_t = []
-    for _ in range(max(1, args.steps)):
+    h2d = sum(lp.nbytes() for lp in lps)
+    d2h = sum((2 * lp.n + lp.m) * 8 for lp in lps)
+    for _ in range(e2e_steps):
         flush.zero_()
         torch.cuda.synchronize()
         t = time.perf_counter()
-        infoe, x, y, s = sk.solve(lp, precision=sk.PREC_MIXED)
+        s = sk.Solver(lps, precision=sk.PREC_MIXED, start=sk.START_LEARNED)
+        s.set_gnn(net)
+        s.run()
+        res = [s.result(k) for k in range(len(lps))]
+        s.close()
         e2e_t.append(time.perf_counter() - t)
-        assert infoe["status"] == 0
+        if not all(r[0]["status"] == 0 for r in res):
+            raise SystemExit("end-to-end batch solve left LPs unsolved")
     e2e_total = barrier_max(dist, sum(e2e_t))
-    e2e_value = world * len(e2e_t) / e2e_total
-    h2d = lp.nbytes()
-    d2h = (2 * lp.n + lp.m) * 8
+    e2e_value = args.batch * len(e2e_t) / e2e_total
+
     hbm, bf16, src = peaks()
-    fp64_peak = 1.25   # TFLOP/s, nominal dense FP64 of a GB300 (no FP64 entry in MEASURED_PEAKS.json)
-    note = ("event-timed replay of one factorisation and one triangular solve at the final iterate; "
-            "the update class includes the diagonal-tile Cholesky fused into it")
-
-    def upd_roof(p, kernel, peak, peak_src, bound):
-        u = p["update"]
-        a = p["update_flops"] / (u["ms"] / 1000.0) / 1e12 if u["ms"] > 0 else 0.0
-        return {"kernel": kernel, "bound": bound, "achieved": a, "peak": peak, "unit": "TFLOP/s", "frac": a / peak,
-                "peak_source": peak_src, "traffic": None, "launches": u["launches"], "ms_total": u["ms"],
-                "algorithmic_flops": p["update_flops"], "note": note}
-
-    def solve_roof(p, kernel, elem):
-        ms = p["fwd_solve"]["ms"] + p["bwd_solve"]["ms"]
-        nbytes = 2.0 * elem * info["nnz_factor"]          # each factor entry read once per direction
-        a = nbytes / (ms / 1000.0) / 1e9 if ms > 0 else 0.0
-        return {"kernel": kernel, "bound": "hbm", "achieved": a, "peak": hbm, "unit": "GB/s", "frac": a / hbm,
-                "peak_source": "%s copy bandwidth (MEASURED_PEAKS.json hbm_gbs)" % src, "traffic": None,
-                "ms_total": ms, "algorithmic_bytes": nbytes, "note": note}
-
-    # The dominant kernel of the mixed solve (launch list in profiles/): the FP64 trailing update of
-    # the last factorisations, an FP64-pipe-bound SIMT kernel.
-    roof = upd_roof(prof64, "k_update<double> (FP64 frontal trailing update)", fp64_peak,
-                    "nominal GB300 dense FP64 1.25 TFLOP/s (of nominal; MEASURED_PEAKS.json has no FP64 entry)",
-                    "fp64")
-    # DRAM bytes of one captured launch (ncu, profiles/k_update_fp64_family1.md): 15.1 MB read, 0 written,
-    # against 59.5 MB of operand bytes for that launch's 465 tiles (panels and C are L2 hits)
-    roof["traffic"] = 15.1e6
-    roof["traffic_note"] = ("dram__bytes_read.sum + dram__bytes_write.sum of one captured launch (465 output "
-                            "tiles; operand bytes 59.5 MB), profiles/k_update_fp64_family1.md")
-    rooflines = [roof,
-                 upd_roof(prof, "k_update_tc (FP32 frontal trailing update, tcgen05 TF32 x3; flops counted once)",
-                          bf16, "%s bf16 dense tensor peak (MEASURED_PEAKS.json bf16_tflops)" % src, "tensor"),
-                 upd_roof(prof_simt, "k_update<float> (FP32 frontal trailing update, SIMT)", bf16,
-                          "%s bf16 dense tensor peak (MEASURED_PEAKS.json bf16_tflops)" % src, "tensor"),
-                 solve_roof(prof, "k_fwd_tasks<float> + k_bwd_tasks<float> (one triangular solve pair)", 4),
-                 solve_roof(prof64, "k_fwd_tasks<double> + k_bwd_tasks<double> (one triangular solve pair)", 8)]
-    rooflines.append(assembly_roofline(prof, hbm, src, "family-1 LP, FP32 fronts", note))
-    if family2 is not None and "profile_fp32" in family2:
-        rooflines.append(assembly_roofline(family2.pop("profile_fp32"), hbm, src,
-                                           "family-2 staircase LP, FP32 fronts", note))
-    if args.spmv_lps > 0:
-        rooflines.extend(spmv_rooflines(sk, hbm, src, nlps=args.spmv_lps))
+    wl = "512-LP family-3 batch, dense normal matrices"
+    classes = {}
+    for tag, pr in (("fp32", prof), ("fp64", prof64)):
+        for k, v in pr.items():
+            if isinstance(v, dict):
+                classes["%s %s" % (k, tag)] = v["ms"]
+    rooflines = [
+        solve_roofline(prof64, nnz_factor, 8, hbm, src, wl + ", FP64 factor",
+                       "k_fwd_tasks<double> + k_bwd_tasks<double> (triangular solves)"),
+        solve_roofline(prof, nnz_factor, 4, hbm, src, wl + ", FP32 factor",
+                       "k_fwd_tasks<float> + k_bwd_tasks<float> (triangular solves)"),
+        update_roofline(prof64, "k_oz_digits + k_update_oz (FP64-accurate trailing update on the tensor cores, "
+                        "BF16 digit products; FP64 flops counted)", bf16, src, wl + ", FP64 fronts"),
+        update_roofline(prof, "k_update_tc (FP32 trailing update, tcgen05 TF32 x3; FP32 flops counted once)", bf16,
+                        src, wl + ", FP32 fronts"),
+        assembly_roofline(prof, hbm, src, wl + ", FP32 fronts", "event-timed replay of one assembly")]
+    # the dominant kernel class of one FP64 factorisation + triangular solve
+    dominant = max(rooflines[:3], key=lambda r: r["ms_total"])
+    extra = {}
+    if not args.quick:
+        if args.spmv:
+            rooflines.extend(spmv_rooflines(sk, lps_all, hbm, src))
+        f1, f1prof = family1_comparison(sk)
+        extra["family1"] = f1
+        rooflines.append(assembly_roofline(f1prof["mixed"], hbm, src, "family-1 LP, FP32 fronts",
+                                           "event-timed replay of one assembly"))
+        if args.family2:
+            f2, f2prof = family2_comparison(sk, net)
+            extra["family2"] = f2
+            if f2prof is not None:
+                rooflines.append(assembly_roofline(f2prof, hbm, src, "family-2 staircase LP, FP32 fronts",
+                                                   "event-timed replay of one assembly"))
+        if args.heldout > 0:
+            extra["family4"] = heldout_comparison(sk, net, args.heldout, args.batch)
+    net.close()
     rooflines = [r for r in rooflines if r is not None]
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(sk, cores=1)
+        cpu = cpu_sample_run(args.cpu_cap)
+        cpu["value"] = cpu.pop("lps_per_s")
+
     line = {"metric": METRIC, "value": value, "unit": "LPs/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32",
-            "data": "synthetic, seeded generator (family 1)",
-            "config": {"workload": WORKLOAD, "precision": "mixed (FP32 fronts, FP64 residuals/refinement)",
-                       "tolerance": "rel pinf, dinf, gap <= 1e-8", "l2": "256 MB buffer written between steps",
-                       "parallelism": "replicas" if world > 1 else "single GPU",
-                       "iterations": info["iterations"], "precision_path": info["precision_path"],
-                       "switch_iteration": info["switch_iteration"], "factorizations": info["factorizations"],
-                       "solves": info["solves"], "nnz_factor": info["nnz_factor"],
-                       "supernodes": info["num_supernodes"], "flops_per_factorization": info["flops_factor"]},
-            "batch_family3": batch,
-            "staircase_family2": family2,
-            "plain_fp64": {"ms_per_solve": info64b["device_ms"], "iterations": info64b["iterations"],
-                           "lps_per_s": 1000.0 / info64b["device_ms"] if info64b["device_ms"] > 0 else None,
-                           "speedup_mixed_vs_fp64": info64b["device_ms"] / (total_ms / args.steps)},
-            "kernel_breakdown_ms": {"mixed": {k: v for k, v in prof.items() if isinstance(v, dict)},
-                                    "mixed_simt_update": {k: v for k, v in prof_simt.items() if isinstance(v, dict)},
-                                    "fp64": {k: v for k, v in prof64.items() if isinstance(v, dict)}},
-            "wall_s_timed_region": wall,
+            "data": "synthetic, seeded generator (family 3, instances 0..%d)" % (args.batch - 1),
+            "config": {"workload": WORKLOAD, "lps": args.batch, "precision": "mixed (FP32/TF32x3 fronts, FP64 "
+                       "residuals/PCG, FP64 fronts with tensor-core FP64-accurate updates after the switch)",
+                       "start": "learned (per-LP fallback to Mehrotra's start)",
+                       "tolerance": "per LP rel pinf, dinf, gap <= 1e-8",
+                       "l2": "inputs 0.73 GB > L2; 256 MB buffer written before every step",
+                       "parallelism": ("LP-sharded batch over %d ranks" % world) if world > 1 else "single GPU",
+                       "mean_iterations": st["mean_iterations"], "max_iterations": st["max_iterations"],
+                       "plain_fp64_lps_per_s": arms["plain_fp64"]["lps_per_s"] if arms else None},
             "gpu_launches": launches,
-            "gpu_launches_note": "kernels of libsankhya_gb300 per solve (CUPTI trace of one extra run) x steps",
-            "roofline": roof, "kernel_rooflines": rooflines, "cpu_baseline": cpu, "clocks": clk,
+            "roofline": dominant, "cpu_baseline": cpu, "clocks": clk,
             "e2e": {"value": e2e_value, "unit": "LPs/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "ms_per_step": 1000.0 * e2e_total / len(e2e_t)}}
+                    "ms_per_step": 1000.0 * e2e_total / len(e2e_t), "steps": len(e2e_t),
+                    "path": "sk_solver_create (host analysis + upload) + sk_solver_run + sk_solver_result for "
+                            "every LP (pageable host arrays)"},
+            "kernel_rooflines": rooflines,
+            "kernel_breakdown_ms": classes,
+            "gpu_launches_note": "kernels of libsankhya_gb300 per batch solve (CUPTI trace of one extra run) x steps",
+            "wall_s_timed_region": wall,
+            "detail": {"mixed_learned": headline, "arms": arms, "sequential_plain_fp64": seq}}
+    # compact comparison blocks last (the end of the line is what a log tail keeps)
+    if arms:
+        p = arms["plain_fp64"]
+        line["config3"] = {
+            "mixed_learned_lps_per_s": value, "plain_fp64_lps_per_s": p["lps_per_s"],
+            "speedup_vs_plain_fp64": value / p["lps_per_s"],
+            "time_ratio_vs_plain_fp64": (total_ms / args.steps) / p["ms"],
+            "mixed_mehrotra_lps_per_s": arms["mixed_mehrotra"]["lps_per_s"],
+            "precision_only_speedup_unit_start": arms["mixed_unit_start"]["lps_per_s"] / p["lps_per_s"],
+            "sequential_plain_fp64_lps_per_s": seq["lps_per_s"] if seq else None,
+            "speedup_vs_sequential_plain_fp64": value / seq["lps_per_s"] if seq else None,
+            "mean_iterations": st["mean_iterations"], "plain_fp64_mean_iterations": p["mean_iterations"],
+            "all_optimal": st["all_optimal"] and p["all_optimal"], "learned_used": headline["learned_used"]}
+    if "family1" in extra:
+        f1 = extra["family1"]
+        line["config1"] = {"mixed_ms": f1["mixed"]["ms"], "plain_fp64_ms": f1["plain_fp64"]["ms"],
+                           "speedup": f1["speedup"], "iterations": f1["mixed"]["iterations"],
+                           "plain_fp64_iterations": f1["plain_fp64"]["iterations"],
+                           "status": [f1["mixed"]["status"], f1["plain_fp64"]["status"]]}
+    if "family2" in extra:
+        f2 = extra["family2"]
+        line["config2"] = {"mixed_learned_device_s": f2["mixed_learned"]["device_s"],
+                           "plain_fp64_device_s": f2["plain_fp64"]["device_s"],
+                           "speedup_device": f2["speedup_device"], "speedup_wall": f2["speedup_wall"],
+                           "mixed_learned_wall_s": f2["mixed_learned"]["wall_s"],
+                           "plain_fp64_wall_s": f2["plain_fp64"]["wall_s"],
+                           "iterations": [f2["mixed_learned"]["iterations"], f2["plain_fp64"]["iterations"]],
+                           "learned_used": f2["mixed_learned"].get("learned_used"),
+                           "rel_obj_diff": f2["rel_obj_diff"],
+                           "status": [f2["mixed_learned"]["status"], f2["plain_fp64"]["status"]]}
+    if "family4" in extra:
+        f4 = extra["family4"]
+        line["config4"] = {"heldout_lps": f4["lps"], "mean_iterations_learned": f4["mixed_learned"]["mean_iterations"],
+                           "mean_iterations_mehrotra": f4["mixed_mehrotra"]["mean_iterations"],
+                           "fallback_rate": f4["mixed_learned"]["fallback_rate"],
+                           "time_to_1e8_s_learned": f4["mixed_learned"]["s"],
+                           "time_to_1e8_s_mehrotra": f4["mixed_mehrotra"]["s"],
+                           "optimal": [f4["mixed_learned"]["optimal"], f4["mixed_mehrotra"]["optimal"]]}
     if rank == 0:
         print(json.dumps(line))
     if dist:
         dist.destroy_process_group()
 
 
-def _cpu_worker(args):
+# ---- CPU baseline -----------------------------------------------------------------------
+
+def cpu_sample_members(count=16):
+    """A stratified sample of the 512-LP batch: the members at every (512 / count)-th
+    position of the batch sorted by row count (from the smallest), so the sample spans
+    the batch's size range. Sizes come from the oracle's copy of the generator."""
     import sk_oracle as so
-    import sankhya_gb300 as sk
-    lp = cpu_sample(sk)
+    sizes = sorted(range(BATCH), key=lambda k: (so.generate_dims(3, k)[0], k))
+    stride = BATCH // count
+    return [sizes[stride // 2 + stride * q] for q in range(count)]
+
+
+def _cpu_kind():
+    import sk_oracle as so
+    return "reference" if so.have_reference() else "port"
+
+
+def _cpu_one(k, q, kind):
+    import sk_oracle as so
+    lp = so.generate(3, k)
     t = time.perf_counter()
-    r, *_ = so.ipm_solve(lp)
-    return time.perf_counter() - t, r["status"], r["objective"]
-
-
-def cpu_baseline(sk, cores=1, rounds=12):
-    """Oracle port (FP64 CPU restatement of the reference algorithm) on the
-    bounded sample; `cores` processes each solve their own copy."""
-    import multiprocessing as mp
-    import sk_oracle as so
-    so.oracle()
-    lp = cpu_sample(sk)
-    t0 = time.perf_counter()
-    if cores == 1:
-        res = [_cpu_worker(None) for _ in range(rounds)]
+    if kind == "reference":
+        st, obj, _ = so.ref_simplex(lp)
     else:
-        ctx = mp.get_context("spawn")
-        with ctx.Pool(cores) as pool:
-            res = pool.map(_cpu_worker, range(cores * rounds))
+        r, *_ = so.ipm_solve(lp)
+        st = r["status"]
+    q.put((k, lp.m, st, time.perf_counter() - t))
+
+
+def cpu_sample_run(cap, members=None, kind=None):
+    """CPU implementation of the path on the stratified sample, one LP per host core, all
+    cores at once: the reference's own CPU simplex (oracle/_ref) where it was built
+    from the reference sources, else the oracle's FP64 dense-Cholesky restatement of
+    the reference's Mehrotra IPM. A member still running after `cap` seconds is
+    stopped and counted as not finished (DNF). LPs/s = finished LPs / wall seconds of
+    the whole sample."""
+    members = members or cpu_sample_members()
+    kind = kind or _cpu_kind()
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    cores = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    procs, done, pending = {}, {}, list(members)
+    while pending or procs:
+        while pending and len(procs) < cores:
+            k = pending.pop(0)
+            p = ctx.Process(target=_cpu_one, args=(k, q, kind))
+            p.start()
+            procs[k] = (p, time.perf_counter())
+        try:
+            k, m, stt, dt = q.get(timeout=0.05)
+            done[k] = {"m": m, "status": stt, "seconds": dt}
+            procs[k][0].join()
+            del procs[k]
+        except Exception:
+            pass
+        now = time.perf_counter()
+        for k in [k for k, (p, ts) in procs.items() if now - ts > cap]:
+            procs[k][0].terminate()
+            procs[k][0].join()
+            del procs[k]
+            done[k] = {"status": "DNF"}
     wall = time.perf_counter() - t0
-    n = len(res)
-    assert all(r[1] == 0 for r in res), res[:2]
-    sample_rate = n / wall
-    return {"value": sample_rate * lp.nnz / FULL_NNZ, "unit": "LPs/s", "cores": cores, "kind": "port",
-            "sample": "%d solves of the one-block member of the family (m=%d, n=%d, nnz=%d) on %d core(s), "
-                      "%.1f s; full-LP rate = sample rate x %d/%d nnz" % (n, lp.m, lp.n, lp.nnz, cores, wall,
-                                                                       lp.nnz, FULL_NNZ),
-            "sample_lps_per_s": sample_rate}
+    fin = [k for k in members if done.get(k, {}).get("status") == 0]
+    what = ("reference CPU Phase-I + primal simplex (oracle/_ref, src/simplex/phase1.cpp:124-449)"
+            if kind == "reference" else "oracle/sk_oracle.c FP64 dense-Cholesky restatement of the reference's "
+                                        "Mehrotra IPM")
+    return {"lps_per_s": len(fin) / wall, "unit": "LPs/s", "cores": min(cores, len(members)), "kind": kind,
+            "nproc": cores, "wall_s": wall, "finished": len(fin), "dnf": [k for k in members if k not in fin],
+            "per_lp_1core_s": {str(k): round(done[k]["seconds"], 3) for k in fin},
+            "sample": ("stratified sample of the 512-LP batch: %d members (every %d-th by row count), one LP per "
+                       "core on %d cores, per-LP cap %.0f s (DNF beyond); %s"
+                       % (len(members), BATCH // len(members), min(cores, len(members)), cap, what))}
 
 
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    sk = ensure_built()
     import sk_oracle as so
     so.oracle()
-    cores = os.cpu_count() or 1
+    kind = _cpu_kind()
+    members = cpu_sample_members()
     for _ in range(args.warmup):
-        cpu_baseline(sk, cores=cores, rounds=1)
+        cpu_sample_run(args.cpu_cap, members, kind)
     vals = []
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        vals.append(cpu_baseline(sk, cores=cores, rounds=1))
+        vals.append(cpu_sample_run(args.cpu_cap, members, kind))
     wall = time.perf_counter() - t0
-    v = statistics.mean(x["value"] for x in vals)
+    v = statistics.mean(x["lps_per_s"] for x in vals)
+    last = vals[-1]
     line = {"metric": METRIC, "impl": "reference", "value": v, "unit": "LPs/s", "n_gpus": 0, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000.0 * wall / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic, seeded generator (family 1)",
-            "config": {"workload": WORKLOAD, "implementation": "CPU restatement of the reference's Mehrotra IPM "
-                       "(oracle/sk_oracle.c, dense FP64 Cholesky); the reference's own CPU code cannot be built "
-                       "on the GPU host (its sources are not there)"},
-            "cpu_baseline": {"value": v, "unit": "LPs/s", "cores": cores, "kind": "port", "sample": vals[0]["sample"]},
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic, seeded generator (family 3, oracle copy)",
+            "config": {"workload": WORKLOAD, "sample": last["sample"],
+                       "implementation": "reference's own CPU simplex" if kind == "reference" else
+                       "CPU restatement of the reference's Mehrotra IPM (the reference's own CPU code needs its "
+                       "sources, which are not on the GPU host)"},
+            "cpu_baseline": {"value": v, "unit": "LPs/s", "cores": last["cores"], "kind": kind,
+                             "nproc": last["nproc"], "sample": last["sample"], "finished": last["finished"],
+                             "dnf": last["dnf"], "per_lp_1core_s": last["per_lp_1core_s"]},
             "e2e": {"value": v, "unit": "LPs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -611,15 +745,17 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--batch", type=int, default=BATCH, help="family-3 members in the batch (instances 0..batch-1)")
+    ap.add_argument("--e2e-steps", type=int, default=3, help="end-to-end steps (at most --steps)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--batch-lps", type=int, default=32,
-                    help="family-3 batch members for the mixed+learned vs plain FP64 batch comparison (0: skip)")
-    ap.add_argument("--spmv-lps", type=int, default=512,
-                    help="family-3 members in the block-diagonal matrix of the SpMV roofline (0: skip)")
-    ap.add_argument("--no-family2", action="store_true",
-                    help="skip the family-2 staircase LP (m=200000) comparison (about 3 minutes)")
-    ap.add_argument("--family2-unit-start", action="store_true",
-                    help="add a mixed-precision unit-start arm to the family-2 comparison")
+    ap.add_argument("--cpu-cap", type=float, default=6.0, help="per-LP time cap of the CPU baseline (s)")
+    ap.add_argument("--quick", action="store_true", help="headline only (no other arms, families or rooflines)")
+    ap.add_argument("--no-sequential", dest="sequential", action="store_false",
+                    help="skip the LPs solved one at a time by the plain FP64 IPM")
+    ap.add_argument("--no-family2", dest="family2", action="store_false",
+                    help="skip the family-2 staircase LP (m=200000) comparison")
+    ap.add_argument("--heldout", type=int, default=512, help="held-out family-3 seeds for the learned start (0: skip)")
+    ap.add_argument("--no-spmv", dest="spmv", action="store_false")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -1397,19 +1397,32 @@ KktEngine::KktEngine(const ipm::FrontPlan& plan, const DeviceLP& lp, cudaStream_
         blk_off[s] = nflags_;
         nflags_ += (p.sn_ncols[s] + T64 - 1) / T64;
     }
+    // Within a level the tasks are ordered by their position in their front's chain
+    // (forward: block index; backward: distance from the last own block), fronts
+    // interleaved: blocks take tasks in list order, so the first tasks of every
+    // front of a level (e.g. all LPs of a dense batch) run side by side instead of
+    // a few fronts' chains at a time. A task only waits on tasks of smaller position
+    // in its own front, which come earlier in the list, so the earliest unfinished
+    // task can always proceed.
     std::vector<int2> ftask, btask;
     fwd_task_off_.assign(static_cast<size_t>(p.nlevels) + 1, 0);
     bwd_task_off_.assign(static_cast<size_t>(p.nlevels) + 1, 0);
     for (int l = 0; l < p.nlevels; ++l) {
         fwd_task_off_[l] = static_cast<int>(ftask.size());
         bwd_task_off_[l] = static_cast<int>(btask.size());
+        std::vector<std::pair<int, int2>> fl, bl;   // (position, task)
         for (int q = p.level_ptr[l]; q < p.level_ptr[l + 1]; ++q) {
             const int s = p.level_sn[q];
             const int nb = (p.sn_ncols[s] + T64 - 1) / T64;
             const int neb = (p.sn_nrows[s] - p.sn_ncols[s] + T64 - 1) / T64;
-            for (int i = 0; i < nb + neb; ++i) ftask.push_back(make_int2(s, i));
-            for (int i = nb - 1; i >= 0; --i) btask.push_back(make_int2(s, i));
+            for (int i = 0; i < nb + neb; ++i) fl.push_back({i, make_int2(s, i)});
+            for (int i = nb - 1; i >= 0; --i) bl.push_back({nb - 1 - i, make_int2(s, i)});
         }
+        auto by_pos = [](const std::pair<int, int2>& a, const std::pair<int, int2>& b) { return a.first < b.first; };
+        std::stable_sort(fl.begin(), fl.end(), by_pos);
+        std::stable_sort(bl.begin(), bl.end(), by_pos);
+        for (const auto& t : fl) ftask.push_back(t.second);
+        for (const auto& t : bl) btask.push_back(t.second);
     }
     fwd_task_off_[p.nlevels] = static_cast<int>(ftask.size());
     bwd_task_off_[p.nlevels] = static_cast<int>(btask.size());
