@@ -33,6 +33,8 @@ struct MehrotraOptions {
     double delta32 = 1e-8;
     double delta64 = 1e-14;
     int fp64_update = SK_FP64_UPDATE_AUTO;
+    // 1: linearly dependent rows of A are dropped before the solve (sk_options.dependent_rows)
+    int dependent_rows = 0;
     // false (default, as the reference): lb / ub of the model are ignored and x >= 0
     // is solved; true: the model's bounds are honoured through the host standard form
     // (core/standard_form.hpp).

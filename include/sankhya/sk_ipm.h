@@ -82,6 +82,11 @@ typedef struct sk_options {
                            * SK_FP64_UPDATE_NATIVE (FP64 pipe) or SK_FP64_UPDATE_TENSOR (tensor cores:
                            * BF16 digits of the FP64 panel, exact FP32 sums, results within about
                            * 2^-53 of sum |a||b|) */
+    int dependent_rows;   /* 0 (default, as the reference): every row of A is kept (a rank-deficient A is
+                           * absorbed by the delta regularisation); 1: rows of A that are linearly
+                           * dependent on the others are found (sk_presolve_dependent_rows) and, when b
+                           * is consistent, dropped before the solve; their y is returned as 0 and
+                           * sk_info.rel_pinf includes their residuals at x */
 } sk_options;
 #define SK_FP64_UPDATE_AUTO 0
 #define SK_FP64_UPDATE_NATIVE 1
@@ -110,6 +115,7 @@ typedef struct sk_info {
     double flops_factor;      /* algorithmic flops of one factorisation: sum_j c_j^2 over factor columns */
     double start_merit;       /* max(rel pinf, rel dinf, rel gap) at the start point used */
     double fallback_merit;    /* the same for Mehrotra's start (SK_START_LEARNED runs), else 0 */
+    int dependent_rows;       /* rows dropped as linearly dependent (sk_options.dependent_rows), else 0 */
 } sk_info;
 
 /* Fills the defaults listed above. */
@@ -333,6 +339,23 @@ int sk_qp_solve(int m, int n, const int* a_col_ptrs, const int* a_row_idx, const
                 const double* c, const double* lb, const double* ub, const int* h_col_ptrs, const int* h_row_idx,
                 const double* h_vals, int convexity, const sk_qp_options* opts, double* x, double* y, double* z,
                 int* status, double* info);
+
+/* ---- Presolve: linearly dependent rows of A (device) ----
+ * No counterpart in the reference (its presolve is the Ruiz scaling below; its IPM
+ * absorbs a rank-deficient A through the delta regularisation). A (m x n, CSC) and b.
+ * A A^T is factored in FP64 on the device (equilibrated to a unit diagonal, delta from
+ * 1e-12) in a fill-reducing order; a row whose pivot L_kk^2 (its squared distance from
+ * the span of the rows eliminated before it, rows normalised) is at most 1e-6 counts as
+ * linearly dependent on them (FP64 rounding through the normal equations leaves about
+ * 1e-9 on an exact dependency). b is consistent when the residual of
+ * A A^T w = b, iteratively refined on that factor, vanishes: *inconsistency (may be NULL)
+ * receives ||b - A A^T w||_inf / (1 + ||b||_inf). keep (m) receives 0 for the dependent
+ * rows when the inconsistency is at most 1e-9 (their equations then follow from the
+ * kept rows) and 1 for every row otherwise; *num_dependent receives the number of
+ * dependent rows found. Returns SK_OK, SK_ERR_INVALID, SK_ERR_NO_DEVICE,
+ * SK_ERR_NUMERICAL or SK_ERR_CUDA. */
+int sk_presolve_dependent_rows(int m, int n, const int* col_ptrs, const int* row_idx, const double* vals,
+                               const double* b, int* keep, int* num_dependent, double* inconsistency);
 
 /* ---- Presolve: Ruiz equilibration of a model (host) ----
  * Replaces: presolve::apply_ruiz_scaling(core::Model&, int max_iterations)

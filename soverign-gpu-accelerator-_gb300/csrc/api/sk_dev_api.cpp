@@ -4,7 +4,9 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
+#include <string>
 #include <memory>
 #include <vector>
 
@@ -20,8 +22,26 @@
 
 using namespace sankhya;
 
+namespace {
+// An LP with its linearly dependent rows dropped (sk_options.dependent_rows): the kept
+// rows' CSC arrays and right-hand side, and the original index of each kept row.
+struct ReducedLp {
+    std::vector<int> rows;         // original row of each kept row; empty: LP not reduced
+    std::vector<int> cp, ri;
+    std::vector<double> v, b;
+    int m_orig = 0;
+    // the dropped rows' entries (row, column, value) and right-hand sides, to measure
+    // their residual at the solution; binf = 1 + ||b||_inf of the original LP
+    std::vector<int> drop_row, drop_col;
+    std::vector<double> drop_val, drop_b;
+    double binf = 1.0;
+    bool reduced() const { return !rows.empty(); }
+};
+}  // namespace
+
 struct sk_solver {
     std::unique_ptr<dev::DeviceIPM> ipm;
+    std::vector<ReducedLp> red;    // per LP
 };
 
 struct sk_gnn {
@@ -74,6 +94,7 @@ void check_options(const sk_options& o) {
     if (o.fp64_update < SK_FP64_UPDATE_AUTO || o.fp64_update > SK_FP64_UPDATE_TENSOR)
         throw std::invalid_argument("bad fp64_update");
     if (o.ordering < SK_ORDER_AUTO || o.ordering > SK_ORDER_DISSECTION) throw std::invalid_argument("bad ordering");
+    if (o.dependent_rows != 0 && o.dependent_rows != 1) throw std::invalid_argument("bad dependent_rows");
 }
 
 void check_csc(int m, int n, const int* cp, const int* ri, const double* v, const double* b, const double* c) {
@@ -81,6 +102,172 @@ void check_csc(int m, int n, const int* cp, const int* ri, const double* v, cons
     if (cp[0] != 0) throw std::invalid_argument("col_ptrs[0] != 0");
     for (int j = 0; j < n; ++j) if (cp[j + 1] < cp[j]) throw std::invalid_argument("col_ptrs not monotone");
     if (cp[n] > 0 && (!ri || !v)) throw std::invalid_argument("invalid LP arrays");
+}
+
+// ---- linearly dependent rows of A ------------------------------------------------
+// A A^T is factored on the device in FP64 (the KKT engine: equilibrated to a unit
+// diagonal, delta from 1e-12) in its fill-reducing elimination order. The pivot L_kk^2
+// of a row is its squared distance (rows normalised) from the span of the rows
+// eliminated before it: 0 in exact arithmetic for a dependent row. Through the normal
+// equations that distance carries FP64 rounding of about 1e-9 (a 2000-row dependency
+// of a staircase LP gives 1.3e-9 and 3.2e-9 against 0.29 for the smallest independent
+// row, dense FP64 Cholesky), so a row with L_kk^2 <= kDepPivot (or 10 delta) counts as
+// dependent. b is consistent with A when b - A A^T w is ~0 for w from the regularised
+// factor with iterative refinement (which converges on the range of A A^T, and leaves
+// the part of b outside it, the inconsistency, in the residual).
+constexpr double kDepPivot = 1e-6;
+constexpr double kConsistent = 1e-9;   // inconsistency at which dependent rows are dropped
+
+struct DependentRows {
+    std::vector<char> dependent;
+    int count = 0;
+    double inconsistency = 0.0;        // ||b - A A^T w||_inf / (1 + ||b||_inf)
+};
+
+DependentRows find_dependent_rows(int m, int n, const int* cp, const int* ri, const double* v, const double* b) {
+    DependentRows out;
+    out.dependent.assign(static_cast<size_t>(m), 0);
+    const int nz = cp[n];
+    std::vector<int> rp(static_cast<size_t>(m) + 1, 0), ci(static_cast<size_t>(nz));
+    std::vector<double> cv(static_cast<size_t>(nz));
+    for (int q = 0; q < nz; ++q) {
+        if (ri[q] < 0 || ri[q] >= m) throw std::invalid_argument("row index out of range");
+        if (!std::isfinite(v[q])) throw std::invalid_argument("non-finite entry of A");
+        rp[ri[q] + 1]++;
+    }
+    for (int i = 0; i < m; ++i) {
+        if (!std::isfinite(b[i])) throw std::invalid_argument("non-finite entry of b");
+        rp[i + 1] += rp[i];
+    }
+    std::vector<int> nx(rp.begin(), rp.end() - 1);
+    for (int j = 0; j < n; ++j)
+        for (int q = cp[j]; q < cp[j + 1]; ++q) {
+            const int d = nx[ri[q]]++;
+            ci[d] = j;
+            cv[d] = v[q];
+        }
+    sk_kkt* raw = nullptr;
+    const int rc = sk_kkt_create(m, n, rp.data(), ci.data(), cv.data(), nullptr, SK_PREC_FP64, &raw);
+    if (rc != SK_OK) throw api::sk_exception(rc, std::string("dependent rows: ") + sk_last_error());
+    std::unique_ptr<sk_kkt> k(raw);
+    dev::KktEngine& E = *k->eng;
+    cudaStream_t st = k->st;
+    const std::vector<double> ones(static_cast<size_t>(n), 1.0);
+    SK_CUDA(cudaMemcpyAsync(k->theta.ptr, ones.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st));
+    double delta = 1e-12;
+    bool ok = false;
+    for (int t = 0; t < 6; ++t) {
+        if ((ok = E.factor(k->theta.ptr, delta, false))) break;
+        delta *= 10.0;
+    }
+    if (!ok) throw api::sk_exception(SK_ERR_NUMERICAL, "dependent rows: A A^T could not be factored");
+    const double tau = std::max(kDepPivot, 10.0 * delta);
+    const std::vector<double> piv = E.pivots_host();
+    const auto& perm = E.plan().perm;
+    for (int q = 0; q < m; ++q)
+        if (!(piv[q] * piv[q] > tau)) {
+            out.dependent[perm[q]] = 1;
+            ++out.count;
+        }
+    // consistency: iterative refinement of (A A^T) w = b on the regularised factor
+    double binf = 0.0;
+    for (int i = 0; i < m; ++i) binf = std::max(binf, std::fabs(b[i]));
+    std::vector<double> w(static_cast<size_t>(m), 0.0), r(b, b + m), h(static_cast<size_t>(m));
+    double best = binf;
+    for (int it = 0; it < 12 && best > 1e-15 * (1.0 + binf); ++it) {
+        SK_CUDA(cudaMemcpyAsync(k->hostio.ptr, r.data(), sizeof(double) * m, cudaMemcpyHostToDevice, st));
+        E.apply_inverse(k->hostio.ptr, k->out.ptr);
+        SK_CUDA(cudaMemcpyAsync(h.data(), k->out.ptr, sizeof(double) * m, cudaMemcpyDeviceToHost, st));
+        SK_CUDA(cudaStreamSynchronize(st));
+        for (int i = 0; i < m; ++i) w[i] += h[i];
+        SK_CUDA(cudaMemcpyAsync(k->hostio.ptr, w.data(), sizeof(double) * m, cudaMemcpyHostToDevice, st));
+        E.apply_normal(k->theta.ptr, k->hostio.ptr, k->out.ptr);
+        SK_CUDA(cudaMemcpyAsync(h.data(), k->out.ptr, sizeof(double) * m, cudaMemcpyDeviceToHost, st));
+        SK_CUDA(cudaStreamSynchronize(st));
+        double rn = 0.0;
+        for (int i = 0; i < m; ++i) {
+            r[i] = b[i] - h[i];
+            rn = std::max(rn, std::fabs(r[i]));
+        }
+        if (!(rn < best)) break;
+        best = rn;
+    }
+    if (E.solve_error()) throw api::sk_exception(SK_ERR_CUDA, "dependent rows: triangular solve timed out");
+    out.inconsistency = best / (1.0 + binf);
+    return out;
+}
+
+// With o.dependent_rows set: the LP's dependent rows are looked for and, when b is
+// consistent, dropped; red then holds the kept rows and view / bptr point at them.
+void reduce_lp(const sk_options& o, int m, int n, const int* cp, const int* ri, const double* v, const double* b,
+               ReducedLp& red, ipm::LpView& view, const double*& bptr) {
+    view.m = m; view.n = n; view.col_ptrs = cp; view.row_idx = ri; view.vals = v;
+    bptr = b;
+    red = ReducedLp();
+    red.m_orig = m;
+    if (!o.dependent_rows) return;
+    const DependentRows d = find_dependent_rows(m, n, cp, ri, v, b);
+    if (d.count == 0 || d.count >= m || d.inconsistency > kConsistent) return;
+    std::vector<int> newrow(static_cast<size_t>(m), -1), droprow(static_cast<size_t>(m), -1);
+    for (int i = 0; i < m; ++i) {
+        red.binf = std::max(red.binf, 1.0 + std::fabs(b[i]));
+        if (!d.dependent[i]) {
+            newrow[i] = static_cast<int>(red.rows.size());
+            red.rows.push_back(i);
+            red.b.push_back(b[i]);
+        } else {
+            droprow[i] = static_cast<int>(red.drop_b.size());
+            red.drop_b.push_back(b[i]);
+        }
+    }
+    red.cp.assign(1, 0);
+    for (int j = 0; j < n; ++j) {
+        for (int q = cp[j]; q < cp[j + 1]; ++q)
+            if (newrow[ri[q]] >= 0) {
+                red.ri.push_back(newrow[ri[q]]);
+                red.v.push_back(v[q]);
+            } else {
+                red.drop_row.push_back(droprow[ri[q]]);
+                red.drop_col.push_back(j);
+                red.drop_val.push_back(v[q]);
+            }
+        red.cp.push_back(static_cast<int>(red.ri.size()));
+    }
+    view.m = static_cast<int>(red.rows.size());
+    view.col_ptrs = red.cp.data();
+    view.row_idx = red.ri.data();
+    view.vals = red.v.data();
+    bptr = red.b.data();
+    if (o.verbose)
+        std::fprintf(stderr, "[sk] %d dependent rows dropped (inconsistency %.2e)\n", d.count, d.inconsistency);
+}
+
+// Result of LP lp of a solver whose LP may have been reduced: y of the dropped rows is 0,
+// and info->rel_pinf also covers the dropped rows' residuals at x (the original LP).
+void reduced_result(const dev::DeviceIPM& ipm, const ReducedLp& red, int lp, double* x, double* y, double* s,
+                    sk_info* info) {
+    if (!red.reduced()) {
+        ipm.result(lp, x, y, s, info);
+        if (info) info->dependent_rows = 0;
+        return;
+    }
+    std::vector<double> yr(red.rows.size());
+    std::vector<double> xl;
+    if (!x && info) xl.resize(static_cast<size_t>(ipm.plan().col_off[lp + 1] - ipm.plan().col_off[lp]));
+    double* xv = x ? x : (xl.empty() ? nullptr : xl.data());
+    ipm.result(lp, xv, y ? yr.data() : nullptr, s, info);
+    if (info && xv) {
+        std::vector<double> r(red.drop_b.size());
+        for (size_t q = 0; q < red.drop_row.size(); ++q) r[red.drop_row[q]] += red.drop_val[q] * xv[red.drop_col[q]];
+        double rmax = 0.0;
+        for (size_t q = 0; q < r.size(); ++q) rmax = std::max(rmax, std::fabs(r[q] - red.drop_b[q]));
+        info->rel_pinf = std::max(info->rel_pinf, rmax / red.binf);
+    }
+    if (y) {
+        std::fill(y, y + red.m_orig, 0.0);
+        for (size_t q = 0; q < red.rows.size(); ++q) y[red.rows[q]] = yr[q];
+    }
+    if (info) info->dependent_rows = red.m_orig - static_cast<int>(red.rows.size());
 }
 
 }  // namespace
@@ -95,10 +282,12 @@ int sk_ipm_solve_csc(int m, int n, const int* col_ptrs, const int* row_idx, cons
         check_options(o);
         check_csc(m, n, col_ptrs, row_idx, vals, b, c);
         ipm::LpView v;
-        v.m = m; v.n = n; v.col_ptrs = col_ptrs; v.row_idx = row_idx; v.vals = vals;
-        dev::DeviceIPM solver({v}, {b}, {c}, o);
+        ReducedLp red;
+        const double* bp = b;
+        reduce_lp(o, m, n, col_ptrs, row_idx, vals, b, red, v, bp);
+        dev::DeviceIPM solver({v}, {bp}, {c}, o);
         solver.run();
-        solver.result(0, x, y, s, info);
+        reduced_result(solver, red, 0, x, y, s, info);
         return SK_OK;
     } catch (...) {
         return api::status_of_current_exception();
@@ -118,12 +307,14 @@ int sk_ipm_solve_bounded(int m, int n, const int* col_ptrs, const int* row_idx, 
         bl.lb = lb; bl.ub = ub;
         const core::StandardForm sf = core::to_standard_form(bl);
         ipm::LpView v;
-        v.m = sf.m; v.n = sf.n; v.col_ptrs = sf.col_ptrs.data(); v.row_idx = sf.row_idx.data(); v.vals = sf.vals.data();
-        dev::DeviceIPM solver({v}, {sf.b.data()}, {sf.c.data()}, o);
+        ReducedLp red;
+        const double* bp = nullptr;
+        reduce_lp(o, sf.m, sf.n, sf.col_ptrs.data(), sf.row_idx.data(), sf.vals.data(), sf.b.data(), red, v, bp);
+        dev::DeviceIPM solver({v}, {bp}, {sf.c.data()}, o);
         solver.run();
         std::vector<double> xs(sf.n), ys(sf.m), ss(sf.n);
         sk_info in{};
-        solver.result(0, xs.data(), ys.data(), ss.data(), &in);
+        reduced_result(solver, red, 0, xs.data(), ys.data(), ss.data(), &in);
         const double obj = core::recover_solution(bl, sf, xs.data(), ys.data(), x, y, s);
         in.objective = obj;
         if (info) *info = in;
@@ -143,14 +334,14 @@ int sk_solver_create(int num_lps, const int* m, const int* n, const int* const* 
         check_options(o);
         std::vector<ipm::LpView> views(num_lps);
         std::vector<const double*> bv(num_lps), cv(num_lps);
+        std::vector<ReducedLp> red(num_lps);
+        for (int k = 0; k < num_lps; ++k) check_csc(m[k], n[k], col_ptrs[k], row_idx[k], vals[k], b[k], c[k]);
         for (int k = 0; k < num_lps; ++k) {
-            check_csc(m[k], n[k], col_ptrs[k], row_idx[k], vals[k], b[k], c[k]);
-            views[k].m = m[k]; views[k].n = n[k];
-            views[k].col_ptrs = col_ptrs[k]; views[k].row_idx = row_idx[k]; views[k].vals = vals[k];
-            bv[k] = b[k];
+            reduce_lp(o, m[k], n[k], col_ptrs[k], row_idx[k], vals[k], b[k], red[k], views[k], bv[k]);
             cv[k] = c[k];
         }
         auto* h = new sk_solver;
+        h->red = std::move(red);
         try {
             h->ipm.reset(new dev::DeviceIPM(views, bv, cv, o));
         } catch (...) {
@@ -168,7 +359,15 @@ int sk_solver_set_start(sk_solver* h, int lp, const double* x, const double* y, 
     api::clear_error();
     if (!h) return SK_ERR_INVALID;
     try {
-        h->ipm->set_start(lp, x, y, s);
+        if (lp < 0 || lp >= h->ipm->num_lps()) return SK_ERR_INVALID;
+        const ReducedLp& red = h->red[lp];
+        if (red.reduced() && y) {    // the start's y restricted to the kept rows
+            std::vector<double> yr(red.rows.size());
+            for (size_t q = 0; q < red.rows.size(); ++q) yr[q] = y[red.rows[q]];
+            h->ipm->set_start(lp, x, yr.data(), s);
+        } else {
+            h->ipm->set_start(lp, x, y, s);
+        }
         return SK_OK;
     } catch (...) {
         return api::status_of_current_exception();
@@ -190,7 +389,8 @@ int sk_solver_result(sk_solver* h, int lp, double* x, double* y, double* s, sk_i
     api::clear_error();
     if (!h) return SK_ERR_INVALID;
     try {
-        h->ipm->result(lp, x, y, s, info);
+        if (lp < 0 || lp >= h->ipm->num_lps()) return SK_ERR_INVALID;
+        reduced_result(*h->ipm, h->red[lp], lp, x, y, s, info);
         return SK_OK;
     } catch (...) {
         return api::status_of_current_exception();
@@ -408,6 +608,26 @@ int sk_kkt_set_fp64_update(sk_kkt* k, int mode) {
 }
 
 void sk_kkt_destroy(sk_kkt* k) { delete k; }
+
+int sk_presolve_dependent_rows(int m, int n, const int* col_ptrs, const int* row_idx, const double* vals,
+                               const double* b, int* keep, int* num_dependent, double* inconsistency) {
+    api::clear_error();
+    if (!keep || !num_dependent) return SK_ERR_INVALID;
+    try {
+        check_csc(m, n, col_ptrs, row_idx, vals, b, b);
+        int ndev = 0;
+        if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+            throw api::sk_exception(SK_ERR_NO_DEVICE, "no CUDA device visible");
+        const DependentRows d = find_dependent_rows(m, n, col_ptrs, row_idx, vals, b);
+        const bool drop = d.count > 0 && d.count < m && d.inconsistency <= kConsistent;
+        for (int i = 0; i < m; ++i) keep[i] = drop && d.dependent[i] ? 0 : 1;
+        *num_dependent = d.count;
+        if (inconsistency) *inconsistency = d.inconsistency;
+        return SK_OK;
+    } catch (...) {
+        return api::status_of_current_exception();
+    }
+}
 
 int sk_spmv_csr(int rows, const int* d_row_ptrs, const int* d_col_idx, const double* d_vals, const double* d_x,
                 double alpha, double beta, double* d_y, void* stream) {

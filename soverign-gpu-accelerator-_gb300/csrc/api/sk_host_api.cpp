@@ -92,6 +92,7 @@ void sk_options_default(sk_options* opt) {
     opt->delta64 = 1e-14;
     opt->learned_accept = 0.5;
     opt->fp64_update = SK_FP64_UPDATE_AUTO;
+    opt->dependent_rows = 0;
 }
 
 int sk_lp_generate(int family, int instance, sk_lp** out) {

@@ -817,6 +817,14 @@ void DeviceIPM::run() {
                 const int max_it = 60;
                 std::vector<double> best = rn, rz(nlp, 0.0), al(nlp, 0.0), be(nlp, 0.0), imp(nlp, 0.0);
                 SK_CUDA(cudaMemcpyAsync(I.bak.ptr, out, sizeof(double) * M, cudaMemcpyDeviceToDevice, st));
+                // preconditioner applications cover only the LPs still iterating (the
+                // others' rows come out 0, and their step sizes are 0)
+                std::vector<char> sub(nlp, 0);
+                auto restrict_to_running = [&]() {
+                    for (int k = 0; k < nlp; ++k) sub[k] = !done[k] && !stag[k];
+                    K.restrict_solves(sub);
+                };
+                restrict_to_running();
                 K.apply_inverse(I.r.ptr, I.pz.ptr);
                 SK_CUDA(cudaMemcpyAsync(I.pp.ptr, I.pz.ptr, sizeof(double) * M, cudaMemcpyDeviceToDevice, st));
                 I.reduce_rows<1>(RedDot{I.r.ptr, I.pz.ptr}, I.redout.ptr);
@@ -843,6 +851,7 @@ void DeviceIPM::run() {
                     for (auto& v : al) v = -v;
                     I.put_scalars(1, al);
                     k_axpy_lp<<<nblk(M), 256, 0, st>>>(M, d_ap, I.pq.ptr, I.row_lp.ptr, I.r.ptr);
+                    restrict_to_running();
                     K.apply_inverse(I.r.ptr, I.pz.ptr);
                     I.reduce_rows<2>(RedRZ{I.r.ptr, I.pz.ptr}, I.redout.ptr);
                     std::vector<double> h = I.fetch(static_cast<size_t>(nlp) * 2);
@@ -867,6 +876,7 @@ void DeviceIPM::run() {
                     I.put_scalars(2, be);
                     k_xpby_lp<<<nblk(M), 256, 0, st>>>(M, I.pz.ptr, d_ad, I.row_lp.ptr, I.pp.ptr);
                 }
+                K.unrestrict_solves();
                 SK_CUDA(cudaMemcpyAsync(out, I.bak.ptr, sizeof(double) * M, cudaMemcpyDeviceToDevice, st));
                 rn = resid_norm(rhs, out);
                 I.last_pcg = last_best_it + 1;

@@ -1793,6 +1793,7 @@ void KktEngine::upload_mask(Slot<int>& dev, std::vector<int>& host, const std::v
 }
 
 void KktEngine::set_active(const std::vector<char>& on) {
+    restricted_ = false;
     mixed_ = false;
     upload_mask(on32_, on32_h_, on);
     upload_mask(on64_, on64_h_, on);
@@ -1801,9 +1802,34 @@ void KktEngine::set_active(const std::vector<char>& on) {
 void KktEngine::set_masks(const std::vector<char>& on32, const std::vector<char>& on64) {
     for (size_t k = 0; k < on32.size() && k < on64.size(); ++k)
         if (on32[k] && on64[k]) throw std::invalid_argument("set_masks: an LP in both precisions");
+    restricted_ = false;
     mixed_ = true;
     upload_mask(on32_, on32_h_, on32);
     upload_mask(on64_, on64_h_, on64);
+}
+
+void KktEngine::restrict_solves(const std::vector<char>& sub) {
+    if (!restricted_) {
+        full32_h_ = on32_h_;
+        full64_h_ = on64_h_;
+        restricted_ = true;
+    }
+    if (sub.size() != full32_h_.size()) throw std::invalid_argument("restrict_solves: one flag per LP");
+    std::vector<char> a(sub.size()), b(sub.size());
+    for (size_t k = 0; k < sub.size(); ++k) {
+        a[k] = full32_h_[k] && sub[k];
+        b[k] = full64_h_[k] && sub[k];
+    }
+    upload_mask(on32_, on32_h_, a);
+    upload_mask(on64_, on64_h_, b);
+}
+
+void KktEngine::unrestrict_solves() {
+    if (!restricted_) return;
+    restricted_ = false;
+    const std::vector<char> a(full32_h_.begin(), full32_h_.end()), b(full64_h_.begin(), full64_h_.end());
+    upload_mask(on32_, on32_h_, a);
+    upload_mask(on64_, on64_h_, b);
 }
 
 int KktEngine::failed_lp() const {
@@ -1871,6 +1897,33 @@ double KktEngine::assembly_bytes(size_t elem) const {
     const double w = static_cast<double>(p.w_ptr.empty() ? 0 : p.w_ptr.back());
     const double offd = static_cast<double>(p.nslots) - M;
     return 12.0 * w + 8.0 * (p.nslots + 1.0) + 8.0 * N + diag_out + (16.0 + elem) * offd + elem * M;
+}
+
+namespace {
+// L's diagonal entries of every front (one block per front, a thread per own column).
+__global__ void k_pivots(const int* __restrict__ sn_first, const int* __restrict__ sn_ncols,
+                         const int* __restrict__ sn_lda, const int64_t* __restrict__ F_off,
+                         const double* __restrict__ F, double* __restrict__ out) {
+    const int s = blockIdx.x;
+    const int K = sn_ncols[s], LD = sn_lda[s], f = sn_first[s];
+    for (int c = threadIdx.x; c < K; c += blockDim.x) out[f + c] = F[F_off[s] + c + static_cast<int64_t>(c) * LD];
+}
+}  // namespace
+
+std::vector<double> KktEngine::pivots_host() {
+    if (fp32_ || !F64_.ptr) throw std::logic_error("pivots_host: no FP64 factor");
+    std::vector<double> out(static_cast<size_t>(plan_.M));
+    Arena tmp;
+    Slot<double> d;
+    reserve(tmp, d, static_cast<size_t>(std::max<int64_t>(1, plan_.M)));
+    tmp.commit();
+    bind(tmp, d);
+    if (plan_.ns > 0)
+        k_pivots<<<plan_.ns, 128, 0, st_>>>(sn_first_.ptr, sn_ncols_.ptr, sn_lda_.ptr, sn_F_off_.ptr, F64_.ptr, d.ptr);
+    SK_CUDA(cudaGetLastError());
+    SK_CUDA(cudaMemcpyAsync(out.data(), d.ptr, sizeof(double) * out.size(), cudaMemcpyDeviceToHost, st_));
+    SK_CUDA(cudaStreamSynchronize(st_));
+    return out;
 }
 
 std::vector<double> KktEngine::fronts_host() {

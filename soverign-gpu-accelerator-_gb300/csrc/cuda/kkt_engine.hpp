@@ -55,6 +55,11 @@ public:
     void set_masks(const std::vector<char>& on32, const std::vector<char>& on64);
     // LP of the front whose pivot failed in the last factor() (-1 if none).
     int failed_lp() const;
+    // Restricts apply_inverse to the LPs flagged in `sub` (within the masks in force),
+    // e.g. the LPs whose conjugate-gradient iteration has not converged yet; rows of
+    // the other LPs then come out 0. unrestrict_solves() brings back the masks.
+    void restrict_solves(const std::vector<char>& sub);
+    void unrestrict_solves();
 
     // Diagnostics: one factorisation + one solve (of d_rhs) without graphs, with
     // CUDA events around every launch; fills out[17] as sk_solver_profile documents.
@@ -68,6 +73,9 @@ public:
     double* diag_D() const { return D_.ptr; }
     // Copies the factored fronts to the host (FP64) for inspection.
     std::vector<double> fronts_host();
+    // Diagonal of the last FP64 factor L (D (A Theta A^T) D + delta I = L L^T) in
+    // elimination order (position k holds the pivot of batch row plan().perm[k]).
+    std::vector<double> pivots_host();
     cudaStream_t stream() const { return st_; }
     // Non-zero when a triangular-solve task gave up waiting for a dependency
     // (synchronises). The solve result is then invalid.
@@ -108,6 +116,8 @@ private:
     Slot<int> sn_lp_, on32_, on64_, q_lp_;    // LP of each front; per-precision LP masks; LP of each permuted row
     std::vector<int> on32_h_, on64_h_, sn_lp_h_;
     bool mixed_ = false;                        // set_masks in force (else one precision for all)
+    bool restricted_ = false;                   // restrict_solves in force: full masks saved below
+    std::vector<int> full32_h_, full64_h_;
     Slot<int> zc_sn_, zc_len_;                  // front-zeroing chunks: front, length and start offset
     Slot<int64_t> zc_off_;
     int64_t nzc_ = 0;

@@ -28,6 +28,7 @@ sk_options to_c(const MehrotraOptions& o) {
     c.delta32 = o.delta32;
     c.delta64 = o.delta64;
     c.fp64_update = o.fp64_update;
+    c.dependent_rows = o.dependent_rows;
     return c;
 }
 

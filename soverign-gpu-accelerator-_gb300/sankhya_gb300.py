@@ -30,7 +30,7 @@ class Options(C.Structure):
                 ("max_iter", C.c_int), ("ordering", C.c_int), ("verbose", C.c_int),
                 ("mu_switch", C.c_double), ("ruiz_passes", C.c_int), ("strict", C.c_int),
                 ("delta32", C.c_double), ("delta64", C.c_double), ("learned_accept", C.c_double),
-                ("fp64_update", C.c_int)]
+                ("fp64_update", C.c_int), ("dependent_rows", C.c_int)]
 
 
 class Info(C.Structure):
@@ -41,7 +41,8 @@ class Info(C.Structure):
                 ("solves", C.c_int), ("refine_steps", C.c_int), ("learned_start", C.c_int),
                 ("setup_ms", C.c_double), ("solve_ms", C.c_double), ("nnz_factor", C.c_longlong),
                 ("num_supernodes", C.c_int), ("dense_front", C.c_int), ("device_ms", C.c_double),
-                ("flops_factor", C.c_double), ("start_merit", C.c_double), ("fallback_merit", C.c_double)]
+                ("flops_factor", C.c_double), ("start_merit", C.c_double), ("fallback_merit", C.c_double),
+                ("dependent_rows", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -102,6 +103,8 @@ def _declare(L):
         L.sk_kkt_get_factor.argtypes = [vp, _f64p, _f64p]
         L.sk_kkt_destroy.argtypes = [vp]
         L.sk_kkt_set_fp64_update.argtypes = [vp, C.c_int]
+        L.sk_presolve_dependent_rows.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p, _f64p, _i32p,
+                                                 C.POINTER(C.c_int), C.POINTER(C.c_double)]
         L.sk_spmv_csr.argtypes = [C.c_int, vp, vp, vp, vp, C.c_double, C.c_double, vp, vp]
         L.sk_spmv_plan_create.argtypes = [C.c_int, C.c_int, C.c_longlong, vp, vp, vp, vp, C.POINTER(vp)]
         L.sk_spmv_plan_execute.argtypes = [vp, vp, C.c_double, C.c_double, vp, vp]
@@ -201,6 +204,16 @@ def generate(family, instance=0):
     h = C.c_void_p()
     check(lib().sk_lp_generate(family, instance, C.byref(h)), "sk_lp_generate")
     return _lp_from_handle(h, "family%d/%d" % (family, instance))
+
+
+def dependent_rows(lp):
+    """Linearly dependent rows of the LP's A (sk_presolve_dependent_rows): returns
+    (keep flags (m,), number of dependent rows found, inconsistency of b)."""
+    keep = np.ones(lp.m, dtype=np.int32)
+    cnt, inc = C.c_int(0), C.c_double(0.0)
+    check(lib().sk_presolve_dependent_rows(lp.m, lp.n, lp.col_ptrs, lp.row_idx, lp.vals, lp.b, keep, C.byref(cnt),
+                                           C.byref(inc)), "sk_presolve_dependent_rows")
+    return keep, cnt.value, inc.value
 
 
 def random_lp(m, n, density, seed):

@@ -157,3 +157,29 @@ def test_presolve_and_spmv_plan_symbols_declared(sk):
     for n in ("sk_presolve_ruiz", "sk_spmv_plan_create", "sk_spmv_plan_execute", "sk_spmv_plan_info",
               "sk_spmv_plan_set_group", "sk_spmv_plan_destroy"):
         assert n in names
+
+
+def test_dependent_rows_entry_checks_arguments_and_needs_a_device(sk):
+    assert "sk_presolve_dependent_rows" in declared_symbols()
+    lp = sk.random_lp(30, 60, 0.1, 5)
+    keep = np.ones(lp.m, dtype=np.int32)
+    cnt, inc = ctypes.c_int(0), ctypes.c_double(0.0)
+    L = sk.lib()
+    # bad column pointers: SK_ERR_INVALID (1) before any device work
+    bad_cp = lp.col_ptrs.copy()
+    bad_cp[0] = 1
+    assert L.sk_presolve_dependent_rows(lp.m, lp.n, bad_cp, lp.row_idx, lp.vals, lp.b, keep, ctypes.byref(cnt),
+                                        ctypes.byref(inc)) == 1
+    assert L.sk_presolve_dependent_rows(lp.m, lp.n, lp.col_ptrs, lp.row_idx, lp.vals, lp.b, keep, None, None) == 1
+    rc = L.sk_presolve_dependent_rows(lp.m, lp.n, lp.col_ptrs, lp.row_idx, lp.vals, lp.b, keep, ctypes.byref(cnt),
+                                      ctypes.byref(inc))
+    if _cuda_visible():
+        assert rc == 0 and cnt.value == 0
+    else:
+        assert rc == 4            # SK_ERR_NO_DEVICE: no CPU fallback
+
+
+def test_dependent_rows_option_is_validated(sk):
+    lp = sk.random_lp(30, 60, 0.1, 5)
+    with pytest.raises(RuntimeError, match="dependent_rows"):
+        sk.solve(lp, dependent_rows=2)
