@@ -1075,7 +1075,10 @@ void DeviceIPM::run() {
             k_theta<<<nblk(N), 256, 0, st>>>(N, I.x.ptr, I.s.ptr, I.col_lp.ptr, d_mask, I.theta.ptr);
             if (!factor_all(0, false))
                 throw api::sk_exception(SK_ERR_NUMERICAL, "learned start: A Theta A^T could not be factored");
-            for (int k = 0; k < nlp; ++k) tol[k] = 1e-8;
+            // the projection only has to move the point towards feasibility (the distance
+            // test below decides whether it is used), so its solves stop at 1e-6: with the
+            // network's Theta an FP32-preconditioned solve to 1e-8 took tens of CG steps
+            for (int k = 0; k < nlp; ++k) tol[k] = 1e-6;
             std::vector<char> ok;
             residuals(I.x.ptr, I.y.ptr, I.s.ptr, I.rp.ptr, I.rd.ptr);
             solve(I.rp.ptr, I.dy.ptr, ok);

@@ -89,8 +89,20 @@ __global__ void __launch_bounds__(256) k_asm_diag_sparse(int M, const int64_t* _
     const int i = static_cast<int>(gid / G), lane = static_cast<int>(gid % G);
     const bool valid = i < M;
     double acc = 0.0;
-    if (valid)
-        for (int64_t t = w_ptr[i] + lane; t < w_ptr[i + 1]; t += G) acc += w_val[t] * theta[w_col[t]];
+    if (valid) {
+        int64_t t = w_ptr[i] + lane;
+        const int64_t t1 = w_ptr[i + 1];
+        for (; t + 3 * G < t1; t += 4 * G) {   // four entries' loads in flight; same summation order
+            const int c0 = w_col[t], c1 = w_col[t + G], c2 = w_col[t + 2 * G], c3 = w_col[t + 3 * G];
+            const double v0 = w_val[t], v1 = w_val[t + G], v2 = w_val[t + 2 * G], v3 = w_val[t + 3 * G];
+            const double h0 = theta[c0], h1 = theta[c1], h2 = theta[c2], h3 = theta[c3];
+            acc += v0 * h0;
+            acc += v1 * h1;
+            acc += v2 * h2;
+            acc += v3 * h3;
+        }
+        for (; t < t1; t += G) acc += w_val[t] * theta[w_col[t]];
+    }
 #pragma unroll
     for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, G);
     if (valid && lane == 0) {
@@ -110,16 +122,20 @@ __global__ void k_asm_slots_sparse(int64_t nslots, int M, const int64_t* __restr
                                    const int* __restrict__ lp_on, T* __restrict__ F) {
     const int64_t s = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (s >= nslots) return;
-    if (!lp_on[q_lp[s < M ? static_cast<int>(s) : si[s]]]) return;
-    double v;
-    if (s < M) {
-        v = Mdiag[s] * D[s] * D[s] + params[0];
-    } else {
-        double acc = 0.0;
-        for (int64_t t = w_ptr[s]; t < w_ptr[s + 1]; ++t) acc += w_val[t] * theta[w_col[t]];
-        v = acc * D[si[s]] * D[sj[s]];
-    }
-    F[pos[s]] = static_cast<T>(v);
+    // every load that depends only on s first, then the ones they index, so a slot
+    // waits for three rounds of loads rather than one per link of the chain
+    const bool diag = s < M;
+    const int i = diag ? static_cast<int>(s) : si[s];
+    const int j = diag ? static_cast<int>(s) : sj[s];
+    const int64_t p = pos[s];
+    const int64_t t0 = diag ? 0 : w_ptr[s], t1 = diag ? 0 : w_ptr[s + 1];
+    const double di = D[i], dj = D[j];
+    const int on = lp_on[q_lp[i]];
+    double acc = 0.0;
+    for (int64_t t = t0; t < t1; ++t) acc += w_val[t] * theta[w_col[t]];
+    if (!on) return;
+    const double v = diag ? Mdiag[s] * di * di + params[0] : acc * di * dj;
+    F[p] = static_cast<T>(v);
 }
 
 template <int G>
@@ -168,7 +184,11 @@ struct DiagDense {
 
 // One warp per column j of M (dense mode: one front per LP, natural order).
 // Column j below the diagonal is sum_k a_jk theta_k A(:,k); the k loop is
-// sequential so every entry is summed in a fixed order.
+// sequential so every entry is summed in a fixed order. The column ranges and
+// coefficients of 32 k at a time are loaded by the lanes together and broadcast,
+// and the rows, values and D of the next k are loaded before the current k's
+// read-modify-write, so the loop carries one dependent memory round trip per k
+// (the update of the front column) instead of four.
 template <class T>
 __global__ void k_asm_cols_dense(int M, const int* __restrict__ rp, const int* __restrict__ ci,
                                  const double* __restrict__ av, const int* __restrict__ tp,
@@ -183,17 +203,49 @@ __global__ void k_asm_cols_dense(int M, const int* __restrict__ rp, const int* _
     const int s = row_lp[j];
     if (!pd.lp_on[s]) return;            // dense mode: front s is LP s
     const int first = pd.sn_first[s];
-    const int N = pd.sn_nrows[s];
     T* col = F + pd.F_off[s] + static_cast<int64_t>(j - first) * pd.sn_lda[s] - first;
     const double dj = D[j];
-    for (int q = rp[j]; q < rp[j + 1]; ++q) {
-        const int k = ci[q];
-        const double coef = av[q] * theta[k] * dj;
-        for (int t = tp[k] + lane; t < tp[k + 1]; t += 32) {
-            const int i = ti[t];
-            if (i > j) col[i] = static_cast<T>(static_cast<double>(col[i]) + coef * tv[t] * D[i]);
+    const int q0 = rp[j], q1 = rp[j + 1];
+    for (int qb = q0; qb < q1; qb += 32) {
+        int ts = 0, te = 0;
+        double cf = 0.0;
+        if (qb + lane < q1) {
+            const int k = ci[qb + lane];
+            ts = tp[k];
+            te = tp[k + 1];
+            cf = av[qb + lane] * theta[k] * dj;
         }
-        __syncwarp();
+        const int nq = min(32, q1 - qb);
+        // first chunk (32 rows) of k = qb: loaded ahead
+        int s0 = __shfl_sync(0xffffffffu, ts, 0), e0 = __shfl_sync(0xffffffffu, te, 0);
+        int i0 = -1;
+        double v0 = 0.0, d0 = 0.0;
+        if (s0 + lane < e0) {
+            i0 = ti[s0 + lane];
+            v0 = tv[s0 + lane];
+            d0 = D[i0];
+        }
+        for (int u = 0; u < nq; ++u) {              // nq is the same for every lane
+            const double coef = __shfl_sync(0xffffffffu, cf, u);
+            const int s1 = s0, e1 = e0, i1 = i0;
+            const double v1 = v0, d1 = d0;
+            if (u + 1 < nq) {                        // next k's first chunk
+                s0 = __shfl_sync(0xffffffffu, ts, u + 1);
+                e0 = __shfl_sync(0xffffffffu, te, u + 1);
+                i0 = -1;
+                if (s0 + lane < e0) {
+                    i0 = ti[s0 + lane];
+                    v0 = tv[s0 + lane];
+                    d0 = D[i0];
+                }
+            }
+            if (i1 > j) col[i1] = static_cast<T>(static_cast<double>(col[i1]) + coef * v1 * d1);
+            for (int t = s1 + 32 + lane; t < e1; t += 32) {   // columns longer than 32 rows
+                const int i = ti[t];
+                if (i > j) col[i] = static_cast<T>(static_cast<double>(col[i]) + coef * tv[t] * D[i]);
+            }
+            __syncwarp();
+        }
     }
     if (lane == 0) col[j] = static_cast<T>(Mdiag[j] * dj * dj + params[0]);
 }
@@ -483,29 +535,12 @@ __global__ void __launch_bounds__(256) k_update(StepArgs a, const int* __restric
     }
 }
 
-// ---- tensor-core trailing update of FP32 fronts (tcgen05, TF32 x3) ---------
-// One block of 256 threads updates a 128x128 block of the trailing lower triangle
-// (four 64x64 tiles): C -= A_i A_j^T with A_i, A_j the 128 x w panel rows, as
-// D = A_lo B_hi^T + A_hi B_lo^T + A_hi B_hi^T on the 5th-generation tensor cores.
-// Each FP32 operand x is split into TF32 parts hi = tf32(x), lo = tf32(x - hi),
-// so the three products recover close to FP32 accuracy. Operands are staged in
-// shared memory in the canonical K-major no-swizzle layout (8-row x 16-byte core
-// matrices; K-adjacent core matrices 128 B apart, 8-row groups 2048 B apart); the
-// MMA shape is M=128, N=128, K=8, accumulating in 128 TMEM columns. One elected
-// thread issues the 24 MMAs and commits them to an mbarrier while every thread
-// loads its C values; all eight warps then read D (warp w: TMEM lanes of quarter
-// w % 4, columns 64 (w / 4) ..) and write C. Every wait is bounded: on a time-out
-// the block records err[2], frees its TMEM and leaves C untouched.
-
-constexpr int kTcRows = 128;                         // operand rows per block (two 64-row tiles)
+// ---- shared helpers of the tensor-core kernels (tcgen05) --------------------
+// Shared-memory descriptors of the canonical K-major no-swizzle layout: 8-row x
+// 16-byte core matrices, K-adjacent core matrices 128 B apart, 8-row groups 2048 B
+// apart (64 four-byte elements per row).
 constexpr uint32_t kTcLbo = 128;                     // bytes between K-adjacent core matrices
 constexpr uint32_t kTcSbo = 2048;                    // bytes between 8-row groups (64 fp32 per row)
-constexpr size_t kTcOp = kTcRows * T64 * 4;          // one operand part: 32 KB
-constexpr size_t kTcSmem = 4 * kTcOp + 64;           // + mbarrier and TMEM address
-constexpr int kTcSpin = 1 << 22;
-// instruction descriptor: D = F32 (bits 4-5 = 1), A = B = TF32 (bits 7-9, 10-12 = 2), both
-// K-major, N >> 3 at bits 17-22, M >> 4 at bits 24-28
-constexpr uint32_t kTcIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((128u >> 3) << 17) | ((128u >> 4) << 24);
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -517,156 +552,10 @@ __device__ __forceinline__ uint64_t tc_sdesc(uint32_t saddr) {
     d |= static_cast<uint64_t>(1) << 46;             // descriptor version bits 46-48 = 0b001
     return d;                                        // base offset 0, no swizzle
 }
-__device__ __forceinline__ uint32_t tc_off(int r, int k) {   // byte offset of (row r, col k)
-    return static_cast<uint32_t>((r >> 3) * kTcSbo + (k >> 2) * kTcLbo + (r & 7) * 16 + (k & 3) * 4);
-}
 __device__ __forceinline__ uint32_t to_tf32(float x) {
     uint32_t r;
     asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
     return r;
-}
-
-__global__ void __launch_bounds__(256, 1) k_update_tc(StepArgs a, const int* __restrict__ items,
-                                                      const int* __restrict__ prefix, PlanDev pd, float* F,
-                                                      float* __restrict__ Linv,
-                                                      const int64_t* __restrict__ inv_off, int* err) {
-    extern __shared__ __align__(1024) unsigned char smraw[];
-    unsigned char* Ahi = smraw;
-    unsigned char* Alo = Ahi + kTcOp;
-    unsigned char* Bhi = Alo + kTcOp;
-    unsigned char* Blo = Bhi + kTcOp;
-    uint64_t* bar = reinterpret_cast<uint64_t*>(Blo + kTcOp);
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(Blo + kTcOp + 16);
-    int* fail = reinterpret_cast<int*>(Blo + kTcOp + 32);
-    const int i = find_item(prefix + a.up2_off, a.nitems, blockIdx.x);
-    const int s = items[a.item_off + i];
-    if (!pd.lp_on[pd.sn_lp[s]]) return;
-    const int lb = blockIdx.x - prefix[a.up2_off + i];
-    int bi, bj;
-    tri_index(lb, bi, bj);
-    const int N = pd.sn_nrows[s], K = pd.sn_ncols[s];
-    const int LD = pd.sn_lda[s];
-    const int k0 = a.k * T64;
-    const int w = min(T64, K - k0);
-    const int t0 = k0 + w;
-    const int r0 = t0 + bi * kTcRows, c0 = t0 + bj * kTcRows;
-    const int nra = min(kTcRows, N - r0), ncb = min(kTcRows, N - c0);
-    float* Fs = F + pd.F_off[s];
-    const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
-    if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_addr(bar)));
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        *fail = 0;
-    }
-    if (wid == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;" :: "r"(smem_addr(tslot)));
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
-    }
-    // operands: rows r0.. (A) and c0.. (B), columns k0..k0+w of the panel, in TF32 parts
-#pragma unroll 4
-    for (int it = 0; it < 32; ++it) {
-        const int idx = tid + it * 256;
-        const int r = idx & (kTcRows - 1), kk = idx >> 7;
-        const int64_t cofs = static_cast<int64_t>(k0 + kk) * LD;
-        const float av = (kk < w && r < nra) ? Fs[r0 + r + cofs] : 0.f;
-        const float bv = (kk < w && r < ncb) ? Fs[c0 + r + cofs] : 0.f;
-        const uint32_t ah = to_tf32(av), bh = to_tf32(bv);
-        const uint32_t o = tc_off(r, kk);
-        *reinterpret_cast<uint32_t*>(Ahi + o) = ah;
-        *reinterpret_cast<uint32_t*>(Alo + o) = to_tf32(av - __uint_as_float(ah));
-        *reinterpret_cast<uint32_t*>(Bhi + o) = bh;
-        *reinterpret_cast<uint32_t*>(Blo + o) = to_tf32(bv - __uint_as_float(bh));
-    }
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    const uint32_t tmem = *tslot;
-    if (tid == 0) {
-        const uint32_t ahi = smem_addr(Ahi), alo = smem_addr(Alo), bhi = smem_addr(Bhi), blo = smem_addr(Blo);
-        const int nk = (w + 7) / 8;
-        uint32_t acc = 0;
-        for (int ks = 0; ks < nk; ++ks) {
-            const uint32_t ko = static_cast<uint32_t>(ks) * 2 * kTcLbo;
-            const uint64_t da[3] = {tc_sdesc(alo + ko), tc_sdesc(ahi + ko), tc_sdesc(ahi + ko)};
-            const uint64_t db[3] = {tc_sdesc(bhi + ko), tc_sdesc(blo + ko), tc_sdesc(bhi + ko)};
-#pragma unroll
-            for (int q = 0; q < 3; ++q) {
-                asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-                             " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n"
-                             :: "r"(tmem), "l"(da[q]), "l"(db[q]), "r"(kTcIdesc), "r"(acc));
-                acc = 1;
-            }
-        }
-        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
-                     :: "r"(smem_addr(bar)) : "memory");
-    }
-    // this thread's row of D (TMEM lane) and 64 columns, and its C values, loaded while the MMAs run
-    const int row = 32 * (wid & 3) + lane, ch = 64 * (wid >> 2);
-    const bool rok = row < nra;
-    float cv[64];
-#pragma unroll
-    for (int j = 0; j < 64; ++j) {
-        const int col = ch + j;
-        const bool in = rok && col < ncb && (bi != bj || row >= col);
-        cv[j] = in ? Fs[(r0 + row) + static_cast<int64_t>(c0 + col) * LD] : 0.f;
-    }
-    if (tid == 0) {
-        uint32_t done = 0;
-        for (int spin = 0; spin < kTcSpin && !done; ++spin) {
-            asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n"
-                         " selp.u32 %0, 1, 0, p;\n}\n" : "=r"(done) : "r"(smem_addr(bar)) : "memory");
-            if (!done) __nanosleep(20);
-        }
-        if (!done) {
-            *fail = 1;
-            atomicExch(err + 2, 1);
-            // Before the TMEM columns are freed below, give MMAs still in flight a
-            // second bounded wait: a CTA must free its TMEM before it exits, and
-            // freeing columns an MMA still writes could hand them to another CTA
-            // mid-write. The host turns err[2] into an error either way.
-            for (int spin = 0; spin < kTcSpin && !done; ++spin) {
-                asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n"
-                             " selp.u32 %0, 1, 0, p;\n}\n" : "=r"(done) : "r"(smem_addr(bar)) : "memory");
-                if (!done) __nanosleep(20);
-            }
-        }
-    }
-    __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    const bool ok = *fail == 0;
-    if (ok) {
-#pragma unroll
-        for (int c16 = 0; c16 < 4; ++c16) {
-            uint32_t v[16];
-            const uint32_t taddr = tmem + (static_cast<uint32_t>(32 * (wid & 3)) << 16) +
-                                   static_cast<uint32_t>(ch + 16 * c16);
-            asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-                         : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
-                           "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
-                           "=r"(v[14]), "=r"(v[15])
-                         : "r"(taddr));
-            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-            for (int q = 0; q < 16; ++q) {
-                const int j = 16 * c16 + q, col = ch + j;
-                if (rok && col < ncb && (bi != bj || row >= col))
-                    Fs[(r0 + row) + static_cast<int64_t>(c0 + col) * LD] = cv[j] - __uint_as_float(v[q]);
-            }
-        }
-    }
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
-    if (wid == 0) {
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;" :: "r"(tmem));
-    }
-    if (!ok) return;
-    // the block holding the first trailing diagonal tile factors it (as in k_update)
-    if (lb == 0 && t0 < K) {
-        __syncthreads();
-        potrf_tile<float>(s, a.k + 1, pd, F, Linv, inv_off, err, smraw);
-    }
 }
 
 // ---- emulated FP64 trailing update on the tensor cores (BF16 digits) --------
@@ -730,6 +619,16 @@ __device__ __forceinline__ bool oz_wait(uint32_t bar) {
 
 // Digits of the step's trailing panel rows: one block per 64-row tile (the trsm
 // tiles), four threads per row with 16 columns each.
+// Row block bi of block lb in a list where row block bi holds 2 bi + 2 blocks
+// (bi (bi + 1) <= lb < (bi + 1)(bi + 2)); FP32 estimate corrected in integers (the
+// FP64 pipe is kept for the epilogues).
+__device__ __forceinline__ int block_row_of(int lb) {
+    int bi = static_cast<int>((sqrtf(4.0f * static_cast<float>(lb) + 1.0f) - 1.0f) * 0.5f);
+    while ((bi + 1) * (bi + 2) <= lb) ++bi;
+    while (bi > 0 && bi * (bi + 1) > lb) --bi;
+    return bi;
+}
+
 __global__ void __launch_bounds__(256) k_oz_digits(StepArgs a, const int* __restrict__ items,
                                                    const int* __restrict__ prefix, PlanDev pd,
                                                    const double* __restrict__ F, unsigned char* __restrict__ dig,
@@ -816,9 +715,7 @@ __global__ void __launch_bounds__(256, 1) k_update_oz(StepArgs a, const int* __r
     const int s = items[a.item_off + i];
     if (!pd.lp_on[pd.sn_lp[s]]) return;
     const int lb = blockIdx.x - prefix[a.up3_off + i];
-    int bi = static_cast<int>((sqrt(4.0 * lb + 1.0) - 1.0) * 0.5);
-    while ((bi + 1) * (bi + 2) <= lb) ++bi;
-    while (bi * (bi + 1) > lb) --bi;
+    int bi = block_row_of(lb);
     const int bj = lb - bi * (bi + 1);
     const int N = pd.sn_nrows[s], K = pd.sn_ncols[s], LD = pd.sn_lda[s];
     const int k0 = a.k * T64;
@@ -949,6 +846,196 @@ __global__ void __launch_bounds__(256, 1) k_update_oz(StepArgs a, const int* __r
     }
 }
 
+// ---- FP32 trailing update on the tensor cores from pre-split panels -----------
+// The step's trailing panel rows (64 FP32 entries each) are split once per step
+// into TF32 parts hi = tf32(x), lo = tf32(x - hi) (k_tc_split, one block per 64-row
+// trsm tile) and written to the digit buffer in the canonical K-major no-swizzle
+// layout of 8-row x 16-byte core matrices (K-adjacent core matrices 128 B apart,
+// 8-row groups 2048 B apart): a block's 128 (A) or 64 (B) consecutive rows are one
+// contiguous 32 KB / 16 KB bulk copy per part. k_update_tcs then computes C(128 x 64)
+// -= A B^T as lo_A hi_B + hi_A lo_B + hi_A hi_B (TF32 x3, close to FP32 accuracy):
+// one thread copies the four parts with cp.async.bulk and issues the 24 MMAs (M=128,
+// N=64, K=8) into 64 TMEM columns while every thread loads its 32 C values; 96 KB of
+// shared memory and at most 128 registers per thread leave room for two blocks per
+// SM. Blocks follow the 128-row x 64-column lower-part list of the emulated FP64
+// update (row block bi holds column blocks 0..2bi+1). Every wait is bounded: on a
+// time-out the block records err[2], waits once more for what it issued, frees its
+// TMEM and leaves C untouched.
+constexpr uint32_t kTsLbo = 128;                       // bytes between K-adjacent core matrices
+constexpr uint32_t kTsSbo = 2048;                      // bytes between 8-row groups (64 FP32 per row)
+constexpr size_t kTsA = 128 * 256;                     // 128 rows x 64 FP32: 32 KB per part
+constexpr size_t kTsB = 64 * 256;                      // 64 rows: 16 KB per part
+constexpr size_t kTsSmem = 2 * (kTsA + kTsB) + 64;
+// instruction descriptor: D = F32 (bits 4-5 = 1), A = B = TF32 (bits 7-9, 10-12 = 2), both
+// K-major, N >> 3 at bits 17-22 (N = 64), M >> 4 at bits 24-28 (M = 128)
+constexpr uint32_t kTsIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
+
+__global__ void __launch_bounds__(256) k_tc_split(StepArgs a, const int* __restrict__ items,
+                                                  const int* __restrict__ prefix, PlanDev pd,
+                                                  const float* __restrict__ F, unsigned char* __restrict__ dig,
+                                                  int64_t plane) {
+    const int i = find_item(prefix + a.tp_off, a.nitems, blockIdx.x);
+    const int s = items[a.item_off + i];
+    if (!pd.lp_on[pd.sn_lp[s]]) return;
+    const int lt = blockIdx.x - prefix[a.tp_off + i];
+    const int N = pd.sn_nrows[s], K = pd.sn_ncols[s], LD = pd.sn_lda[s];
+    const int k0 = a.k * T64;
+    const int w = min(T64, K - k0);
+    const int t0 = k0 + w;
+    const int r = threadIdx.x & 63, cg = threadIdx.x >> 6;
+    const int row = t0 + lt * T64 + r;
+    const bool rin = row < N;
+    const float* Fs = F + pd.F_off[s];
+    const int q = prefix[a.dr_off + i] + lt * T64 + r;
+    unsigned char* base = dig + static_cast<int64_t>(q >> 3) * kTsSbo + (q & 7) * 16;
+#pragma unroll
+    for (int h = 0; h < 4; ++h) {                      // one core matrix (4 columns) per pass
+        uint32_t hi[4], lo[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int k = cg * 16 + h * 4 + u;
+            const float v = (rin && k < w) ? Fs[row + static_cast<int64_t>(k0 + k) * LD] : 0.f;
+            hi[u] = to_tf32(v);
+            lo[u] = to_tf32(v - __uint_as_float(hi[u]));
+        }
+        const int kc = cg * 4 + h;
+        *reinterpret_cast<uint4*>(base + kc * kTsLbo) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+        *reinterpret_cast<uint4*>(base + plane + kc * kTsLbo) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+    }
+}
+
+__global__ void __launch_bounds__(256, 2) k_update_tcs(StepArgs a, const int* __restrict__ items,
+                                                       const int* __restrict__ prefix, PlanDev pd, float* F,
+                                                       float* __restrict__ Linv, const int64_t* __restrict__ inv_off,
+                                                       const unsigned char* __restrict__ dig, int64_t plane,
+                                                       int* err) {
+    extern __shared__ __align__(1024) unsigned char smraw[];
+    unsigned char* Ah = smraw;
+    unsigned char* Al = Ah + kTsA;
+    unsigned char* Bh = Al + kTsA;
+    unsigned char* Bl = Bh + kTsB;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(Bl + kTsB);   // [0] parts loaded, [1] MMAs done
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 2);
+    int* fail = reinterpret_cast<int*>(bar + 3);
+    const int i = find_item(prefix + a.up3_off, a.nitems, blockIdx.x);
+    const int s = items[a.item_off + i];
+    if (!pd.lp_on[pd.sn_lp[s]]) return;
+    const int lb = blockIdx.x - prefix[a.up3_off + i];
+    int bi = block_row_of(lb);
+    const int bj = lb - bi * (bi + 1);
+    const int N = pd.sn_nrows[s], K = pd.sn_ncols[s], LD = pd.sn_lda[s];
+    const int k0 = a.k * T64;
+    const int w = min(T64, K - k0);
+    const int t0 = k0 + w;
+    const int r0 = t0 + bi * 128, c0 = t0 + bj * T64;
+    if (c0 >= N) return;                              // the whole block: column block past the front
+    const int nra = min(128, N - r0), ncb = min(T64, N - c0);
+    const int qa = prefix[a.dr_off + i] + bi * 128, qb = prefix[a.dr_off + i] + bj * T64;
+    float* Fs = F + pd.F_off[s];
+    const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_addr(bar)));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_addr(bar + 1)));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        *fail = 0;
+    }
+    if (wid == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 64;" :: "r"(smem_addr(tslot)));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tslot;
+    if (tid == 0) {
+        const uint32_t b0 = smem_addr(bar);
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                     :: "r"(b0), "r"(static_cast<uint32_t>(2 * (kTsA + kTsB))) : "memory");
+        const unsigned char* ga = dig + static_cast<int64_t>(qa >> 3) * kTsSbo;
+        const unsigned char* gb = dig + static_cast<int64_t>(qb >> 3) * kTsSbo;
+        const unsigned char* src[4] = {ga, ga + plane, gb, gb + plane};
+        unsigned char* dst[4] = {Ah, Al, Bh, Bl};
+        const uint32_t len[4] = {static_cast<uint32_t>(kTsA), static_cast<uint32_t>(kTsA),
+                                 static_cast<uint32_t>(kTsB), static_cast<uint32_t>(kTsB)};
+        for (int c = 0; c < 4; ++c)
+            asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                         :: "r"(smem_addr(dst[c])), "l"(src[c]), "r"(len[c]), "r"(b0) : "memory");
+        bool ok = oz_wait(b0);
+        if (ok) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t ah = smem_addr(Ah), al = smem_addr(Al), bh = smem_addr(Bh), bl = smem_addr(Bl);
+            uint32_t acc = 0;
+            for (int ks = 0; ks < T64 / 8; ++ks) {
+                const uint32_t ko = static_cast<uint32_t>(ks) * 2 * kTsLbo;
+                const uint64_t da[3] = {tc_sdesc(al + ko), tc_sdesc(ah + ko), tc_sdesc(ah + ko)};
+                const uint64_t db[3] = {tc_sdesc(bh + ko), tc_sdesc(bl + ko), tc_sdesc(bh + ko)};
+#pragma unroll
+                for (int q = 0; q < 3; ++q) {
+                    asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                                 " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n"
+                                 :: "r"(tmem), "l"(da[q]), "l"(db[q]), "r"(kTsIdesc), "r"(acc));
+                    acc = 1;
+                }
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                         :: "r"(smem_addr(bar + 1)) : "memory");
+            ok = oz_wait(smem_addr(bar + 1));
+            if (!ok) oz_wait(smem_addr(bar + 1));     // a second bounded wait before TMEM is freed
+        } else {
+            oz_wait(b0);                               // copies still in flight: a second bounded wait
+        }
+        if (!ok) {
+            *fail = 1;
+            atomicExch(err + 2, 1);
+        }
+    }
+    // this thread's row (TMEM lane) and 32 columns, and its C values, loaded while the MMAs run
+    const int row = 32 * (wid & 3) + lane, ch = 32 * (wid >> 2);
+    const bool rok = row < nra;
+    float cv[32];
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+        const int col = ch + j;
+        const bool in = rok && col < ncb && r0 + row >= c0 + col;
+        cv[j] = in ? Fs[(r0 + row) + static_cast<int64_t>(c0 + col) * LD] : 0.f;
+    }
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const bool ok = *fail == 0;
+    if (ok) {
+#pragma unroll
+        for (int c16 = 0; c16 < 2; ++c16) {
+            uint32_t v[16];
+            const uint32_t taddr = tmem + (static_cast<uint32_t>(32 * (wid & 3)) << 16) +
+                                   static_cast<uint32_t>(ch + 16 * c16);
+            asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                         : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+                           "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+                           "=r"(v[14]), "=r"(v[15])
+                         : "r"(taddr));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+                const int j = 16 * c16 + q, col = ch + j;
+                if (rok && col < ncb && r0 + row >= c0 + col)
+                    Fs[(r0 + row) + static_cast<int64_t>(c0 + col) * LD] = cv[j] - __uint_as_float(v[q]);
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (wid == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" :: "r"(tmem));
+    }
+    if (!ok) return;
+    // the block holding the first trailing diagonal tile factors it (as in k_update)
+    if (lb == 0 && t0 < K) {
+        __syncthreads();
+        potrf_tile<float>(s, a.k + 1, pd, F, Linv, inv_off, err, smraw);
+    }
+}
+
 template <class T>
 __global__ void k_extend_add(int item_off, int nitems, int prefix_off, const int* __restrict__ items,
                              const int* __restrict__ prefix, PlanDev pd, T* F) {
@@ -1048,7 +1135,9 @@ __device__ __forceinline__ bool wait_flag(const int* flag, int target, int* err,
             *abort_sh = 1;
             return false;
         }
-        __nanosleep(40);
+        // poll back to back first (the flag of the last dependency usually comes within
+        // microseconds: this wait is on the solve's critical path), then back off
+        if (spins > 512) __nanosleep(64);
     }
     __threadfence();
     return true;
@@ -1184,7 +1273,7 @@ __global__ void __launch_bounds__(256, 1) k_fwd_tasks(const int2* __restrict__ t
 // blocks are taken oldest first (nb - 1 downwards), ready ones together, and the
 // L values of the first block of each pass are loaded before its wait.
 template <class T>
-__global__ void __launch_bounds__(256, 1) k_bwd_tasks(const int2* __restrict__ tasks, int ntasks, int* counter,
+__global__ void __launch_bounds__(256, 2) k_bwd_tasks(const int2* __restrict__ tasks, int ntasks, int* counter,
                                                    PlanDev pd, const T* __restrict__ F, const T* __restrict__ Linv,
                                                    const int64_t* __restrict__ inv_off,
                                                    const int* __restrict__ blk_off, int* flags, T* xp,
@@ -1366,8 +1455,8 @@ struct KktEngine::Prof {
 template <class T>
 static void set_smem_attrs() {
     if (std::is_same<T, float>::value)
-        SK_CUDA(cudaFuncSetAttribute(k_update_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     static_cast<int>(kTcSmem)));
+        SK_CUDA(cudaFuncSetAttribute(k_update_tcs, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     static_cast<int>(kTsSmem)));
     SK_CUDA(cudaFuncSetAttribute(k_potrf<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  static_cast<int>(potrf_smem(sizeof(T)))));
     SK_CUDA(cudaFuncSetAttribute(k_trsm<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1595,8 +1684,12 @@ void KktEngine::launch_factor(T* F, T* Linv, Prof* prof) {
                     if constexpr (std::is_same<T, float>::value) {
                         if (tensor_) {
                             tc = true;
-                            k_update_tc<<<static_cast<int>(st.upd2_blocks), 256, kTcSmem, st_>>>(
-                                a, step_items_.ptr, step_prefix_.ptr, pdv, F, Linv, inv_off_.ptr, err_.ptr);
+                            const int64_t plane = plan_.max_digit_rows * 256;
+                            k_tc_split<<<static_cast<int>(st.trsm_tiles), 256, 0, st_>>>(
+                                a, step_items_.ptr, step_prefix_.ptr, pdv, F, dig_.ptr, plane);
+                            k_update_tcs<<<static_cast<int>(st.upd3_blocks), 256, kTsSmem, st_>>>(
+                                a, step_items_.ptr, step_prefix_.ptr, pdv, F, Linv, inv_off_.ptr, dig_.ptr, plane,
+                                err_.ptr);
                         }
                     } else {
                         if (emulate64_) {
@@ -1710,7 +1803,7 @@ void KktEngine::ensure_digits() {
 bool KktEngine::factor(const double* d_theta, double delta, bool fp32) {
     const int q = fp32 ? (tensor_ ? 2 : 1) : (emulate64_ ? 3 : 0);
     ensure_fronts(fp32);
-    if (!fp32 && emulate64_) ensure_digits();
+    if ((!fp32 && emulate64_) || (fp32 && tensor_)) ensure_digits();
     fp32_ = fp32;
     double hp[4] = {delta, 0, 0, 0};
     SK_CUDA(cudaMemcpyAsync(params_.ptr, hp, sizeof(hp), cudaMemcpyHostToDevice, st_));

@@ -21,6 +21,28 @@
 namespace sankhya {
 namespace dev {
 
+// acc + sum over q = q0, q0 + G, ... < q1 of v[q] xs[ci[q] - off], in that order (so
+// the sum is the same as a plain loop's), with four entries' index, value and
+// gather loads in flight at a time.
+template <int G>
+__device__ __forceinline__ double spmv_row_part(int q0, int q1, const int* __restrict__ ci,
+                                                const double* __restrict__ v, const double* __restrict__ xs,
+                                                int off) {
+    double acc = 0.0;
+    int q = q0;
+    for (; q + 3 * G < q1; q += 4 * G) {
+        const int c0 = ci[q], c1 = ci[q + G], c2 = ci[q + 2 * G], c3 = ci[q + 3 * G];
+        const double v0 = v[q], v1 = v[q + G], v2 = v[q + 2 * G], v3 = v[q + 3 * G];
+        const double x0 = xs[c0 - off], x1 = xs[c1 - off], x2 = xs[c2 - off], x3 = xs[c3 - off];
+        acc += v0 * x0;
+        acc += v1 * x1;
+        acc += v2 * x2;
+        acc += v3 * x3;
+    }
+    for (; q < q1; q += G) acc += v[q] * xs[ci[q] - off];
+    return acc;
+}
+
 template <int G, class Epi>
 __global__ void __launch_bounds__(256) k_spmv(int rows, const int* __restrict__ rp, const int* __restrict__ ci,
                                               const double* __restrict__ v, const double* __restrict__ x, Epi epi) {
@@ -28,8 +50,7 @@ __global__ void __launch_bounds__(256) k_spmv(int rows, const int* __restrict__ 
     const int row = gid / G, lane = gid % G;
     const bool valid = row < rows;
     double acc = 0.0;
-    if (valid)
-        for (int q = rp[row] + lane; q < rp[row + 1]; q += G) acc += v[q] * x[ci[q]];
+    if (valid) acc = spmv_row_part<G>(rp[row] + lane, rp[row + 1], ci, v, x, 0);
 #pragma unroll
     for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, G);
     if (valid && lane == 0) epi(row, acc);
@@ -80,10 +101,8 @@ __global__ void __launch_bounds__(kWinThreads) k_spmv_win(const int4* __restrict
         double acc = 0.0;
         if (valid) {
             const int q1 = rp[row + 1];
-            if (staged)
-                for (int q = rp[row] + lane; q < q1; q += G) acc += v[q] * xs[ci[q] - ch.z];
-            else
-                for (int q = rp[row] + lane; q < q1; q += G) acc += v[q] * x[ci[q]];
+            if (staged) acc = spmv_row_part<G>(rp[row] + lane, q1, ci, v, xs, ch.z);
+            else acc = spmv_row_part<G>(rp[row] + lane, q1, ci, v, x, 0);
         }
 #pragma unroll
         for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, G);

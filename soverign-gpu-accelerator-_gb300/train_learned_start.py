@@ -138,9 +138,10 @@ def main():
            "heldout_instances": [HELDOUT_BASE, HELDOUT_BASE + args.heldout], "batch": args.batch,
            "epochs": args.epochs, "lr": args.lr, "capture_mu": args.capture_mu, "seed": args.seed,
            "target_solve_s": t_solve, "train_s": t_train, "loss_history": hist, "heldout": summary,
-           "per_lp": rows}
+           "per_lp_columns": list(rows[0].keys()),
+           "per_lp": [[round(v, 6) if isinstance(v, float) else v for v in r.values()] for r in rows]}
     with open(os.path.splitext(args.out)[0] + ".json", "w") as f:
-        json.dump(rep, f, indent=1)
+        json.dump(rep, f, separators=(",", ":"))
 
 
 if __name__ == "__main__":
