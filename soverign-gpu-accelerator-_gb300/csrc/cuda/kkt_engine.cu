@@ -571,8 +571,10 @@ __device__ __forceinline__ uint32_t to_tf32(float x) {
 // 9 * 2^20 in magnitude (|d_0 e_0| <= 2^16, |d_0 e_j| <= 2^15, |d_i e_j| <= 2^14,
 // at most L + 1 pairs of 64 products), so the tensor cores add it exactly. Levels
 // 0..6 (28 pairs; the pairs beyond level 6 weigh below 2^-56 and are left out)
-// are combined in 64-bit integers, hi = levels 0..2 and lo = levels 3..6, and
-// applied with two FP64 FMAs per entry: C - hi 2^(Ea+Eb-30) - lo 2^(Ea+Eb-62).
+// are combined in 64-bit integers, hi = levels 0..2 and lo = levels 3..6, folded
+// into u = hi 2^22 + round(lo 2^-10) (below 2^62 in magnitude) and applied with
+// one conversion and one FP64 FMA per entry: C - u 2^(Ea+Eb-52) (GB300's FP64 pipe
+// is the scarce resource of this epilogue).
 // This is the error-free splitting of Ozaki, Ogita, Oishi and Rump (2012) with
 // BF16 digits, exact FP32 tensor-core sums and an integer epilogue; the result
 // agrees with an FP64 product to about 2^-53 of sum_k |a_k| |b_k|.
@@ -615,6 +617,40 @@ __device__ __forceinline__ bool oz_wait(uint32_t bar) {
         if (!done) __nanosleep(20);
     }
     return done != 0;
+}
+
+// The 7 balanced base-256 digits of 16 entries v of row q (columns 16 cg .. 16 cg + 15)
+// with row exponent E, as BF16 into the digit planes (layout above).
+__device__ __forceinline__ void oz_store_digits(const double* v, int E, int q, int cg, unsigned char* dig,
+                                                int64_t plane) {
+    const double mul = oz_pow2(55 - E);             // |v mul| < 2^56
+    uint32_t pk[kOzDigits][8];                      // 16 BF16 digits per plane, packed in pairs
+#pragma unroll
+    for (int t = 0; t < 16; t += 2) {
+        int d0[kOzDigits], d1[kOzDigits];
+        long long f0 = llrint(v[t] * mul), f1 = llrint(v[t + 1] * mul);
+#pragma unroll
+        for (int j = kOzDigits - 1; j >= 1; --j) {
+            int l0 = static_cast<int>(f0 & 255), l1 = static_cast<int>(f1 & 255);
+            f0 >>= 8;
+            f1 >>= 8;
+            if (l0 >= 128) { l0 -= 256; f0 += 1; }
+            if (l1 >= 128) { l1 -= 256; f1 += 1; }
+            d0[j] = l0;
+            d1[j] = l1;
+        }
+        d0[0] = static_cast<int>(f0);
+        d1[0] = static_cast<int>(f1);
+#pragma unroll
+        for (int j = 0; j < kOzDigits; ++j) pk[j][t >> 1] = oz_bf16(d0[j]) | (oz_bf16(d1[j]) << 16);
+    }
+    unsigned char* base = dig + static_cast<int64_t>(q >> 3) * 1024 + (q & 7) * 16;
+#pragma unroll
+    for (int j = 0; j < kOzDigits; ++j)
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+            *reinterpret_cast<uint4*>(base + j * plane + (cg * 2 + h) * 128) =
+                make_uint4(pk[j][4 * h], pk[j][4 * h + 1], pk[j][4 * h + 2], pk[j][4 * h + 3]);
 }
 
 // Digits of the step's trailing panel rows: one block per 64-row tile (the trsm
@@ -660,35 +696,8 @@ __global__ void __launch_bounds__(256) k_oz_digits(StepArgs a, const int* __rest
     // E is held at -968 or above so that 2^(55 - E) stays a normal double (rows whose
     // largest entry is below 2^-967 keep fewer digits; they do not matter next to 1)
     const int E = mx > 0.0 ? max(ilogb(mx), -968) : 0;
-    const double mul = oz_pow2(55 - E);             // |v mul| < 2^56
-    uint32_t pk[kOzDigits][8];                      // 16 BF16 digits per plane, packed in pairs
-#pragma unroll
-    for (int t = 0; t < 16; t += 2) {
-        int d0[kOzDigits], d1[kOzDigits];
-        long long f0 = llrint(v[t] * mul), f1 = llrint(v[t + 1] * mul);
-#pragma unroll
-        for (int j = kOzDigits - 1; j >= 1; --j) {
-            int l0 = static_cast<int>(f0 & 255), l1 = static_cast<int>(f1 & 255);
-            f0 >>= 8;
-            f1 >>= 8;
-            if (l0 >= 128) { l0 -= 256; f0 += 1; }
-            if (l1 >= 128) { l1 -= 256; f1 += 1; }
-            d0[j] = l0;
-            d1[j] = l1;
-        }
-        d0[0] = static_cast<int>(f0);
-        d1[0] = static_cast<int>(f1);
-#pragma unroll
-        for (int j = 0; j < kOzDigits; ++j) pk[j][t >> 1] = oz_bf16(d0[j]) | (oz_bf16(d1[j]) << 16);
-    }
     const int q = prefix[a.dr_off + i] + lt * T64 + r;
-    unsigned char* base = dig + static_cast<int64_t>(q >> 3) * 1024 + (q & 7) * 16;
-#pragma unroll
-    for (int j = 0; j < kOzDigits; ++j)
-#pragma unroll
-        for (int h = 0; h < 2; ++h)
-            *reinterpret_cast<uint4*>(base + j * plane + (cg * 2 + h) * 128) =
-                make_uint4(pk[j][4 * h], pk[j][4 * h + 1], pk[j][4 * h + 2], pk[j][4 * h + 3]);
+    oz_store_digits(v, E, q, cg, dig, plane);
     if (cg == 0) dexp[q] = E;
 }
 
@@ -823,12 +832,14 @@ __global__ void __launch_bounds__(256, 1) k_update_oz(StepArgs a, const int* __r
                 long long lv[kOzDigits];
 #pragma unroll
                 for (int L = 0; L < kOzDigits; ++L) lv[L] = __float2int_rn(__uint_as_float(v[L][q]));
-                const long long hi = lv[0] * 65536LL + lv[1] * 256LL + lv[2];
-                const long long lo = lv[3] * 16777216LL + lv[4] * 65536LL + lv[5] * 256LL + lv[6];
+                const long long hi = lv[0] * 65536LL + lv[1] * 256LL + lv[2];   // |hi| < 2^39.2
+                const long long lo = lv[3] * 16777216LL + lv[4] * 65536LL + lv[5] * 256LL + lv[6];  // < 2^47.2
+                // hi 2^(E-30) + lo 2^(E-62) = 2^(E-52) (hi 2^22 + lo 2^-10): one integer below 2^62
+                // (lo rounded to 2^(E-53)), one conversion and one FP64 FMA on the slow FP64 pipe
+                const long long u = hi * 4194304LL + ((lo + 512) >> 10);
                 const int eb = dexp[qb + col];
-                const double shi = oz_pow2(ea + eb - 30), slo = oz_pow2(ea + eb - 62);
                 Fs[(r0 + row) + static_cast<int64_t>(c0 + col) * LD] =
-                    fma(-static_cast<double>(hi), shi, fma(-static_cast<double>(lo), slo, cv[j]));
+                    fma(-static_cast<double>(u), oz_pow2(ea + eb - 52), cv[j]);
             }
         }
     }
@@ -843,6 +854,169 @@ __global__ void __launch_bounds__(256, 1) k_update_oz(StepArgs a, const int* __r
     if (lb == 0 && t0 < K) {
         __syncthreads();
         potrf_tile<double>(s, a.k + 1, pd, F, Linv, inv_off, err, smraw);
+    }
+}
+
+// ---- FP64 panel solve on the tensor cores (the same digit products) ----------
+// X = B Linv^T for the step's panel rows below the diagonal tile (B = their current
+// values, Linv = the inverse of the factored diagonal tile): k_oz_digits writes the
+// digits of B before the solve, k_oz_linv_digits those of the 64 rows of Linv of
+// every item of the step (one block per item, rows i * 64 .. in a buffer of its own),
+// and k_trsm_oz forms X = u 2^(Ea+Eb-52) per 128-row block with the MMAs of
+// k_update_oz (N = 64 = the Linv rows) and no C operand.
+__global__ void __launch_bounds__(256) k_oz_linv_digits(StepArgs a, const int* __restrict__ items, PlanDev pd,
+                                                        const double* __restrict__ Linv,
+                                                        const int64_t* __restrict__ inv_off,
+                                                        unsigned char* __restrict__ dig, int* __restrict__ dexp,
+                                                        int64_t plane) {
+    __shared__ double smax[4][64];
+    const int i = blockIdx.x;
+    const int s = items[a.item_off + i];
+    if (!pd.lp_on[pd.sn_lp[s]]) return;
+    const double* Li = Linv + inv_off[s] + static_cast<int64_t>(a.k) * T64 * T64;   // column-major 64 x 64
+    const int r = threadIdx.x & 63, cg = threadIdx.x >> 6;
+    double v[16];
+    double mx = 0.0;
+#pragma unroll
+    for (int t = 0; t < 16; ++t) {
+        v[t] = Li[r + (cg * 16 + t) * T64];
+        mx = fmax(mx, fabs(v[t]));
+    }
+    smax[cg][r] = mx;
+    __syncthreads();
+    mx = fmax(fmax(smax[0][r], smax[1][r]), fmax(smax[2][r], smax[3][r]));
+    const int E = mx > 0.0 ? max(ilogb(mx), -968) : 0;
+    const int q = i * T64 + r;
+    oz_store_digits(v, E, q, cg, dig, plane);
+    if (cg == 0) dexp[q] = E;
+}
+
+__global__ void __launch_bounds__(256, 1) k_trsm_oz(StepArgs a, const int* __restrict__ items,
+                                                    const int* __restrict__ prefix, PlanDev pd, double* F,
+                                                    const unsigned char* __restrict__ dig,
+                                                    const int* __restrict__ dexp, int64_t plane,
+                                                    const unsigned char* __restrict__ ldig,
+                                                    const int* __restrict__ lexp, int64_t lplane, int* err) {
+    extern __shared__ __align__(1024) unsigned char smraw[];
+    unsigned char* As = smraw;
+    unsigned char* Bs = smraw + kOzDigits * kOzA;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(Bs + kOzDigits * kOzB);   // [0] planes loaded, [1] MMAs done
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 2);
+    int* fail = reinterpret_cast<int*>(bar + 3);
+    const int i = find_item(prefix + a.dr_off, a.nitems, blockIdx.x * 128);
+    const int s = items[a.item_off + i];
+    if (!pd.lp_on[pd.sn_lp[s]]) return;
+    const int blk = blockIdx.x - prefix[a.dr_off + i] / 128;
+    const int N = pd.sn_nrows[s], K = pd.sn_ncols[s], LD = pd.sn_lda[s];
+    const int k0 = a.k * T64;
+    const int w = min(T64, K - k0);
+    const int r0 = k0 + w + blk * 128;
+    if (r0 >= N) return;                              // a padded block of the digit rows
+    const int nra = min(128, N - r0);
+    const int qa = prefix[a.dr_off + i] + blk * 128, qb = i * T64;
+    double* Fs = F + pd.F_off[s];
+    const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_addr(bar)));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_addr(bar + 1)));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        *fail = 0;
+    }
+    if (wid == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" :: "r"(smem_addr(tslot)));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tslot;
+    if (tid == 0) {
+        const uint32_t b0 = smem_addr(bar);
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                     :: "r"(b0), "r"(static_cast<uint32_t>(kOzDigits * (kOzA + kOzB))) : "memory");
+        for (int j = 0; j < kOzDigits; ++j) {
+            const unsigned char* ga = dig + j * plane + static_cast<int64_t>(qa >> 3) * 1024;
+            const unsigned char* gb = ldig + j * lplane + static_cast<int64_t>(qb >> 3) * 1024;
+            asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                         :: "r"(smem_addr(As + j * kOzA)), "l"(ga), "r"(static_cast<uint32_t>(kOzA)), "r"(b0)
+                         : "memory");
+            asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                         :: "r"(smem_addr(Bs + j * kOzB)), "l"(gb), "r"(static_cast<uint32_t>(kOzB)), "r"(b0)
+                         : "memory");
+        }
+        bool ok = oz_wait(b0);
+        if (ok) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t sa = smem_addr(As), sb = smem_addr(Bs);
+            for (int L = 0; L < kOzDigits; ++L) {
+                uint32_t acc = 0;
+                for (int da = 0; da <= L; ++da) {
+                    const int db = L - da;
+                    for (int ks = 0; ks < T64 / 16; ++ks) {
+                        const uint64_t adesc = oz_sdesc(sa + da * static_cast<uint32_t>(kOzA) + ks * 2 * kOzLbo);
+                        const uint64_t bdesc = oz_sdesc(sb + db * static_cast<uint32_t>(kOzB) + ks * 2 * kOzLbo);
+                        asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                                     " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+                                     :: "r"(tmem + static_cast<uint32_t>(64 * L)), "l"(adesc), "l"(bdesc),
+                                        "r"(kOzIdesc), "r"(acc));
+                        acc = 1;
+                    }
+                }
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                         :: "r"(smem_addr(bar + 1)) : "memory");
+            ok = oz_wait(smem_addr(bar + 1));
+            if (!ok) oz_wait(smem_addr(bar + 1));     // a second bounded wait before TMEM is freed
+        } else {
+            oz_wait(b0);                               // copies still in flight: a second bounded wait
+        }
+        if (!ok) {
+            *fail = 1;
+            atomicExch(err + 2, 1);
+        }
+    }
+    const int row = 32 * (wid & 3) + lane, ch = 32 * (wid >> 2);
+    const bool rok = row < nra;
+    const int ea = rok ? dexp[qa + row] : 0;
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const bool ok = *fail == 0;
+    if (ok) {
+#pragma unroll
+        for (int c16 = 0; c16 < 2; ++c16) {
+            uint32_t v[kOzDigits][16];
+#pragma unroll
+            for (int L = 0; L < kOzDigits; ++L) {
+                const uint32_t taddr = tmem + (static_cast<uint32_t>(32 * (wid & 3)) << 16) +
+                                       static_cast<uint32_t>(64 * L + ch + 16 * c16);
+                asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                             : "=r"(v[L][0]), "=r"(v[L][1]), "=r"(v[L][2]), "=r"(v[L][3]), "=r"(v[L][4]),
+                               "=r"(v[L][5]), "=r"(v[L][6]), "=r"(v[L][7]), "=r"(v[L][8]), "=r"(v[L][9]),
+                               "=r"(v[L][10]), "=r"(v[L][11]), "=r"(v[L][12]), "=r"(v[L][13]), "=r"(v[L][14]),
+                               "=r"(v[L][15])
+                             : "r"(taddr));
+            }
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+                const int col = ch + 16 * c16 + q;
+                if (!(rok && col < w)) continue;
+                long long lv[kOzDigits];
+#pragma unroll
+                for (int L = 0; L < kOzDigits; ++L) lv[L] = __float2int_rn(__uint_as_float(v[L][q]));
+                const long long hi = lv[0] * 65536LL + lv[1] * 256LL + lv[2];
+                const long long lo = lv[3] * 16777216LL + lv[4] * 65536LL + lv[5] * 256LL + lv[6];
+                const long long u = hi * 4194304LL + ((lo + 512) >> 10);
+                Fs[(r0 + row) + static_cast<int64_t>(k0 + col) * LD] =
+                    static_cast<double>(u) * oz_pow2(ea + lexp[qb + col] - 52);
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (wid == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" :: "r"(tmem));
     }
 }
 
@@ -1466,6 +1640,9 @@ static void set_smem_attrs() {
     if (std::is_same<T, double>::value)
         SK_CUDA(cudaFuncSetAttribute(k_update_oz, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      static_cast<int>(kOzSmem)));
+    if (std::is_same<T, double>::value)
+        SK_CUDA(cudaFuncSetAttribute(k_trsm_oz, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     static_cast<int>(kOzSmem)));
 }
 
 KktEngine::KktEngine(const ipm::FrontPlan& plan, const DeviceLP& lp, cudaStream_t stream)
@@ -1675,8 +1852,23 @@ void KktEngine::launch_factor(T* F, T* Linv, Prof* prof) {
                 });
             if (st.trsm_tiles > 0)
                 run(2, [&] {
-                    k_trsm<T><<<static_cast<int>(st.trsm_tiles), 256, 2 * T64 * T64 * sizeof(T), st_>>>(
-                        a, step_items_.ptr, step_prefix_.ptr, pdv, F, Linv, inv_off_.ptr);
+                    bool oz = false;
+                    if constexpr (std::is_same<T, double>::value) {
+                        if (emulate64_) {   // FP64-accurate panel solve on the tensor cores
+                            oz = true;
+                            const int64_t plane = plan_.max_digit_rows * 128, lplane = max_step_items_ * T64 * 128;
+                            k_oz_digits<<<static_cast<int>(st.trsm_tiles), 256, 0, st_>>>(
+                                a, step_items_.ptr, step_prefix_.ptr, pdv, F, dig_.ptr, dexp_.ptr, plane);
+                            k_oz_linv_digits<<<st.nitems, 256, 0, st_>>>(a, step_items_.ptr, pdv, Linv, inv_off_.ptr,
+                                                                         ldig_.ptr, lexp_.ptr, lplane);
+                            k_trsm_oz<<<static_cast<int>(st.digit_rows / 128), 256, kOzSmem, st_>>>(
+                                a, step_items_.ptr, step_prefix_.ptr, pdv, F, dig_.ptr, dexp_.ptr, plane, ldig_.ptr,
+                                lexp_.ptr, lplane, err_.ptr);
+                        }
+                    }
+                    if (!oz)
+                        k_trsm<T><<<static_cast<int>(st.trsm_tiles), 256, 2 * T64 * T64 * sizeof(T), st_>>>(
+                            a, step_items_.ptr, step_prefix_.ptr, pdv, F, Linv, inv_off_.ptr);
                 });
             if (st.upd_tiles > 0) {
                 run(3, [&] {
@@ -1792,12 +1984,18 @@ void KktEngine::ensure_fronts(bool fp32) {
 
 void KktEngine::ensure_digits() {
     if (dig_.ptr || plan_.max_digit_rows <= 0) return;
+    max_step_items_ = 1;
+    for (const auto& st : plan_.steps) max_step_items_ = std::max(max_step_items_, static_cast<int64_t>(st.nitems));
     dig_arena_.reset();
     reserve(dig_arena_, dig_, static_cast<size_t>(kOzDigits) * static_cast<size_t>(plan_.max_digit_rows) * 128);
     reserve(dig_arena_, dexp_, static_cast<size_t>(plan_.max_digit_rows));
+    reserve(dig_arena_, ldig_, static_cast<size_t>(kOzDigits) * static_cast<size_t>(max_step_items_) * T64 * 128);
+    reserve(dig_arena_, lexp_, static_cast<size_t>(max_step_items_) * T64);
     dig_arena_.commit();
     bind(dig_arena_, dig_);
     bind(dig_arena_, dexp_);
+    bind(dig_arena_, ldig_);
+    bind(dig_arena_, lexp_);
 }
 
 bool KktEngine::factor(const double* d_theta, double delta, bool fp32) {

@@ -134,8 +134,9 @@ private:
     bool tensor_ = true;
     bool emulate64_ = false;
     Arena dig_arena_;                           // digit planes and row exponents of the emulated FP64 update
-    Slot<unsigned char> dig_;
-    Slot<int> dexp_;
+    Slot<unsigned char> dig_, ldig_;            // panel-row digits; digits of each item's Linv rows
+    Slot<int> dexp_, lexp_;
+    int64_t max_step_items_ = 1;
     // FP64, FP32 SIMT update, FP32 tensor-core update, FP64 emulated on the tensor cores
     cudaGraphExec_t gfac_[4] = {nullptr, nullptr, nullptr, nullptr};
     cudaGraphExec_t gsol_[2] = {nullptr, nullptr};
