@@ -250,82 +250,6 @@ __global__ void k_asm_cols_dense(int M, const int* __restrict__ rp, const int* _
     if (lane == 0) col[j] = static_cast<T>(Mdiag[j] * dj * dj + params[0]);
 }
 
-// The same column sums with each warp's column accumulated in shared memory (a
-// buffer of nbuf entries of the front's type per warp, rows below the diagonal):
-// the read-modify-write of every k then stays on the SM, and the finished column
-// goes to the front in one coalesced pass (which also writes its zeros). Every
-// entry is rounded to T after each addition in the same k order as above, so the
-// fronts are bit-identical.
-constexpr int kAsmSmemMax = 160 * 1024;          // shared memory for the column buffers of one block
-
-template <class T>
-__global__ void __launch_bounds__(256) k_asm_cols_dense_sm(int M, const int* __restrict__ rp, const int* __restrict__ ci,
-                                                           const double* __restrict__ av, const int* __restrict__ tp,
-                                                           const int* __restrict__ ti, const double* __restrict__ tv,
-                                                           const double* __restrict__ theta,
-                                                           const double* __restrict__ Mdiag,
-                                                           const double* __restrict__ D,
-                                                           const int* __restrict__ row_lp, PlanDev pd,
-                                                           const double* __restrict__ params, T* __restrict__ F,
-                                                           int nbuf) {
-    extern __shared__ __align__(16) unsigned char smraw[];
-    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int j = blockIdx.x * (blockDim.x >> 5) + wib;
-    if (j >= M) return;                  // only warp-level synchronisation below
-    const int s = row_lp[j];
-    if (!pd.lp_on[s]) return;            // dense mode: front s is LP s
-    T* buf = reinterpret_cast<T*>(smraw) + static_cast<size_t>(wib) * nbuf;   // buf[i - j - 1]: row i > j
-    const int first = pd.sn_first[s], N = pd.sn_nrows[s];
-    const int jl = j - first, nb = N - jl - 1;
-    for (int r = lane; r < nb; r += 32) buf[r] = T(0);
-    __syncwarp();
-    const double dj = D[j];
-    const int q0 = rp[j], q1 = rp[j + 1];
-    for (int qb = q0; qb < q1; qb += 32) {
-        int ts = 0, te = 0;
-        double cf = 0.0;
-        if (qb + lane < q1) {
-            const int k = ci[qb + lane];
-            ts = tp[k];
-            te = tp[k + 1];
-            cf = av[qb + lane] * theta[k] * dj;
-        }
-        const int nq = min(32, q1 - qb);
-        int s0 = __shfl_sync(0xffffffffu, ts, 0), e0 = __shfl_sync(0xffffffffu, te, 0);
-        int i0 = -1;
-        double v0 = 0.0, d0 = 0.0;
-        if (s0 + lane < e0) {
-            i0 = ti[s0 + lane];
-            v0 = tv[s0 + lane];
-            d0 = D[i0];
-        }
-        for (int u = 0; u < nq; ++u) {              // nq is the same for every lane
-            const double coef = __shfl_sync(0xffffffffu, cf, u);
-            const int s1 = s0, e1 = e0, i1 = i0;
-            const double v1 = v0, d1 = d0;
-            if (u + 1 < nq) {                        // next k's first chunk
-                s0 = __shfl_sync(0xffffffffu, ts, u + 1);
-                e0 = __shfl_sync(0xffffffffu, te, u + 1);
-                i0 = -1;
-                if (s0 + lane < e0) {
-                    i0 = ti[s0 + lane];
-                    v0 = tv[s0 + lane];
-                    d0 = D[i0];
-                }
-            }
-            if (i1 > j) buf[i1 - j - 1] = static_cast<T>(static_cast<double>(buf[i1 - j - 1]) + coef * v1 * d1);
-            for (int t = s1 + 32 + lane; t < e1; t += 32) {   // columns longer than 32 rows
-                const int i = ti[t];
-                if (i > j) buf[i - j - 1] = static_cast<T>(static_cast<double>(buf[i - j - 1]) + coef * tv[t] * D[i]);
-            }
-            __syncwarp();
-        }
-    }
-    T* col = F + pd.F_off[s] + static_cast<int64_t>(jl) * pd.sn_lda[s];
-    for (int r = lane; r < nb; r += 32) col[jl + 1 + r] = buf[r];
-    if (lane == 0) col[jl] = static_cast<T>(Mdiag[j] * dj * dj + params[0]);
-}
-
 // ------------------------------------------------------------------- factor
 
 // Cholesky of the 64x64 diagonal tile of step k of one front, in the front's
@@ -690,7 +614,9 @@ __device__ __forceinline__ bool oz_wait(uint32_t bar) {
     for (int spin = 0; spin < kOzSpin && !done; ++spin) {
         asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n"
                      " selp.u32 %0, 1, 0, p;\n}\n" : "=r"(done) : "r"(bar) : "memory");
-        if (!done) __nanosleep(20);
+        // back-to-back polls first: a copy or an MMA batch of one tile completes within
+        // microseconds, and a sleep per poll adds its own latency to every tile
+        if (!done && spin >= 4096) __nanosleep(32);
     }
     return done != 0;
 }
@@ -1704,7 +1630,6 @@ struct KktEngine::Prof {
 
 template <class T>
 static void set_smem_attrs() {
-    SK_CUDA(cudaFuncSetAttribute(k_asm_cols_dense_sm<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, kAsmSmemMax));
     if (std::is_same<T, float>::value)
         SK_CUDA(cudaFuncSetAttribute(k_update_tcs, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      static_cast<int>(kTsSmem)));
@@ -1725,7 +1650,6 @@ static void set_smem_attrs() {
 KktEngine::KktEngine(const ipm::FrontPlan& plan, const DeviceLP& lp, cudaStream_t stream)
     : plan_(plan), lp_(lp), st_(stream) {
     const auto& p = plan_;
-    for (int s = 0; s < p.ns; ++s) max_front_rows_ = std::max<int64_t>(max_front_rows_, p.sn_nrows[s]);
     // tile-inverse offsets and per-level column-block prefixes of the backward pass
     std::vector<int64_t> inv_off(static_cast<size_t>(p.ns), 0);
     inv_size_ = 0;
@@ -1907,19 +1831,9 @@ void KktEngine::launch_factor(T* F, T* Linv, Prof* prof) {
         if (p.dense_mode) {
             launch_diag<DiagDense>(p.M, lp_.spmv_group_A, st_, lp_.a_rp, lp_.a_ci, lp_.a_v, theta, Mdiag_.ptr,
                                    D_.ptr);
-            // column buffers in shared memory when the widest front allows two or more per block
-            const int nbuf = static_cast<int>(std::max<int64_t>(1, max_front_rows_));
-            const int warps = static_cast<int>(std::min<int64_t>(8, kAsmSmemMax / (static_cast<int64_t>(nbuf) * sizeof(T))));
-            if (warps >= 2) {
-                k_asm_cols_dense_sm<T><<<static_cast<int>((p.M + warps - 1) / warps), 32 * warps,
-                                          static_cast<size_t>(warps) * nbuf * sizeof(T), st_>>>(
-                    p.M, lp_.a_rp, lp_.a_ci, lp_.a_v, lp_.t_rp, lp_.t_ci, lp_.t_v, theta, Mdiag_.ptr, D_.ptr,
-                    lp_.row_lp, pdv, params_.ptr, F, nbuf);
-            } else {
-                k_asm_cols_dense<T><<<blocks_for(static_cast<int64_t>(p.M) * 32, 256), 256, 0, st_>>>(
-                    p.M, lp_.a_rp, lp_.a_ci, lp_.a_v, lp_.t_rp, lp_.t_ci, lp_.t_v, theta, Mdiag_.ptr, D_.ptr,
-                    lp_.row_lp, pdv, params_.ptr, F);
-            }
+            k_asm_cols_dense<T><<<blocks_for(static_cast<int64_t>(p.M) * 32, 256), 256, 0, st_>>>(
+                p.M, lp_.a_rp, lp_.a_ci, lp_.a_v, lp_.t_rp, lp_.t_ci, lp_.t_v, theta, Mdiag_.ptr, D_.ptr, lp_.row_lp,
+                pdv, params_.ptr, F);
         } else {
             launch_diag<DiagSparse>(p.M, lp_.spmv_group_A, st_, w_ptr_.ptr, w_col_.ptr, w_val_.ptr, theta,
                                     Mdiag_.ptr, D_.ptr);

@@ -137,7 +137,6 @@ private:
     Slot<unsigned char> dig_, ldig_;            // panel-row digits; digits of each item's Linv rows
     Slot<int> dexp_, lexp_;
     int64_t max_step_items_ = 1;
-    int64_t max_front_rows_ = 0;                // rows of the widest front (dense-mode assembly buffers)
     // FP64, FP32 SIMT update, FP32 tensor-core update, FP64 emulated on the tensor cores
     cudaGraphExec_t gfac_[4] = {nullptr, nullptr, nullptr, nullptr};
     cudaGraphExec_t gsol_[2] = {nullptr, nullptr};
