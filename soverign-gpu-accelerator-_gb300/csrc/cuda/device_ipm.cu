@@ -1065,19 +1065,17 @@ void DeviceIPM::run() {
         I.gnn->forward(lp_, st, I.dx.ptr, I.ds.ptr, I.dy.ptr);
         k_learned_point<<<nblk(N), 256, 0, st>>>(N, I.dx.ptr, I.ds.ptr, I.x.ptr, I.s.ptr);
         SK_CUDA(cudaMemcpyAsync(I.y.ptr, I.dy.ptr, sizeof(double) * M, cudaMemcpyDeviceToDevice, st));
-        // Weighted projection towards Ax = b and A^T y + s = c with the predicted
-        // Theta = x / s (rp = Ax - b, rd = A^T y + s - c): x -= a_p Theta A^T w with
-        // (A Theta A^T) w = rp; y -= a_d v, s -= a_d (rd - A^T v) with (A Theta A^T) v =
-        // A Theta rd; a_p, a_d the longest steps (at most 1) that keep 10% of x and s.
+        // Projection towards Ax = b and A^T y + s = c (rp = Ax - b, rd = A^T y + s - c):
+        // x -= a_p A^T w with (A A^T) w = rp; y -= a_d v, s -= a_d (rd - A^T v) with
+        // (A A^T) v = A rd; a_p, a_d the longest steps (at most 1) that keep 10% of x and
+        // s. A A^T is the matrix of Mehrotra's start, factored just above, so the
+        // projection costs two solves and no factorisation of its own.
         {
             std::vector<double> one(nlp, 1.0);
             I.put_scalars(0, one);
-            k_theta<<<nblk(N), 256, 0, st>>>(N, I.x.ptr, I.s.ptr, I.col_lp.ptr, d_mask, I.theta.ptr);
-            if (!factor_all(0, false))
-                throw api::sk_exception(SK_ERR_NUMERICAL, "learned start: A Theta A^T could not be factored");
+            k_fill<<<nblk(N), 256, 0, st>>>(N, I.theta.ptr, 1.0);
             // the projection only has to move the point towards feasibility (the distance
-            // test below decides whether it is used), so its solves stop at 1e-6: with the
-            // network's Theta an FP32-preconditioned solve to 1e-8 took tens of CG steps
+            // test below decides whether it is used), so its solves stop at 1e-6
             for (int k = 0; k < nlp; ++k) tol[k] = 1e-6;
             std::vector<char> ok;
             residuals(I.x.ptr, I.y.ptr, I.s.ptr, I.rp.ptr, I.rd.ptr);
