@@ -56,19 +56,30 @@ struct StepArgs {
 };
 
 
+// Largest i in [0, n) with prefix[i] <= b (prefix ascending, prefix[0] = 0 <= b). The
+// whole warp searches (every lane must call it, converged, with the same arguments):
+// each round probes 32 evenly spaced entries and keeps the segment after the last
+// one <= b, so n <= 32 takes one dependent load and n <= 1024 two, where a binary
+// search takes log2(n) (this sits at the head of every tile of a factorisation step).
 __device__ __forceinline__ int find_item(const int* prefix, int n, int b) {
-    int lo = 0, hi = n - 1;   // largest i with prefix[i] <= b
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (prefix[mid] <= b) lo = mid; else hi = mid - 1;
+    const int lane = threadIdx.x & 31;
+    int lo = 0, len = n;      // the answer lies in [lo, lo + len)
+    while (len > 1) {
+        const int step = (len + 31) >> 5;
+        const int idx = lo + lane * step;
+        const bool le = idx < lo + len && prefix[idx] <= b;
+        const unsigned m = __ballot_sync(0xffffffffu, le);   // lane 0 probes lo: always set
+        const int nlo = lo + (31 - __clz(m)) * step;
+        len = min(step, lo + len - nlo);
+        lo = nlo;
     }
     return lo;
 }
 
 __device__ __forceinline__ void tri_index(int lt, int& ti, int& tj) {
-    int t = static_cast<int>((sqrt(8.0 * lt + 1.0) - 1.0) * 0.5);
+    int t = static_cast<int>((sqrtf(8.0f * static_cast<float>(lt) + 1.0f) - 1.0f) * 0.5f);
     while ((t + 1) * (t + 2) / 2 <= lt) ++t;
-    while (t * (t + 1) / 2 > lt) --t;
+    while (t > 0 && t * (t + 1) / 2 > lt) --t;
     ti = t;
     tj = lt - t * (t + 1) / 2;
 }
