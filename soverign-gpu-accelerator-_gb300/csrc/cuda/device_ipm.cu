@@ -28,7 +28,10 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <atomic>
 #include <numeric>
+#include <string>
+#include <thread>
 
 namespace sankhya {
 namespace dev {
@@ -474,9 +477,14 @@ DeviceIPM::DeviceIPM(const std::vector<ipm::LpView>& lps, const std::vector<cons
     I.M = I.row_off[I.nlp];
     I.N = I.col_off[I.nlp];
     const int M = I.M, N = I.N;
-    // --- Ruiz scaling per LP (mehrotra_device.cu:289-323) and batch CSC / CSR
-    int64_t nnz = 0;
-    for (auto& l : lps) nnz += l.col_ptrs[l.n];
+    // --- Ruiz scaling per LP (mehrotra_device.cu:289-323) and batch CSC / CSR. The LPs
+    // are independent and own disjoint ranges of every array (LP k's entries sit at
+    // [nz_off[k], nz_off[k + 1]) in the CSC and in the CSR order alike, A being block
+    // diagonal), so they are processed on worker threads with the same results.
+    std::vector<int64_t> nz_off(static_cast<size_t>(I.nlp) + 1, 0);
+    for (int k = 0; k < I.nlp; ++k) nz_off[k + 1] = nz_off[k] + lps[k].col_ptrs[lps[k].n];
+    const int64_t nnz = nz_off[I.nlp];
+    if (nnz >= (int64_t(1) << 31)) throw api::sk_exception(SK_ERR_TOO_LARGE, "batch exceeds 2^31 nonzeros");
     std::vector<int> cp(static_cast<size_t>(N) + 1, 0), ri(static_cast<size_t>(nnz));
     std::vector<double> cv(static_cast<size_t>(nnz));
     std::vector<double> hb(M), hc(N);
@@ -484,86 +492,98 @@ DeviceIPM::DeviceIPM(const std::vector<ipm::LpView>& lps, const std::vector<cons
     I.C_h.assign(N, 1.0);
     I.binf.assign(I.nlp, 0.0);
     I.cinf.assign(I.nlp, 0.0);
-    {
-        int64_t pos = 0;
-        std::vector<double> rmax, cmax;
-        for (int k = 0; k < I.nlp; ++k) {
-            const auto& l = lps[k];
-            const int ro = I.row_off[k], co = I.col_off[k];
-            const int64_t base = pos;
-            for (int j = 0; j < l.n; ++j) {
-                cp[co + j] = static_cast<int>(pos);
-                for (int q = l.col_ptrs[j]; q < l.col_ptrs[j + 1]; ++q) {
-                    if (l.row_idx[q] < 0 || l.row_idx[q] >= l.m)
-                        throw api::sk_exception(SK_ERR_INVALID, "row index out of range");
-                    ri[pos] = ro + l.row_idx[q];
-                    cv[pos] = l.vals[q];
-                    ++pos;
-                }
-            }
-            for (int i = 0; i < l.m; ++i) { hb[ro + i] = bvec[k][i]; I.binf[k] = std::max(I.binf[k], std::fabs(bvec[k][i])); }
-            for (int j = 0; j < l.n; ++j) { hc[co + j] = cvec[k][j]; I.cinf[k] = std::max(I.cinf[k], std::fabs(cvec[k][j])); }
-            for (int pass = 0; pass < opt.ruiz_passes; ++pass) {
-                rmax.assign(l.m, 0.0);
-                cmax.assign(l.n, 0.0);
-                for (int j = 0; j < l.n; ++j)
-                    for (int64_t q = cp[co + j]; q < (j + 1 < l.n ? cp[co + j + 1] : pos); ++q) {
-                        const double a = std::fabs(cv[q]);
-                        rmax[ri[q] - ro] = std::max(rmax[ri[q] - ro], a);
-                        cmax[j] = std::max(cmax[j], a);
-                    }
-                for (int i = 0; i < l.m; ++i) {
-                    const double f = rmax[i] > 1e-8 ? 1.0 / std::sqrt(rmax[i]) : 1.0;
-                    I.R_h[ro + i] *= f; hb[ro + i] *= f; rmax[i] = f;
-                }
-                for (int j = 0; j < l.n; ++j) {
-                    const double f = cmax[j] > 1e-8 ? 1.0 / std::sqrt(cmax[j]) : 1.0;
-                    I.C_h[co + j] *= f; hc[co + j] *= f; cmax[j] = f;
-                }
-                for (int j = 0; j < l.n; ++j)
-                    for (int64_t q = cp[co + j]; q < (j + 1 < l.n ? cp[co + j + 1] : pos); ++q)
-                        cv[q] *= rmax[ri[q] - ro] * cmax[j];
-            }
-            (void)base;
-        }
-        cp[N] = static_cast<int>(pos);
-    }
-    for (double v : hb) if (!std::isfinite(v)) throw api::sk_exception(SK_ERR_INVALID, "non-finite b");
-    for (double v : hc) if (!std::isfinite(v)) throw api::sk_exception(SK_ERR_INVALID, "non-finite c");
-    for (double v : cv) if (!std::isfinite(v)) throw api::sk_exception(SK_ERR_INVALID, "non-finite A");
-    // batch CSR
     core::CSRMatrix A;
     A.rows = M;
     A.cols = N;
     A.row_ptrs.assign(static_cast<size_t>(M) + 1, 0);
-    for (int64_t q = 0; q < nnz; ++q) A.row_ptrs[ri[q] + 1]++;
-    for (int i = 0; i < M; ++i) A.row_ptrs[i + 1] += A.row_ptrs[i];
     A.col_indices.resize(static_cast<size_t>(nnz));
     A.values.resize(static_cast<size_t>(nnz));
-    {
-        std::vector<int> nx(A.row_ptrs.begin(), A.row_ptrs.end() - 1);
-        for (int j = 0; j < N; ++j)
-            for (int q = cp[j]; q < cp[j + 1]; ++q) {
-                const int d = nx[ri[q]]++;
-                A.col_indices[d] = j;
-                A.values[d] = cv[q];
-            }
-    }
-    // --- symbolic plan on the scaled batch
     std::vector<ipm::LpView> sl(I.nlp);
     std::vector<std::vector<int>> lcp(I.nlp), lri(I.nlp);
-    for (int k = 0; k < I.nlp; ++k) {
-        const int co = I.col_off[k], ro = I.row_off[k];
-        lcp[k].resize(lps[k].n + 1);
-        for (int j = 0; j <= lps[k].n; ++j) lcp[k][j] = cp[co + j] - cp[co];
+    std::vector<std::string> bad(I.nlp);
+    auto one_lp = [&](int k) {
+        const auto& l = lps[k];
+        const int ro = I.row_off[k], co = I.col_off[k];
+        int64_t pos = nz_off[k];
+        for (int j = 0; j < l.n; ++j) {
+            cp[co + j] = static_cast<int>(pos);
+            for (int q = l.col_ptrs[j]; q < l.col_ptrs[j + 1]; ++q) {
+                if (l.row_idx[q] < 0 || l.row_idx[q] >= l.m) { bad[k] = "row index out of range"; return; }
+                ri[pos] = ro + l.row_idx[q];
+                cv[pos] = l.vals[q];
+                ++pos;
+            }
+        }
+        const int64_t end = pos;
+        for (int i = 0; i < l.m; ++i) { hb[ro + i] = bvec[k][i]; I.binf[k] = std::max(I.binf[k], std::fabs(bvec[k][i])); }
+        for (int j = 0; j < l.n; ++j) { hc[co + j] = cvec[k][j]; I.cinf[k] = std::max(I.cinf[k], std::fabs(cvec[k][j])); }
+        std::vector<double> rmax, cmax;
+        for (int pass = 0; pass < opt.ruiz_passes; ++pass) {
+            rmax.assign(l.m, 0.0);
+            cmax.assign(l.n, 0.0);
+            for (int j = 0; j < l.n; ++j)
+                for (int64_t q = cp[co + j]; q < (j + 1 < l.n ? cp[co + j + 1] : end); ++q) {
+                    const double a = std::fabs(cv[q]);
+                    rmax[ri[q] - ro] = std::max(rmax[ri[q] - ro], a);
+                    cmax[j] = std::max(cmax[j], a);
+                }
+            for (int i = 0; i < l.m; ++i) {
+                const double f = rmax[i] > 1e-8 ? 1.0 / std::sqrt(rmax[i]) : 1.0;
+                I.R_h[ro + i] *= f; hb[ro + i] *= f; rmax[i] = f;
+            }
+            for (int j = 0; j < l.n; ++j) {
+                const double f = cmax[j] > 1e-8 ? 1.0 / std::sqrt(cmax[j]) : 1.0;
+                I.C_h[co + j] *= f; hc[co + j] *= f; cmax[j] = f;
+            }
+            for (int j = 0; j < l.n; ++j)
+                for (int64_t q = cp[co + j]; q < (j + 1 < l.n ? cp[co + j + 1] : end); ++q)
+                    cv[q] *= rmax[ri[q] - ro] * cmax[j];
+        }
+        for (int i = 0; i < l.m; ++i) if (!std::isfinite(hb[ro + i])) { bad[k] = "non-finite b"; return; }
+        for (int j = 0; j < l.n; ++j) if (!std::isfinite(hc[co + j])) { bad[k] = "non-finite c"; return; }
+        for (int64_t q = nz_off[k]; q < end; ++q) if (!std::isfinite(cv[q])) { bad[k] = "non-finite A"; return; }
+        // this LP's rows of the batch CSR (its entries keep their range)
+        std::vector<int> cnt(static_cast<size_t>(l.m) + 1, 0);
+        for (int64_t q = nz_off[k]; q < end; ++q) cnt[ri[q] - ro + 1]++;
+        for (int i = 0; i < l.m; ++i) cnt[i + 1] += cnt[i];
+        for (int i = 0; i < l.m; ++i) A.row_ptrs[ro + i + 1] = static_cast<int>(nz_off[k] + cnt[i + 1]);
+        std::vector<int64_t> nx(static_cast<size_t>(l.m));
+        for (int i = 0; i < l.m; ++i) nx[i] = nz_off[k] + cnt[i];
+        for (int j = 0; j < l.n; ++j)
+            for (int q = cp[co + j]; q < (j + 1 < l.n ? cp[co + j + 1] : static_cast<int>(end)); ++q) {
+                const int64_t d = nx[ri[q] - ro]++;
+                A.col_indices[d] = co + j;
+                A.values[d] = cv[q];
+            }
+        // this LP's scaled view (local indices) for the symbolic plan
+        lcp[k].resize(l.n + 1);
+        for (int j = 0; j < l.n; ++j) lcp[k][j] = static_cast<int>(cp[co + j] - nz_off[k]);
+        lcp[k][l.n] = static_cast<int>(end - nz_off[k]);
         lri[k].resize(lcp[k].back());
-        for (int q = 0; q < lcp[k].back(); ++q) lri[k][q] = ri[cp[co] + q] - ro;
-        sl[k].m = lps[k].m;
-        sl[k].n = lps[k].n;
+        for (int64_t q = nz_off[k]; q < end; ++q) lri[k][q - nz_off[k]] = ri[q] - ro;
+        sl[k].m = l.m;
+        sl[k].n = l.n;
         sl[k].col_ptrs = lcp[k].data();
         sl[k].row_idx = lri[k].data();
-        sl[k].vals = cv.data() + cp[co];
+        sl[k].vals = cv.data() + nz_off[k];
+    };
+    {
+        const int nt = static_cast<int>(std::max(1u, std::min(16u, std::thread::hardware_concurrency())));
+        std::atomic<int> next{0};
+        auto work = [&]() {
+            for (int k = next++; k < I.nlp; k = next++) one_lp(k);
+        };
+        if (nt <= 1 || I.nlp <= 1 || nnz < 100000) {
+            work();
+        } else {
+            std::vector<std::thread> pool;
+            for (int t = 0; t < std::min(nt, I.nlp); ++t) pool.emplace_back(work);
+            for (auto& th : pool) th.join();
+        }
     }
+    for (int k = 0; k < I.nlp; ++k)
+        if (!bad[k].empty()) throw api::sk_exception(SK_ERR_INVALID, bad[k]);
+    cp[N] = static_cast<int>(nnz);
     ipm::FrontPlan plan;
     ipm::build_front_plan(sl, A, opt.ordering, plan);
     lcp.clear();
