@@ -749,21 +749,13 @@ __global__ void __launch_bounds__(256, 1) k_update_oz(StepArgs a, const int* __r
     const int qa = prefix[a.dr_off + i] + bi * 128, qb = prefix[a.dr_off + i] + bj * T64;
     double* Fs = F + pd.F_off[s];
     const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
+    // thread 0 starts the copies first; TMEM allocation and every thread's C loads
+    // then overlap them
     if (tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_addr(bar)));
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_addr(bar + 1)));
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         *fail = 0;
-    }
-    if (wid == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" :: "r"(smem_addr(tslot)));
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
-    }
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    const uint32_t tmem = *tslot;
-    if (tid == 0) {
         const uint32_t b0 = smem_addr(bar);
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
                      :: "r"(b0), "r"(static_cast<uint32_t>(kOzDigits * (kOzA + kOzB))) : "memory");
@@ -777,6 +769,28 @@ __global__ void __launch_bounds__(256, 1) k_update_oz(StepArgs a, const int* __r
                          :: "r"(smem_addr(Bs + j * kOzB)), "l"(gb), "r"(static_cast<uint32_t>(kOzB)), "r"(b0)
                          : "memory");
         }
+    }
+    if (wid == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" :: "r"(smem_addr(tslot)));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    // this thread's row (TMEM lane) and 32 columns, and its C values
+    const int row = 32 * (wid & 3) + lane, ch = 32 * (wid >> 2);
+    const bool rok = row < nra;
+    double cv[32];
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+        const int col = ch + j;
+        const bool in = rok && col < ncb && r0 + row >= c0 + col;
+        cv[j] = in ? Fs[(r0 + row) + static_cast<int64_t>(c0 + col) * LD] : 0.0;
+    }
+    const int ea = rok ? dexp[qa + row] : 0;
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tslot;
+    if (tid == 0) {
+        const uint32_t b0 = smem_addr(bar);
         bool ok = oz_wait(b0);
         if (ok) {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -808,17 +822,6 @@ __global__ void __launch_bounds__(256, 1) k_update_oz(StepArgs a, const int* __r
             atomicExch(err + 2, 1);
         }
     }
-    // this thread's row (TMEM lane) and 32 columns, and its C values, loaded while the MMAs run
-    const int row = 32 * (wid & 3) + lane, ch = 32 * (wid >> 2);
-    const bool rok = row < nra;
-    double cv[32];
-#pragma unroll
-    for (int j = 0; j < 32; ++j) {
-        const int col = ch + j;
-        const bool in = rok && col < ncb && r0 + row >= c0 + col;
-        cv[j] = in ? Fs[(r0 + row) + static_cast<int64_t>(c0 + col) * LD] : 0.0;
-    }
-    const int ea = rok ? dexp[qa + row] : 0;
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const bool ok = *fail == 0;
@@ -1120,21 +1123,13 @@ __global__ void __launch_bounds__(256, 2) k_update_tcs(StepArgs a, const int* __
     const int qa = prefix[a.dr_off + i] + bi * 128, qb = prefix[a.dr_off + i] + bj * T64;
     float* Fs = F + pd.F_off[s];
     const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
+    // thread 0 starts the copies first; TMEM allocation and every thread's C loads
+    // then overlap them
     if (tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_addr(bar)));
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_addr(bar + 1)));
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         *fail = 0;
-    }
-    if (wid == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 64;" :: "r"(smem_addr(tslot)));
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
-    }
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    const uint32_t tmem = *tslot;
-    if (tid == 0) {
         const uint32_t b0 = smem_addr(bar);
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
                      :: "r"(b0), "r"(static_cast<uint32_t>(2 * (kTsA + kTsB))) : "memory");
@@ -1147,6 +1142,27 @@ __global__ void __launch_bounds__(256, 2) k_update_tcs(StepArgs a, const int* __
         for (int c = 0; c < 4; ++c)
             asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
                          :: "r"(smem_addr(dst[c])), "l"(src[c]), "r"(len[c]), "r"(b0) : "memory");
+    }
+    if (wid == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 64;" :: "r"(smem_addr(tslot)));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    // this thread's row (TMEM lane) and 32 columns, and its C values
+    const int row = 32 * (wid & 3) + lane, ch = 32 * (wid >> 2);
+    const bool rok = row < nra;
+    float cv[32];
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+        const int col = ch + j;
+        const bool in = rok && col < ncb && r0 + row >= c0 + col;
+        cv[j] = in ? Fs[(r0 + row) + static_cast<int64_t>(c0 + col) * LD] : 0.f;
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tslot;
+    if (tid == 0) {
+        const uint32_t b0 = smem_addr(bar);
         bool ok = oz_wait(b0);
         if (ok) {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -1175,16 +1191,6 @@ __global__ void __launch_bounds__(256, 2) k_update_tcs(StepArgs a, const int* __
             *fail = 1;
             atomicExch(err + 2, 1);
         }
-    }
-    // this thread's row (TMEM lane) and 32 columns, and its C values, loaded while the MMAs run
-    const int row = 32 * (wid & 3) + lane, ch = 32 * (wid >> 2);
-    const bool rok = row < nra;
-    float cv[32];
-#pragma unroll
-    for (int j = 0; j < 32; ++j) {
-        const int col = ch + j;
-        const bool in = rok && col < ncb && r0 + row >= c0 + col;
-        cv[j] = in ? Fs[(r0 + row) + static_cast<int64_t>(c0 + col) * LD] : 0.f;
     }
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
