@@ -116,6 +116,8 @@ typedef struct sk_info {
     double start_merit;       /* max(rel pinf, rel dinf, rel gap) at the start point used */
     double fallback_merit;    /* the same for Mehrotra's start (SK_START_LEARNED runs), else 0 */
     int dependent_rows;       /* rows dropped as linearly dependent (sk_options.dependent_rows), else 0 */
+    double factor_ms_fp32;    /* device time of the last run's factorisations with FP32 fronts (batch-wide) */
+    double factor_ms_fp64;    /* the same with FP64 fronts */
 } sk_info;
 
 /* Fills the defaults listed above. */

@@ -397,6 +397,8 @@ struct DeviceIPM::Impl {
     std::vector<int> m_of, n_of, row_off, col_off;
     std::vector<double> R_h, C_h;           // Ruiz factors (batch order)
     std::vector<double> binf, cinf;         // ||b||_inf, ||c||_inf of the unscaled LPs
+    std::vector<int64_t> nnz_lp;            // entries of each LP's A
+    int64_t nnz_total = 0;
     // device vectors
     Slot<int> a_rp, a_ci, t_rp, t_ci, row_lp, col_lp, mc_s, mc_e, mc_p, nc_s, nc_e, nc_p;
     Slot<double> a_v, t_v, b, c, R, C;
@@ -418,6 +420,7 @@ struct DeviceIPM::Impl {
     std::vector<char> sw, sw_now;
     std::vector<int> pcg_k;
     double solve_ms = 0.0, device_ms = 0.0;
+    double factor_ms32 = 0.0, factor_ms64 = 0.0;   // device time of the run's factorisations
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::vector<double> hx0, hy0, hs0;      // user start (scaled)
     SpmvShape ga, gt;                       // SpMV launch shapes of A and A^T (autotuned at set-up)
@@ -584,6 +587,9 @@ DeviceIPM::DeviceIPM(const std::vector<ipm::LpView>& lps, const std::vector<cons
     for (int k = 0; k < I.nlp; ++k)
         if (!bad[k].empty()) throw api::sk_exception(SK_ERR_INVALID, bad[k]);
     cp[N] = static_cast<int>(nnz);
+    I.nnz_lp.assign(I.nlp, 0);
+    for (int k = 0; k < I.nlp; ++k) I.nnz_lp[k] = static_cast<int64_t>(cp[I.col_off[k + 1]]) - cp[I.col_off[k]];
+    I.nnz_total = static_cast<int64_t>(nnz);
     ipm::FrontPlan plan;
     ipm::build_front_plan(sl, A, opt.ordering, plan);
     lcp.clear();
@@ -725,6 +731,7 @@ void DeviceIPM::run() {
         SK_CUDA(cudaEventCreate(&I.ev1));
     }
     SK_CUDA(cudaEventRecord(I.ev0, st));
+    K.reset_factor_time();
     const auto& o = I.opt;
     if (o.start == SK_START_LEARNED && !I.gnn)
         throw api::sk_exception(SK_ERR_INVALID, "SK_START_LEARNED needs a network (sk_solver_set_gnn)");
@@ -789,6 +796,16 @@ void DeviceIPM::run() {
         spmv(N, I.gt, I.t_rp.ptr, I.t_ci.ptr, I.t_v.ptr, xx, EpiTheta{I.theta.ptr, K.scratch_n()}, st);
         spmv(M, I.ga, I.a_rp.ptr, I.a_ci.ptr, I.a_v.ptr, K.scratch_n(), EpiAxpby{1.0, 0.0, out}, st);
     };
+    // the same for the rows and columns of the LPs with a nonzero entry in d_on only
+    // (the batch is block diagonal: their rows of out are exact, the others' are left
+    // as they were)
+    double* d_on = I.sc(5);
+    auto normal_apply_some = [&](const double* xx, double* out) {
+        spmv_masked(N, I.gt.group, I.t_rp.ptr, I.t_ci.ptr, I.t_v.ptr, xx, I.col_lp.ptr, d_on,
+                    EpiTheta{I.theta.ptr, K.scratch_n()}, st);
+        spmv_masked(M, I.ga.group, I.a_rp.ptr, I.a_ci.ptr, I.a_v.ptr, K.scratch_n(), I.row_lp.ptr, d_on,
+                    EpiAxpby{1.0, 0.0, out}, st);
+    };
     auto resid_norm = [&](const double* rhs, const double* xx) {   // I.r = rhs - M0 xx, returns max|r| per LP
         spmv(N, I.gt, I.t_rp.ptr, I.t_ci.ptr, I.t_v.ptr, xx, EpiTheta{I.theta.ptr, K.scratch_n()}, st);
         spmv(M, I.ga, I.a_rp.ptr, I.a_ci.ptr, I.a_v.ptr, K.scratch_n(), EpiRhsMinus{rhs, I.r.ptr}, st);
@@ -797,6 +814,11 @@ void DeviceIPM::run() {
     };
     auto solve = [&](const double* rhs, double* out, std::vector<char>& ok) {
         ++I.solves;
+        // verbose >= 3: per-solve timing (the stream is drained first, so the time is this solve's)
+        const bool trace = o.verbose >= 3;
+        if (trace) SK_CUDA(cudaStreamSynchronize(st));
+        const auto ts0 = std::chrono::steady_clock::now();
+        const int steps0 = I.refine_steps;
         K.apply_inverse(rhs, out);
         std::vector<double> rn = resid_norm(rhs, out);
         std::vector<char> done(nlp, 0), stag(nlp, 0);
@@ -839,10 +861,21 @@ void DeviceIPM::run() {
                 SK_CUDA(cudaMemcpyAsync(I.bak.ptr, out, sizeof(double) * M, cudaMemcpyDeviceToDevice, st));
                 // preconditioner applications cover only the LPs still iterating (the
                 // others' rows come out 0, and their step sizes are 0)
+                // and while their entries are under half of A's, A Theta A^T p is formed
+                // for their rows alone
                 std::vector<char> sub(nlp, 0);
+                std::vector<double> subd(nlp, 0.0);
+                bool few = false;
                 auto restrict_to_running = [&]() {
-                    for (int k = 0; k < nlp; ++k) sub[k] = !done[k] && !stag[k];
+                    int64_t nz = 0;
+                    for (int k = 0; k < nlp; ++k) {
+                        sub[k] = !done[k] && !stag[k];
+                        subd[k] = sub[k] ? 1.0 : 0.0;
+                        if (sub[k]) nz += I.nnz_lp[k];
+                    }
                     K.restrict_solves(sub);
+                    few = 2 * nz < I.nnz_total;
+                    if (few) I.put_scalars(5, subd);
                 };
                 restrict_to_running();
                 K.apply_inverse(I.r.ptr, I.pz.ptr);
@@ -852,7 +885,8 @@ void DeviceIPM::run() {
                 int last_best_it = 0;
                 for (int it = 0; it < max_it; ++it) {
                     ++I.refine_steps;
-                    normal_apply(I.pp.ptr, I.pq.ptr);
+                    if (few) normal_apply_some(I.pp.ptr, I.pq.ptr);
+                    else normal_apply(I.pp.ptr, I.pq.ptr);
                     I.reduce_rows<1>(RedDot{I.pp.ptr, I.pq.ptr}, I.redout.ptr);
                     std::vector<double> pq = I.fetch(nlp);
                     bool run = false;
@@ -907,6 +941,13 @@ void DeviceIPM::run() {
         }
         if (K.solve_error())
             throw api::sk_exception(SK_ERR_CUDA, "triangular solve: a task timed out waiting for a dependency");
+        if (trace) {
+            int na = 0, nd = 0;
+            for (int k = 0; k < nlp; ++k) { na += I.active[k] != 0; nd += I.active[k] && !done[k]; }
+            std::fprintf(stderr, "[sk] solve: %d active LPs, %d needed refinement, %d steps, %.3f ms\n", na, nd,
+                         I.refine_steps - steps0,
+                         std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - ts0).count());
+        }
         ok.assign(nlp, 0);
         for (int k = 0; k < nlp; ++k) ok[k] = !I.active[k] || rn[k] <= tol[k];
     };
@@ -926,7 +967,14 @@ void DeviceIPM::run() {
         double delta = want_fp32 ? o.delta32 : (o.strict ? 1e-9 : o.delta64);
         for (int retry = 0; retry < (o.strict ? 5 : 6); ++retry, delta *= 10.0) {
             ++I.factorizations;
-            if (K.factor(I.theta.ptr, delta, want_fp32)) {
+            const double f0 = K.factor_ms(want_fp32);
+            const bool fok = K.factor(I.theta.ptr, delta, want_fp32);
+            if (o.verbose >= 3) {
+                const std::vector<int>& on = want_fp32 ? K.mask32() : K.mask64();
+                std::fprintf(stderr, "[sk] factor %s: %d LPs, %.3f ms\n", want_fp32 ? "fp32" : "fp64",
+                             static_cast<int>(std::count(on.begin(), on.end(), 1)), K.factor_ms(want_fp32) - f0);
+            }
+            if (fok) {
                 if (want_fp32) I.used_fp32 = true;
                 return true;
             }
@@ -1510,6 +1558,8 @@ void DeviceIPM::run() {
         SK_CUDA(cudaEventElapsedTime(&ms, I.ev0, I.ev1));
         I.device_ms = ms;
     }
+    I.factor_ms32 = K.factor_ms(true);
+    I.factor_ms64 = K.factor_ms(false);
     I.solve_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }
 
@@ -1553,6 +1603,8 @@ void DeviceIPM::result(int lp, double* x, double* y, double* s, sk_info* info) c
         info->flops_factor = p.flops_factor;
         info->start_merit = r.start_merit;
         info->fallback_merit = r.fallback_merit;
+        info->factor_ms_fp32 = I.factor_ms32;
+        info->factor_ms_fp64 = I.factor_ms64;
     }
 }
 

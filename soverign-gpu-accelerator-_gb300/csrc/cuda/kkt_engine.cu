@@ -1792,6 +1792,10 @@ KktEngine::KktEngine(const ipm::FrontPlan& plan, const DeviceLP& lp, cudaStream_
     reserve(arena_, tn_, static_cast<size_t>(std::max(1, p.N)));
     reserve(arena_, params_, 4);
     reserve(arena_, err_, 4);
+    for (auto& sb : sub_) {
+        reserve(arena_, sb.d_items, std::max<size_t>(1, p.step_items.size()));
+        reserve(arena_, sb.d_prefix, std::max<size_t>(1, p.step_prefix.size()));
+    }
     arena_.commit();
     auto bnd = [&](auto& slot) { bind(arena_, slot); };
     bnd(sn_first_); bnd(sn_ncols_); bnd(sn_nrows_); bnd(sn_lda_); bnd(sn_parent_); bnd(rows_); bnd(ea_map_); bnd(ch_ptr_);
@@ -1800,6 +1804,7 @@ KktEngine::KktEngine(const ipm::FrontPlan& plan, const DeviceLP& lp, cudaStream_
     bnd(slot_i_); bnd(slot_j_); bnd(w_col_); bnd(w_val_); bnd(inv_off_); bnd(blk_off_); bnd(fwd_tasks_);
     bnd(bwd_tasks_); bnd(g_dst_); bnd(g_zp_); bnd(g_ptr_); bnd(g_src_); bnd(sn_lp_); bnd(on32_); bnd(on64_); bnd(q_lp_); bnd(zc_sn_); bnd(zc_len_); bnd(zc_off_); bnd(flags_); bnd(counters_); bnd(solve_err_); bnd(D_); bnd(Mdiag_);
     bnd(zp_); bnd(xp_); bnd(zsol_); bnd(fvec_); bnd(tn_); bnd(params_); bnd(err_);
+    for (auto& sb : sub_) { bnd(sb.d_items); bnd(sb.d_prefix); }
     upload(sn_first_, p.sn_first, st_); upload(sn_ncols_, p.sn_ncols, st_); upload(sn_nrows_, p.sn_nrows, st_);
     upload(sn_lda_, p.sn_lda, st_);
     upload(sn_parent_, p.sn_parent, st_); upload(rows_, p.rows, st_); upload(ea_map_, p.ea_map, st_);
@@ -1818,9 +1823,21 @@ KktEngine::KktEngine(const ipm::FrontPlan& plan, const DeviceLP& lp, cudaStream_
     SK_CUDA(cudaStreamSynchronize(st_));
     set_smem_attrs<float>();
     set_smem_attrs<double>();
+    // per LP: the update blocks (plus the panel tiles) of one factorisation
+    lp_work_.assign(sn_lp.empty() ? 0 : static_cast<size_t>(*std::max_element(sn_lp.begin(), sn_lp.end())) + 1, 0.0);
+    for (const auto& st : p.steps)
+        for (int i = 0; i < st.nitems; ++i) {
+            const int s = p.step_items[st.item_off + i];
+            const double w = p.step_prefix[st.upd3_prefix_off + i + 1] - p.step_prefix[st.upd3_prefix_off + i] +
+                             p.step_prefix[st.trsm_prefix_off + i + 1] - p.step_prefix[st.trsm_prefix_off + i] + 1;
+            lp_work_[sn_lp[s]] += w;
+            total_work_ += w;
+        }
 }
 
 KktEngine::~KktEngine() {
+    for (int q = 0; q < 2; ++q)
+        if (fev_[q]) cudaEventDestroy(fev_[q]);
     for (int q = 0; q < 4; ++q)
         if (gfac_[q]) cudaGraphExecDestroy(gfac_[q]);
     for (int q = 0; q < 2; ++q)
@@ -1834,7 +1851,7 @@ PlanDev KktEngine::pd(bool fp32) const {
 }
 
 template <class T>
-void KktEngine::launch_factor(T* F, T* Linv, Prof* prof) {
+void KktEngine::launch_factor(T* F, T* Linv, Prof* prof, const SubSteps* sub) {
     auto run = [&](int cls, auto&& f) {
         if (prof) prof->timed(cls, f); else f();
     };
@@ -1859,14 +1876,18 @@ void KktEngine::launch_factor(T* F, T* Linv, Prof* prof) {
                 Mdiag_.ptr, D_.ptr, params_.ptr, q_lp_.ptr, pdv.lp_on, F);
         }
     });
+    const std::vector<ipm::PlanStep>& steps = sub ? sub->steps : p.steps;
+    const std::vector<int>& level_ptr = sub ? sub->level_ptr : p.step_level_ptr;
+    const int* items = sub ? sub->d_items.ptr : step_items_.ptr;
+    const int* prefix = sub ? sub->d_prefix.ptr : step_prefix_.ptr;
     for (int l = 0; l < p.nlevels; ++l) {
-        for (int q = p.step_level_ptr[l]; q < p.step_level_ptr[l + 1]; ++q) {
-            const auto& st = p.steps[q];
+        for (int q = level_ptr[l]; q < level_ptr[l + 1]; ++q) {
+            const auto& st = steps[q];
             StepArgs a{st.k,           st.item_off,         st.nitems,           st.trsm_prefix_off,
                        st.upd_prefix_off, st.upd2_prefix_off, st.upd3_prefix_off, st.digit_row_off};
             if (st.k == 0)   // later diagonal tiles are factored by the previous step's update
                 run(1, [&] {
-                    k_potrf<T><<<st.nitems, 256, potrf_smem(sizeof(T)), st_>>>(a, step_items_.ptr, pdv, F, Linv,
+                    k_potrf<T><<<st.nitems, 256, potrf_smem(sizeof(T)), st_>>>(a, items, pdv, F, Linv,
                                                                                inv_off_.ptr, err_.ptr);
                 });
             if (st.trsm_tiles > 0)
@@ -1877,17 +1898,17 @@ void KktEngine::launch_factor(T* F, T* Linv, Prof* prof) {
                             oz = true;
                             const int64_t plane = plan_.max_digit_rows * 128, lplane = max_step_items_ * T64 * 128;
                             k_oz_digits<<<static_cast<int>(st.trsm_tiles), 256, 0, st_>>>(
-                                a, step_items_.ptr, step_prefix_.ptr, pdv, F, dig_.ptr, dexp_.ptr, plane);
-                            k_oz_linv_digits<<<st.nitems, 256, 0, st_>>>(a, step_items_.ptr, pdv, Linv, inv_off_.ptr,
+                                a, items, prefix, pdv, F, dig_.ptr, dexp_.ptr, plane);
+                            k_oz_linv_digits<<<st.nitems, 256, 0, st_>>>(a, items, pdv, Linv, inv_off_.ptr,
                                                                          ldig_.ptr, lexp_.ptr, lplane);
                             k_trsm_oz<<<static_cast<int>(st.digit_rows / 128), 256, kOzSmem, st_>>>(
-                                a, step_items_.ptr, step_prefix_.ptr, pdv, F, dig_.ptr, dexp_.ptr, plane, ldig_.ptr,
+                                a, items, prefix, pdv, F, dig_.ptr, dexp_.ptr, plane, ldig_.ptr,
                                 lexp_.ptr, lplane, err_.ptr);
                         }
                     }
                     if (!oz)
                         k_trsm<T><<<static_cast<int>(st.trsm_tiles), 256, 2 * T64 * T64 * sizeof(T), st_>>>(
-                            a, step_items_.ptr, step_prefix_.ptr, pdv, F, Linv, inv_off_.ptr);
+                            a, items, prefix, pdv, F, Linv, inv_off_.ptr);
                 });
             if (st.upd_tiles > 0) {
                 run(3, [&] {
@@ -1897,9 +1918,9 @@ void KktEngine::launch_factor(T* F, T* Linv, Prof* prof) {
                             tc = true;
                             const int64_t plane = plan_.max_digit_rows * 256;
                             k_tc_split<<<static_cast<int>(st.trsm_tiles), 256, 0, st_>>>(
-                                a, step_items_.ptr, step_prefix_.ptr, pdv, F, dig_.ptr, plane);
+                                a, items, prefix, pdv, F, dig_.ptr, plane);
                             k_update_tcs<<<static_cast<int>(st.upd3_blocks), 256, kTsSmem, st_>>>(
-                                a, step_items_.ptr, step_prefix_.ptr, pdv, F, Linv, inv_off_.ptr, dig_.ptr, plane,
+                                a, items, prefix, pdv, F, Linv, inv_off_.ptr, dig_.ptr, plane,
                                 err_.ptr);
                         }
                     } else {
@@ -1907,19 +1928,19 @@ void KktEngine::launch_factor(T* F, T* Linv, Prof* prof) {
                             tc = true;
                             const int64_t plane = plan_.max_digit_rows * 128;
                             k_oz_digits<<<static_cast<int>(st.trsm_tiles), 256, 0, st_>>>(
-                                a, step_items_.ptr, step_prefix_.ptr, pdv, F, dig_.ptr, dexp_.ptr, plane);
+                                a, items, prefix, pdv, F, dig_.ptr, dexp_.ptr, plane);
                             k_update_oz<<<static_cast<int>(st.upd3_blocks), 256, kOzSmem, st_>>>(
-                                a, step_items_.ptr, step_prefix_.ptr, pdv, F, Linv, inv_off_.ptr, dig_.ptr,
+                                a, items, prefix, pdv, F, Linv, inv_off_.ptr, dig_.ptr,
                                 dexp_.ptr, plane, err_.ptr);
                         }
                     }
                     if (!tc)
                         k_update<T><<<static_cast<int>(st.upd_tiles), 256, potrf_smem(sizeof(T)), st_>>>(
-                            a, step_items_.ptr, step_prefix_.ptr, pdv, F, Linv, inv_off_.ptr, err_.ptr);
+                            a, items, prefix, pdv, F, Linv, inv_off_.ptr, err_.ptr);
                 });
                 if (prof) {
                     for (int it = 0; it < st.nitems; ++it) {
-                        const int s2 = p.step_items[st.item_off + it];
+                        const int s2 = (sub ? sub->items : p.step_items)[st.item_off + it];
                         const double w = std::min<int64_t>(T64, p.sn_ncols[s2] - static_cast<int64_t>(st.k) * T64);
                         const double t = p.sn_nrows[s2] - static_cast<double>(st.k) * T64 - w;
                         prof->upd_flops += 2.0 * w * t * (t + 1.0) / 2.0;
@@ -2017,6 +2038,68 @@ void KktEngine::ensure_digits() {
     bind(dig_arena_, lexp_);
 }
 
+// The step lists for a factorisation of the LPs of this precision's mask: the
+// plan's own (and its captured graph) while the LPs that are on hold at least 3/4
+// of the batch's update blocks, else lists restricted to them (rebuilt and
+// uploaded when the mask has changed since the last call).
+const KktEngine::SubSteps* KktEngine::pick_steps(bool fp32) {
+    const std::vector<int>& mask = fp32 ? on32_h_ : on64_h_;
+    double on_work = 0.0;
+    for (size_t k = 0; k < mask.size() && k < lp_work_.size(); ++k)
+        if (mask[k]) on_work += lp_work_[k];
+    if (on_work >= 0.75 * total_work_) return nullptr;
+    SubSteps& sb = sub_[fp32 ? 0 : 1];
+    if (sb.mask == mask && !sb.level_ptr.empty()) return &sb;
+    const auto& p = plan_;
+    sb.mask = mask;
+    sb.steps.clear();
+    sb.items.clear();
+    sb.prefix.clear();
+    sb.level_ptr.assign(static_cast<size_t>(p.nlevels) + 1, 0);
+    std::vector<int> keep;
+    for (int l = 0; l < p.nlevels; ++l) {
+        for (int q = p.step_level_ptr[l]; q < p.step_level_ptr[l + 1]; ++q) {
+            const ipm::PlanStep& st = p.steps[q];
+            keep.clear();
+            for (int i = 0; i < st.nitems; ++i) {
+                const int lp = sn_lp_h_[p.step_items[st.item_off + i]];
+                if (lp < static_cast<int>(mask.size()) && mask[lp]) keep.push_back(i);
+            }
+            if (keep.empty()) continue;
+            ipm::PlanStep c = st;
+            c.item_off = static_cast<int>(sb.items.size());
+            c.nitems = static_cast<int>(keep.size());
+            for (int i : keep) sb.items.push_back(p.step_items[st.item_off + i]);
+            // the kept items' counts, summed again from 0
+            auto remap = [&](int off, int64_t& total) {
+                const int at = static_cast<int>(sb.prefix.size());
+                int64_t acc = 0;
+                sb.prefix.push_back(0);
+                for (int i : keep) {
+                    acc += p.step_prefix[off + i + 1] - p.step_prefix[off + i];
+                    sb.prefix.push_back(static_cast<int>(acc));
+                }
+                total = acc;
+                return at;
+            };
+            c.trsm_prefix_off = remap(st.trsm_prefix_off, c.trsm_tiles);
+            c.upd_prefix_off = remap(st.upd_prefix_off, c.upd_tiles);
+            c.upd2_prefix_off = remap(st.upd2_prefix_off, c.upd2_blocks);
+            c.upd3_prefix_off = remap(st.upd3_prefix_off, c.upd3_blocks);
+            c.digit_row_off = remap(st.digit_row_off, c.digit_rows);
+            sb.steps.push_back(c);
+        }
+        sb.level_ptr[l + 1] = static_cast<int>(sb.steps.size());
+    }
+    if (!sb.items.empty())
+        SK_CUDA(cudaMemcpyAsync(sb.d_items.ptr, sb.items.data(), sizeof(int) * sb.items.size(),
+                                cudaMemcpyHostToDevice, st_));
+    if (!sb.prefix.empty())
+        SK_CUDA(cudaMemcpyAsync(sb.d_prefix.ptr, sb.prefix.data(), sizeof(int) * sb.prefix.size(),
+                                cudaMemcpyHostToDevice, st_));
+    return &sb;
+}
+
 bool KktEngine::factor(const double* d_theta, double delta, bool fp32) {
     const int q = fp32 ? (tensor_ ? 2 : 1) : (emulate64_ ? 3 : 0);
     ensure_fronts(fp32);
@@ -2024,21 +2107,39 @@ bool KktEngine::factor(const double* d_theta, double delta, bool fp32) {
     fp32_ = fp32;
     double hp[4] = {delta, 0, 0, 0};
     SK_CUDA(cudaMemcpyAsync(params_.ptr, hp, sizeof(hp), cudaMemcpyHostToDevice, st_));
-    if (!gfac_[q] || gfac_theta_[q] != d_theta) {
-        if (gfac_[q]) { cudaGraphExecDestroy(gfac_[q]); gfac_[q] = nullptr; }
-        theta_bound_ = d_theta;
-        cudaGraph_t g;
-        SK_CUDA(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
-        if (fp32) launch_factor<float>(F32_.ptr, Linv32_.ptr); else launch_factor<double>(F64_.ptr, Linv64_.ptr);
-        SK_CUDA(cudaStreamEndCapture(st_, &g));
-        SK_CUDA(cudaGraphInstantiate(&gfac_[q], g, 0));
-        cudaGraphDestroy(g);
-        gfac_theta_[q] = d_theta;
+    if (!fev_[0]) {
+        SK_CUDA(cudaEventCreate(&fev_[0]));
+        SK_CUDA(cudaEventCreate(&fev_[1]));
     }
-    SK_CUDA(cudaGraphLaunch(gfac_[q], st_));
+    const SubSteps* sub = pick_steps(fp32);
+    if (sub) {   // a few LPs of the batch: their blocks only, launched directly
+        theta_bound_ = d_theta;
+        SK_CUDA(cudaEventRecord(fev_[0], st_));
+        if (fp32) launch_factor<float>(F32_.ptr, Linv32_.ptr, nullptr, sub);
+        else launch_factor<double>(F64_.ptr, Linv64_.ptr, nullptr, sub);
+        SK_CUDA(cudaEventRecord(fev_[1], st_));
+    } else {
+        if (!gfac_[q] || gfac_theta_[q] != d_theta) {
+            if (gfac_[q]) { cudaGraphExecDestroy(gfac_[q]); gfac_[q] = nullptr; }
+            theta_bound_ = d_theta;
+            cudaGraph_t g;
+            SK_CUDA(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
+            if (fp32) launch_factor<float>(F32_.ptr, Linv32_.ptr); else launch_factor<double>(F64_.ptr, Linv64_.ptr);
+            SK_CUDA(cudaStreamEndCapture(st_, &g));
+            SK_CUDA(cudaGraphInstantiate(&gfac_[q], g, 0));
+            cudaGraphDestroy(g);
+            gfac_theta_[q] = d_theta;
+        }
+        SK_CUDA(cudaEventRecord(fev_[0], st_));
+        SK_CUDA(cudaGraphLaunch(gfac_[q], st_));
+        SK_CUDA(cudaEventRecord(fev_[1], st_));
+    }
     int herr[3];
     SK_CUDA(cudaMemcpyAsync(herr, err_.ptr, sizeof(herr), cudaMemcpyDeviceToHost, st_));
     SK_CUDA(cudaStreamSynchronize(st_));
+    float fms = 0.f;
+    SK_CUDA(cudaEventElapsedTime(&fms, fev_[0], fev_[1]));
+    fact_ms_[fp32 ? 0 : 1] += fms;
     if (herr[2]) throw std::runtime_error("tensor-core update: a copy or an MMA did not complete in time");
     failed_sn_ = herr[0] ? herr[1] : -1;
     return herr[0] == 0;

@@ -28,6 +28,12 @@ public:
     // in FP64 (fp32 = false) or FP32 fronts. Returns true when every pivot was
     // positive (one host synchronisation).
     bool factor(const double* d_theta, double delta, bool fp32);
+    // Device time of the factor() calls since reset_factor_time(), per front precision
+    // (CUDA events around each factorisation graph).
+    double factor_ms(bool fp32) const { return fact_ms_[fp32 ? 0 : 1]; }
+    void reset_factor_time() { fact_ms_[0] = fact_ms_[1] = 0.0; }
+    const std::vector<int>& mask32() const { return on32_h_; }   // per LP: 1 = fronts in that precision
+    const std::vector<int>& mask64() const { return on64_h_; }
     // FP32 fronts: trailing updates on the tensor cores (tcgen05, TF32 x3; default) or
     // as exact FP32 SIMT arithmetic. Applies to the next factor() call.
     void set_tensor_update(bool on) { tensor_ = on; }
@@ -87,7 +93,23 @@ private:
     void run_factor_levels(bool fp32);
     void run_solve_levels();
     struct Prof;
-    template <class T> void launch_factor(T* F, T* Linv, Prof* prof = nullptr);
+    // The plan's tile steps restricted to the fronts of the LPs of one mask: the
+    // items of each step whose LP is on and their prefix arrays, rebuilt when the
+    // mask changes, so that a factorisation of a few LPs of a large batch launches
+    // only their blocks (each launch of the full plan has one block per tile of
+    // every front, and those of LPs that are off still take an SM slot each).
+    struct SubSteps {
+        std::vector<int> mask;                  // the mask the lists were built for
+        std::vector<ipm::PlanStep> steps;
+        std::vector<int> level_ptr;             // nlevels + 1 into steps
+        std::vector<int> items, prefix;
+        Slot<int> d_items, d_prefix;
+    };
+    SubSteps sub_[2];                           // FP32 passes, FP64 passes
+    std::vector<double> lp_work_;               // per LP: update blocks of one factorisation
+    double total_work_ = 0.0;
+    const SubSteps* pick_steps(bool fp32);
+    template <class T> void launch_factor(T* F, T* Linv, Prof* prof = nullptr, const SubSteps* sub = nullptr);
     template <class T> void launch_solve(const T* F, const T* Linv, Prof* prof = nullptr);
     void ensure_fronts(bool fp32);
     void ensure_digits();
@@ -139,6 +161,8 @@ private:
     int64_t max_step_items_ = 1;
     // FP64, FP32 SIMT update, FP32 tensor-core update, FP64 emulated on the tensor cores
     cudaGraphExec_t gfac_[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t fev_[2] = {nullptr, nullptr};
+    double fact_ms_[2] = {0.0, 0.0};
     cudaGraphExec_t gsol_[2] = {nullptr, nullptr};
     const double* gfac_theta_[4] = {nullptr, nullptr, nullptr, nullptr};
 };

@@ -58,6 +58,24 @@ __global__ void __launch_bounds__(256) k_spmv(int rows, const int* __restrict__ 
 
 inline int spmv_blocks(int64_t threads) { return static_cast<int>((threads + 255) / 256); }
 
+// k_spmv over the rows of the LPs whose entry of `on` is nonzero (lp_of: the LP of
+// each row); the other rows are skipped without reading their entries, and their
+// outputs are left as they are.
+template <int G, class Epi>
+__global__ void __launch_bounds__(256) k_spmv_masked(int rows, const int* __restrict__ rp, const int* __restrict__ ci,
+                                                     const double* __restrict__ v, const double* __restrict__ x,
+                                                     const int* __restrict__ lp_of, const double* __restrict__ on,
+                                                     Epi epi) {
+    const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int row = gid / G, lane = gid % G;
+    const bool valid = row < rows && on[lp_of[row]] != 0.0;
+    double acc = 0.0;
+    if (valid) acc = spmv_row_part<G>(rp[row] + lane, rp[row + 1], ci, v, x, 0);
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, G);
+    if (valid && lane == 0) epi(row, acc);
+}
+
 // Launches the SpMV with `group` lanes per row (2, 4, 8, 16; anything else: 32).
 template <class Epi>
 void spmv(int rows, int group, const int* rp, const int* ci, const double* v, const double* x, Epi epi,
@@ -70,6 +88,21 @@ void spmv(int rows, int group, const int* rp, const int* ci, const double* v, co
     case 8: k_spmv<8><<<spmv_blocks(threads), 256, 0, st>>>(rows, rp, ci, v, x, epi); break;
     case 16: k_spmv<16><<<spmv_blocks(threads), 256, 0, st>>>(rows, rp, ci, v, x, epi); break;
     default: k_spmv<32><<<spmv_blocks(threads), 256, 0, st>>>(rows, rp, ci, v, x, epi); break;
+    }
+}
+
+// Launches k_spmv_masked with `group` lanes per row (as spmv above).
+template <class Epi>
+void spmv_masked(int rows, int group, const int* rp, const int* ci, const double* v, const double* x,
+                 const int* lp_of, const double* on, Epi epi, cudaStream_t st) {
+    if (rows <= 0) return;
+    const int64_t threads = static_cast<int64_t>(rows) * group;
+    switch (group) {
+    case 2: k_spmv_masked<2><<<spmv_blocks(threads), 256, 0, st>>>(rows, rp, ci, v, x, lp_of, on, epi); break;
+    case 4: k_spmv_masked<4><<<spmv_blocks(threads), 256, 0, st>>>(rows, rp, ci, v, x, lp_of, on, epi); break;
+    case 8: k_spmv_masked<8><<<spmv_blocks(threads), 256, 0, st>>>(rows, rp, ci, v, x, lp_of, on, epi); break;
+    case 16: k_spmv_masked<16><<<spmv_blocks(threads), 256, 0, st>>>(rows, rp, ci, v, x, lp_of, on, epi); break;
+    default: k_spmv_masked<32><<<spmv_blocks(threads), 256, 0, st>>>(rows, rp, ci, v, x, lp_of, on, epi); break;
     }
 }
 

@@ -42,7 +42,7 @@ class Info(C.Structure):
                 ("setup_ms", C.c_double), ("solve_ms", C.c_double), ("nnz_factor", C.c_longlong),
                 ("num_supernodes", C.c_int), ("dense_front", C.c_int), ("device_ms", C.c_double),
                 ("flops_factor", C.c_double), ("start_merit", C.c_double), ("fallback_merit", C.c_double),
-                ("dependent_rows", C.c_int)]
+                ("dependent_rows", C.c_int), ("factor_ms_fp32", C.c_double), ("factor_ms_fp64", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
