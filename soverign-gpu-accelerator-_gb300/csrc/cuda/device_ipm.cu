@@ -958,28 +958,47 @@ void DeviceIPM::run() {
     // FP32 trailing updates run on the tensor cores (TF32 x3) while mu >= kTensorMu; the
     // last FP32 iterations, whose directions decide the FP64 switch, use exact FP32.
     bool tensor_now = true;
-    // One precision's fronts (the LPs of that precision's mask) through the delta ladder.
+    // One precision's fronts (the LPs of that precision's mask) through the delta
+    // ladder. The LPs are independent blocks of one matrix: after a pass in which some
+    // of them had a pivot that was not positive, only those are assembled and factored
+    // again, with delta x10, while the others keep the factors they have. On failure
+    // ladder_failed holds the LPs that failed every pass.
     const bool emulate64 = o.fp64_update == SK_FP64_UPDATE_TENSOR ||
                            (o.fp64_update == SK_FP64_UPDATE_AUTO && o.precision == SK_PREC_MIXED);
+    std::vector<char> ladder_failed;
     auto ladder = [&](bool want_fp32) -> bool {
         K.set_tensor_update(tensor_now);
         K.set_fp64_emulation(emulate64);
         double delta = want_fp32 ? o.delta32 : (o.strict ? 1e-9 : o.delta64);
+        const std::vector<char> m32(K.mask32().begin(), K.mask32().end());
+        const std::vector<char> m64(K.mask64().begin(), K.mask64().end());
+        std::vector<char> pend = want_fp32 ? m32 : m64;
+        bool ok = false, narrowed = false;
         for (int retry = 0; retry < (o.strict ? 5 : 6); ++retry, delta *= 10.0) {
             ++I.factorizations;
             const double f0 = K.factor_ms(want_fp32);
             const bool fok = K.factor(I.theta.ptr, delta, want_fp32);
             if (o.verbose >= 3) {
                 const std::vector<int>& on = want_fp32 ? K.mask32() : K.mask64();
-                std::fprintf(stderr, "[sk] factor %s: %d LPs, %.3f ms\n", want_fp32 ? "fp32" : "fp64",
-                             static_cast<int>(std::count(on.begin(), on.end(), 1)), K.factor_ms(want_fp32) - f0);
+                std::fprintf(stderr, "[sk] factor %s: %d LPs, delta %.0e, %.3f ms\n", want_fp32 ? "fp32" : "fp64",
+                             static_cast<int>(std::count(on.begin(), on.end(), 1)), delta,
+                             K.factor_ms(want_fp32) - f0);
             }
-            if (fok) {
-                if (want_fp32) I.used_fp32 = true;
-                return true;
-            }
+            if (fok) { ok = true; break; }
+            std::vector<char> nf(nlp, 0);
+            bool any = false;
+            for (int k : K.failed_lps())
+                if (k >= 0 && k < nlp && pend[k]) { nf[k] = 1; any = true; }
+            if (!any) continue;          // no LP recorded: all of them again
+            pend = nf;
+            narrowed = true;
+            if (want_fp32) K.set_masks(pend, m64);
+            else K.set_masks(m32, pend);
         }
-        return false;
+        if (narrowed) K.set_masks(m32, m64);
+        if (ok && want_fp32) I.used_fp32 = true;
+        ladder_failed = ok ? std::vector<char>(nlp, 0) : pend;
+        return ok;
     };
     auto any_of = [&](const std::vector<char>& v) {
         for (char c : v) if (c) return true;
@@ -996,29 +1015,25 @@ void DeviceIPM::run() {
         if (I.res[k].switch_iteration < 0) I.res[k].switch_iteration = it;
     };
     // Factors every active LP: FP32 fronts for the LPs not (yet) switched, FP64 fronts
-    // for the others. When the FP32 ladder fails, the LP whose pivot failed moves to
-    // FP64 fronts (up to four LPs one by one, then all that remain); with `sticky`
-    // false that move lasts for this factorisation only (start points). Returns false
-    // when the FP64 ladder fails.
+    // for the others. The LPs whose FP32 pivots failed at every delta of the ladder
+    // move to FP64 fronts (the other LPs keep their FP32 factors); with `sticky` false
+    // that move lasts for this factorisation only (start points). Returns false when
+    // the FP64 ladder fails.
     auto factor_all = [&](int it, bool sticky) -> bool {
         I.sw_now = I.sw;
         std::vector<char> on32, on64;
         masks_now(on32, on64);
         const std::vector<char> none(nlp, 0);
-        int single = 0;
-        while (any_of(on32)) {
+        if (any_of(on32)) {
             K.set_masks(on32, none);
-            if (ladder(true)) break;
-            const int k = K.failed_lp();
-            std::vector<char> move(nlp, 0);
-            if (k >= 0 && k < nlp && on32[k] && single < 4) { move[k] = 1; ++single; }
-            else move = on32;
-            for (int q = 0; q < nlp; ++q) {
-                if (!move[q]) continue;
-                if (o.verbose) std::fprintf(stderr, "[sk] lp %d: FP32 factorisation failed, FP64 fronts\n", q);
-                if (sticky) mark_switch(q, it);
-                else I.sw_now[q] = 1;
-                on32[q] = 0;
+            if (!ladder(true)) {
+                const std::vector<char> move = any_of(ladder_failed) ? ladder_failed : on32;
+                for (int q = 0; q < nlp; ++q) {
+                    if (!move[q] || !on32[q]) continue;
+                    if (o.verbose) std::fprintf(stderr, "[sk] lp %d: FP32 factorisation failed, FP64 fronts\n", q);
+                    if (sticky) mark_switch(q, it);
+                    else I.sw_now[q] = 1;
+                }
             }
         }
         masks_now(on32, on64);
@@ -1044,9 +1059,9 @@ void DeviceIPM::run() {
     // acc[k]: the solve met its tolerance and e1, e2, e3 <= 1e-8 (the reference's test);
     // use[k]: the direction may be used (strict: acc; otherwise finite with e1, e2, e3 <= 1e-6).
     struct DirStats { std::vector<double> e1, e2, e3, rx, rs, xs, xds, dxs, dxds; };
+    std::vector<char> solved;   // per LP: the last direction's solve met its tolerance
     auto direction = [&](double* dxo, double* dyo, double* dso, const double* rxs, std::vector<char>& acc,
                          std::vector<char>& use, DirStats& ds_) {
-        std::vector<char> solved;
         spmv(M, I.ga, I.a_rp.ptr, I.a_ci.ptr, I.a_v.ptr, I.v.ptr, EpiSub{I.rp.ptr, I.rkkt.ptr}, st);
         solve(I.rkkt.ptr, dyo, solved);
         spmv(N, I.gt, I.t_rp.ptr, I.t_ci.ptr, I.t_v.ptr, dyo,
@@ -1306,7 +1321,9 @@ void DeviceIPM::run() {
         bool fac_ok = true;
         // An FP32 direction that misses the check is first recomputed with the same
         // factor and a 100x tighter PCG target; an LP whose direction misses again moves
-        // to FP64 fronts (alone: the other LPs keep their precision).
+        // to FP64 fronts (alone: the other LPs keep their precision). An LP whose PCG
+        // did not reach its tolerance moves at once: PCG from the same start with the
+        // same factor repeats the same steps, so a tighter target cannot be met.
         std::vector<char> tightened(nlp, 0);
         auto retry_fp32_misses = [&](const std::vector<char>& acc, const char* what) -> int {
             // returns 0: nothing to redo; 1: redo the direction; -1: FP64 factorisation failed
@@ -1315,7 +1332,7 @@ void DeviceIPM::run() {
             for (int k = 0; k < nlp; ++k) {
                 if (!I.active[k] || I.sw[k] || acc[k]) continue;
                 redo = true;
-                if (!tightened[k]) { tightened[k] = 1; tol[k] *= 0.01; }
+                if (!tightened[k] && solved[k]) { tightened[k] = 1; tol[k] *= 0.01; }
                 else { now[k] = 1; any_now = true; }
             }
             if (any_now) {

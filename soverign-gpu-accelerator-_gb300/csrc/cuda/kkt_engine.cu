@@ -37,6 +37,7 @@ struct PlanDev {
     const int* sn_parent;
     const int* sn_lp;      // LP of each front (fronts never span LPs)
     const int* lp_on;      // 1 while an LP of the batch is still being solved; 0 skips its fronts
+    int* lp_fail;          // per LP: set to 1 when one of its pivots was not positive
 };
 
 namespace {
@@ -304,6 +305,7 @@ __device__ __noinline__ void potrf_tile(int s, int kstep, PlanDev pd, T* F, T* _
                     T p = A[c * LDS + c];
                     if (!(p > T(0))) {
                         if (atomicCAS(err, 0, 1) == 0) err[1] = s;
+                        pd.lp_fail[pd.sn_lp[s]] = 1;
                         p = T(1);
                     }
                     const T d = sqrt(p);
@@ -1792,6 +1794,7 @@ KktEngine::KktEngine(const ipm::FrontPlan& plan, const DeviceLP& lp, cudaStream_
     reserve(arena_, tn_, static_cast<size_t>(std::max(1, p.N)));
     reserve(arena_, params_, 4);
     reserve(arena_, err_, 4);
+    reserve(arena_, lp_fail_, std::max<size_t>(1, static_cast<size_t>(p.nlp)));
     for (auto& sb : sub_) {
         reserve(arena_, sb.d_items, std::max<size_t>(1, p.step_items.size()));
         reserve(arena_, sb.d_prefix, std::max<size_t>(1, p.step_prefix.size()));
@@ -1803,7 +1806,7 @@ KktEngine::KktEngine(const ipm::FrontPlan& plan, const DeviceLP& lp, cudaStream_
     bnd(step_prefix_); bnd(round_items_); bnd(round_prefix_); bnd(level_sn_); bnd(slot_pos_); bnd(w_ptr_);
     bnd(slot_i_); bnd(slot_j_); bnd(w_col_); bnd(w_val_); bnd(inv_off_); bnd(blk_off_); bnd(fwd_tasks_);
     bnd(bwd_tasks_); bnd(g_dst_); bnd(g_zp_); bnd(g_ptr_); bnd(g_src_); bnd(sn_lp_); bnd(on32_); bnd(on64_); bnd(q_lp_); bnd(zc_sn_); bnd(zc_len_); bnd(zc_off_); bnd(flags_); bnd(counters_); bnd(solve_err_); bnd(D_); bnd(Mdiag_);
-    bnd(zp_); bnd(xp_); bnd(zsol_); bnd(fvec_); bnd(tn_); bnd(params_); bnd(err_);
+    bnd(zp_); bnd(xp_); bnd(zsol_); bnd(fvec_); bnd(tn_); bnd(params_); bnd(err_); bnd(lp_fail_);
     for (auto& sb : sub_) { bnd(sb.d_items); bnd(sb.d_prefix); }
     upload(sn_first_, p.sn_first, st_); upload(sn_ncols_, p.sn_ncols, st_); upload(sn_nrows_, p.sn_nrows, st_);
     upload(sn_lda_, p.sn_lda, st_);
@@ -1847,7 +1850,7 @@ KktEngine::~KktEngine() {
 PlanDev KktEngine::pd(bool fp32) const {
     return PlanDev{sn_first_.ptr, sn_ncols_.ptr, sn_nrows_.ptr, sn_lda_.ptr, sn_F_off_.ptr, sn_f_off_.ptr, sn_rows_off_.ptr,
                    rows_.ptr, ea_off_.ptr, ea_map_.ptr, ch_ptr_.ptr, ch_list_.ptr, sn_parent_.ptr, sn_lp_.ptr,
-                   fp32 ? on32_.ptr : on64_.ptr};
+                   fp32 ? on32_.ptr : on64_.ptr, lp_fail_.ptr};
 }
 
 template <class T>
@@ -1860,6 +1863,7 @@ void KktEngine::launch_factor(T* F, T* Linv, Prof* prof, const SubSteps* sub) {
     if (nzc_ > 0)
         k_zero_fronts<T><<<static_cast<int>(nzc_), 256, 0, st_>>>(zc_sn_.ptr, zc_len_.ptr, zc_off_.ptr, pdv, F);
     SK_CUDA(cudaMemsetAsync(err_.ptr, 0, 4 * sizeof(int), st_));
+    SK_CUDA(cudaMemsetAsync(lp_fail_.ptr, 0, lp_fail_.count * sizeof(int), st_));
     const double* theta = theta_bound_;
     run(0, [&] {
         if (p.dense_mode) {
@@ -2142,6 +2146,13 @@ bool KktEngine::factor(const double* d_theta, double delta, bool fp32) {
     fact_ms_[fp32 ? 0 : 1] += fms;
     if (herr[2]) throw std::runtime_error("tensor-core update: a copy or an MMA did not complete in time");
     failed_sn_ = herr[0] ? herr[1] : -1;
+    failed_lps_.clear();
+    if (herr[0]) {
+        std::vector<int> f(lp_fail_.count, 0);
+        SK_CUDA(cudaMemcpy(f.data(), lp_fail_.ptr, sizeof(int) * f.size(), cudaMemcpyDeviceToHost));
+        for (size_t k = 0; k < f.size(); ++k)
+            if (f[k]) failed_lps_.push_back(static_cast<int>(k));
+    }
     return herr[0] == 0;
 }
 

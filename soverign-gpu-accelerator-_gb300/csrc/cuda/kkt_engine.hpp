@@ -61,6 +61,8 @@ public:
     void set_masks(const std::vector<char>& on32, const std::vector<char>& on64);
     // LP of the front whose pivot failed in the last factor() (-1 if none).
     int failed_lp() const;
+    // Every LP with a pivot that was not positive in the last factor() (ascending).
+    const std::vector<int>& failed_lps() const { return failed_lps_; }
     // Restricts apply_inverse to the LPs flagged in `sub` (within the masks in force),
     // e.g. the LPs whose conjugate-gradient iteration has not converged yet; rows of
     // the other LPs then come out 0. unrestrict_solves() brings back the masks.
@@ -152,6 +154,8 @@ private:
     Slot<int> err_;
     bool fp32_ = false;
     int failed_sn_ = -1;
+    std::vector<int> failed_lps_;
+    Slot<int> lp_fail_;                         // per LP: a pivot failed in this factorisation
     const double* theta_bound_ = nullptr;
     bool tensor_ = true;
     bool emulate64_ = false;
