@@ -404,6 +404,7 @@ struct DeviceIPM::Impl {
     Slot<double> a_v, t_v, b, c, R, C;
     Slot<double> x, y, s, rp, rd, theta, rxs, v, rkkt, dy, dx, ds, dxa, dya, dsa, e1, e2, e3;
     Slot<double> xt, yt, stt, rpt, rdt, r, corr, bak, tm, cdx, cdy, cds, crxs, pz, pp, pq;
+    Slot<double> kdx, kdy, kds;             // directions kept while a direction is redone for some LPs
     Slot<double> scal;                      // per-LP scalars [8][nlp]
     Slot<double> partial, redout;
     int max_chunks = 0;
@@ -612,10 +613,10 @@ DeviceIPM::DeviceIPM(const std::vector<ipm::LpView>& lps, const std::vector<cons
     reserve(ar, I.mc_s, ms.size()); reserve(ar, I.mc_e, me.size()); reserve(ar, I.mc_p, mp.size());
     reserve(ar, I.nc_s, ns_.size()); reserve(ar, I.nc_e, ne.size()); reserve(ar, I.nc_p, np_.size());
     for (auto* sl2 : {&I.x, &I.s, &I.rd, &I.theta, &I.rxs, &I.v, &I.dx, &I.ds, &I.dxa, &I.dsa, &I.e2, &I.e3, &I.xt,
-                      &I.stt, &I.rdt, &I.cdx, &I.cds, &I.crxs})
+                      &I.stt, &I.rdt, &I.cdx, &I.cds, &I.crxs, &I.kdx, &I.kds})
         reserve(ar, *sl2, N);
     for (auto* sl2 : {&I.y, &I.rp, &I.rkkt, &I.dy, &I.dya, &I.e1, &I.yt, &I.rpt, &I.r, &I.corr, &I.bak, &I.tm, &I.cdy,
-                      &I.pz, &I.pp, &I.pq})
+                      &I.pz, &I.pp, &I.pq, &I.kdy})
         reserve(ar, *sl2, M);
     reserve(ar, I.scal, static_cast<size_t>(8) * I.nlp);
     reserve(ar, I.partial, static_cast<size_t>(I.max_chunks) * kMaxR);
@@ -627,7 +628,7 @@ DeviceIPM::DeviceIPM(const std::vector<ipm::LpView>& lps, const std::vector<cons
     for (auto* sl2 : {&I.a_v, &I.t_v, &I.b, &I.c, &I.R, &I.C, &I.x, &I.s, &I.rd, &I.theta, &I.rxs, &I.v, &I.dx, &I.ds,
                       &I.dxa, &I.dsa, &I.e2, &I.e3, &I.xt, &I.stt, &I.rdt, &I.cdx, &I.cds, &I.crxs, &I.y, &I.rp,
                       &I.rkkt, &I.dy, &I.dya, &I.e1, &I.yt, &I.rpt, &I.r, &I.corr, &I.bak, &I.tm, &I.cdy, &I.scal,
-                      &I.partial, &I.redout, &I.pz, &I.pp, &I.pq})
+                      &I.partial, &I.redout, &I.pz, &I.pp, &I.pq, &I.kdx, &I.kds, &I.kdy})
         bind(ar, *sl2);
     upload(I.a_rp, A.row_ptrs, I.st); upload(I.a_ci, A.col_indices, I.st); upload(I.a_v, A.values, I.st);
     upload(I.t_rp, cp, I.st); upload(I.t_ci, ri, I.st); upload(I.t_v, cv, I.st);
@@ -812,19 +813,23 @@ void DeviceIPM::run() {
         I.reduce_rows<1>(RedAbsMax{I.r.ptr}, I.redout.ptr);
         return I.fetch(nlp);
     };
-    auto solve = [&](const double* rhs, double* out, std::vector<char>& ok) {
+    // which (optional): solve for these LPs only; the others' rows of out are not
+    // meaningful afterwards and their ok entries are left as they are
+    auto solve = [&](const double* rhs, double* out, std::vector<char>& ok, const std::vector<char>* which = nullptr) {
         ++I.solves;
         // verbose >= 3: per-solve timing (the stream is drained first, so the time is this solve's)
         const bool trace = o.verbose >= 3;
         if (trace) SK_CUDA(cudaStreamSynchronize(st));
         const auto ts0 = std::chrono::steady_clock::now();
         const int steps0 = I.refine_steps;
+        if (which) K.restrict_solves(*which);
         K.apply_inverse(rhs, out);
+        if (which) K.unrestrict_solves();
         std::vector<double> rn = resid_norm(rhs, out);
         std::vector<char> done(nlp, 0), stag(nlp, 0);
         I.last_pcg = 0;
         std::vector<int> steps(nlp, 0);
-        for (int k = 0; k < nlp; ++k) done[k] = !I.active[k] || rn[k] <= tol[k];
+        for (int k = 0; k < nlp; ++k) done[k] = !I.active[k] || (which && !(*which)[k]) || rn[k] <= tol[k];
         if (o.strict) {
             for (int it = 0; it < 10; ++it) {
                 bool any = false;
@@ -948,8 +953,9 @@ void DeviceIPM::run() {
                          I.refine_steps - steps0,
                          std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - ts0).count());
         }
-        ok.assign(nlp, 0);
-        for (int k = 0; k < nlp; ++k) ok[k] = !I.active[k] || rn[k] <= tol[k];
+        ok.resize(nlp, 0);
+        for (int k = 0; k < nlp; ++k)
+            if (!which || (*which)[k]) ok[k] = !I.active[k] || rn[k] <= tol[k];
     };
     // ---- factorisation with delta retries and the precision policy
     // delta: the reference's 1e-9 x10 ladder in strict mode (src/cuda/kkt.cu:35, 665-669);
@@ -1060,18 +1066,40 @@ void DeviceIPM::run() {
     // use[k]: the direction may be used (strict: acc; otherwise finite with e1, e2, e3 <= 1e-6).
     struct DirStats { std::vector<double> e1, e2, e3, rx, rs, xs, xds, dxs, dxds; };
     std::vector<char> solved;   // per LP: the last direction's solve met its tolerance
+    // which (optional): a direction redone for these LPs alone; the other LPs keep
+    // the direction, statistics and flags of the previous call with the same outputs
     auto direction = [&](double* dxo, double* dyo, double* dso, const double* rxs, std::vector<char>& acc,
-                         std::vector<char>& use, DirStats& ds_) {
+                         std::vector<char>& use, DirStats& ds_, const std::vector<char>* which = nullptr) {
+        if (which) {
+            SK_CUDA(cudaMemcpyAsync(I.kdx.ptr, dxo, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
+            SK_CUDA(cudaMemcpyAsync(I.kds.ptr, dso, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
+            SK_CUDA(cudaMemcpyAsync(I.kdy.ptr, dyo, sizeof(double) * M, cudaMemcpyDeviceToDevice, st));
+        }
         spmv(M, I.ga, I.a_rp.ptr, I.a_ci.ptr, I.a_v.ptr, I.v.ptr, EpiSub{I.rp.ptr, I.rkkt.ptr}, st);
-        solve(I.rkkt.ptr, dyo, solved);
+        solve(I.rkkt.ptr, dyo, solved, which);
         spmv(N, I.gt, I.t_rp.ptr, I.t_ci.ptr, I.t_v.ptr, dyo,
              EpiDsDx{I.rd.ptr, I.theta.ptr, rxs, I.x.ptr, I.s.ptr, dso, dxo, I.e2.ptr, I.e3.ptr}, st);
         spmv(M, I.ga, I.a_rp.ptr, I.a_ci.ptr, I.a_v.ptr, dxo, EpiAdd{I.rp.ptr, I.e1.ptr}, st);
         I.reduce_rows<1>(RedSq{I.e1.ptr}, I.redout.ptr);
         I.reduce_cols<9>(RedDir{I.e2.ptr, I.e3.ptr, rxs, I.x.ptr, I.s.ptr, dxo, dso}, I.redout.ptr + nlp);
+        if (which) {
+            std::vector<double> keep(nlp, 0.0);
+            for (int k = 0; k < nlp; ++k) keep[k] = (*which)[k] ? 0.0 : 1.0;
+            I.put_scalars(6, keep);
+            k_masked_copy<<<nblk(N), 256, 0, st>>>(N, I.kdx.ptr, I.col_lp.ptr, I.sc(6), dxo);
+            k_masked_copy<<<nblk(N), 256, 0, st>>>(N, I.kds.ptr, I.col_lp.ptr, I.sc(6), dso);
+            k_masked_copy<<<nblk(M), 256, 0, st>>>(M, I.kdy.ptr, I.row_lp.ptr, I.sc(6), dyo);
+        }
         std::vector<double> h = I.fetch(static_cast<size_t>(nlp) * 10);
+        const DirStats old = ds_;
         ds_ = DirStats();
         for (int k = 0; k < nlp; ++k) {
+            if (which && !(*which)[k] && k < static_cast<int>(old.e1.size())) {
+                ds_.e1.push_back(old.e1[k]); ds_.e2.push_back(old.e2[k]); ds_.e3.push_back(old.e3[k]);
+                ds_.rx.push_back(old.rx[k]); ds_.rs.push_back(old.rs[k]); ds_.xs.push_back(old.xs[k]);
+                ds_.xds.push_back(old.xds[k]); ds_.dxs.push_back(old.dxs[k]); ds_.dxds.push_back(old.dxds[k]);
+                continue;
+            }
             const double* q = h.data() + nlp + k * 9;
             ds_.e1.push_back(std::sqrt(h[k]) / std::max(1.0, nrp[k]));
             ds_.e2.push_back(std::sqrt(q[0]) / std::max(1.0, nrd[k]));
@@ -1083,6 +1111,7 @@ void DeviceIPM::run() {
             ds_.dxs.push_back(q[7]);
             ds_.dxds.push_back(q[8]);
         }
+        const std::vector<char> acc0 = acc, use0 = use;
         acc.assign(nlp, 0);
         use.assign(nlp, 0);
         if (o.verbose > 1)
@@ -1092,6 +1121,11 @@ void DeviceIPM::run() {
                                  k, (int)solved[k], ds_.e1[k], ds_.e2[k], ds_.e3[k], ds_.rx[k], ds_.rs[k], tol[k],
                                  I.sw_now[k] ? "fp64" : "fp32");
         for (int k = 0; k < nlp; ++k) {
+            if (which && !(*which)[k] && k < static_cast<int>(acc0.size()) && k < static_cast<int>(use0.size())) {
+                acc[k] = acc0[k];
+                use[k] = use0[k];
+                continue;
+            }
             const double e = std::max(ds_.e1[k], std::max(ds_.e2[k], ds_.e3[k]));
             const bool fin = std::isfinite(ds_.e1[k]) && std::isfinite(ds_.e2[k]) && std::isfinite(ds_.e3[k]) &&
                              std::isfinite(ds_.rx[k]) && std::isfinite(ds_.rs[k]);
@@ -1325,13 +1359,17 @@ void DeviceIPM::run() {
         // did not reach its tolerance moves at once: PCG from the same start with the
         // same factor repeats the same steps, so a tighter target cannot be met.
         std::vector<char> tightened(nlp, 0);
-        auto retry_fp32_misses = [&](const std::vector<char>& acc, const char* what) -> int {
-            // returns 0: nothing to redo; 1: redo the direction; -1: FP64 factorisation failed
+        auto retry_fp32_misses = [&](const std::vector<char>& acc, const char* what,
+                                     std::vector<char>& again) -> int {
+            // returns 0: nothing to redo; 1: redo the direction of the LPs in `again`;
+            // -1: FP64 factorisation failed
             std::vector<char> now(nlp, 0);
             bool redo = false, any_now = false;
+            again.assign(nlp, 0);
             for (int k = 0; k < nlp; ++k) {
                 if (!I.active[k] || I.sw[k] || acc[k]) continue;
                 redo = true;
+                again[k] = 1;
                 if (!tightened[k] && solved[k]) { tightened[k] = 1; tol[k] *= 0.01; }
                 else { now[k] = 1; any_now = true; }
             }
@@ -1345,12 +1383,14 @@ void DeviceIPM::run() {
             }
             return redo ? 1 : 0;
         };
+        // a repeated direction is solved for the LPs that retry alone
+        std::vector<char> again;
         for (int attempt = 0; attempt < 3; ++attempt) {
             k_rhs<<<nblk(N), 256, 0, st>>>(N, I.x.ptr, I.s.ptr, I.theta.ptr, I.rd.ptr, nullptr, nullptr, nullptr,
                                           I.col_lp.ptr, I.rxs.ptr, I.v.ptr);
-            direction(I.dxa.ptr, I.dya.ptr, I.dsa.ptr, I.rxs.ptr, acc_p, use_p, pd);
+            direction(I.dxa.ptr, I.dya.ptr, I.dsa.ptr, I.rxs.ptr, acc_p, use_p, pd, attempt > 0 ? &again : nullptr);
             if (attempt == 2) break;
-            const int r = retry_fp32_misses(acc_p, "predictor");
+            const int r = retry_fp32_misses(acc_p, "predictor", again);
             if (r < 0) { fac_ok = false; break; }
             if (r == 0) break;
         }
@@ -1377,9 +1417,9 @@ void DeviceIPM::run() {
         for (int attempt = 0; attempt < 3; ++attempt) {
             k_rhs<<<nblk(N), 256, 0, st>>>(N, I.x.ptr, I.s.ptr, I.theta.ptr, I.rd.ptr, I.dxa.ptr, I.dsa.ptr, d_tgt,
                                           I.col_lp.ptr, I.rxs.ptr, I.v.ptr);
-            direction(I.dx.ptr, I.dy.ptr, I.ds.ptr, I.rxs.ptr, acc_c, okc, cd);
+            direction(I.dx.ptr, I.dy.ptr, I.ds.ptr, I.rxs.ptr, acc_c, okc, cd, attempt > 0 ? &again : nullptr);
             if (attempt == 2) break;
-            const int r = retry_fp32_misses(acc_c, "corrector");
+            const int r = retry_fp32_misses(acc_c, "corrector", again);
             if (r < 0) { okc.assign(nlp, 0); break; }
             if (r == 0) break;
         }
