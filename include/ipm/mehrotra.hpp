@@ -27,7 +27,7 @@ struct MehrotraOptions {
     int max_iter = 200;
     int ordering = SK_ORDER_AUTO;
     int verbose = 0;
-    double mu_switch = 1e-6;
+    double mu_switch = 1e-4;
     int ruiz_passes = 10;
     int strict = 0;
     double delta32 = 1e-8;

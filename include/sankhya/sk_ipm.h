@@ -64,7 +64,7 @@ typedef struct sk_options {
     int max_iter;         /* default 200 (src/ipm/mehrotra_device.cu:703) */
     int ordering;         /* SK_ORDER_* (default SK_ORDER_AUTO) */
     int verbose;          /* 0 = silent; >0 prints per-iteration lines on stderr */
-    double mu_switch;     /* mixed precision: switch the factor to FP64 once mu < mu_switch (default 1e-6) */
+    double mu_switch;     /* mixed precision: switch the factor to FP64 once mu < mu_switch (default 1e-4) */
     int ruiz_passes;      /* default 10 (src/ipm/mehrotra_device.cu:293) */
     int strict;           /* 1: a normal-equation solve that misses 1e-9 max(1, ||rp||_2) or a direction
                            * with e1, e2 or e3 > 1e-8 ends the LP with IterationLimit, as the reference

@@ -85,7 +85,7 @@ void sk_options_default(sk_options* opt) {
     opt->max_iter = 200;
     opt->ordering = SK_ORDER_AUTO;
     opt->verbose = 0;
-    opt->mu_switch = 1e-6;
+    opt->mu_switch = 1e-4;
     opt->ruiz_passes = 10;
     opt->strict = 0;
     opt->delta32 = 1e-8;
