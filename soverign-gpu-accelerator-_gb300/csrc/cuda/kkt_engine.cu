@@ -592,21 +592,26 @@ __device__ __forceinline__ uint32_t to_tf32(float x) {
 // BF16 digits, exact FP32 tensor-core sums and an integer epilogue; the result
 // agrees with an FP64 product to about 2^-53 of sum_k |a_k| |b_k|.
 //
-// Digit layout (global and shared alike): per digit plane i, row q, column k at
-// byte i * plane + (q >> 3) * 1024 + (k >> 3) * 128 + (q & 7) * 16 + (k & 7) * 2:
-// the canonical K-major no-swizzle layout of 8-row x 16-byte core matrices, so a
-// block's 128 (or 64) consecutive rows are one contiguous bulk copy.
+// Digit layout (global and shared alike): per digit plane i, K half h = k >> 5, row q
+// and column k at byte i * plane + h * (plane / 2) + (q >> 3) * 512 + ((k & 31) >> 3) * 128
+// + (q & 7) * 16 + (k & 7) * 2: within one half the canonical K-major no-swizzle layout
+// of 8-row x 16-byte core matrices, so a block's 128 (32, 64) consecutive rows of one
+// plane and half are one contiguous 8 KB (2 KB, 4 KB) bulk copy, and a block streams
+// the two K halves through one buffer.
 
 constexpr int kOzDigits = 7;
 constexpr uint32_t kOzLbo = 128;                       // bytes between K-adjacent core matrices
-constexpr uint32_t kOzSbo = 1024;                      // bytes between 8-row groups (64 bf16 per row)
-constexpr size_t kOzA = 128 * 128;                     // one digit plane of 128 rows: 16 KB
-constexpr size_t kOzB = 64 * 128;                      // one digit plane of 64 rows: 8 KB
-constexpr size_t kOzSmem = kOzDigits * (kOzA + kOzB) + 64;
+constexpr uint32_t kOzSbo = 512;                       // bytes between 8-row groups (32 bf16 per row and half)
+constexpr size_t kOzA = 128 * 64;                      // 128 rows of one plane and half: 8 KB
+constexpr size_t kOzBu = 32 * 64;                      // 32 rows (update tiles): 2 KB
+constexpr size_t kOzBt = 64 * 64;                      // 64 rows (Linv rows of the panel solve): 4 KB
+constexpr size_t kOzSmemU = kOzDigits * (kOzA + kOzBu) + 64;   // 70 KB: two blocks per SM
+constexpr size_t kOzSmemT = kOzDigits * (kOzA + kOzBt) + 64;   // 84 KB
 constexpr int kOzSpin = 1 << 22;
-// instruction descriptor (kind::f16): D = F32 (bits 4-5 = 1), A = B = BF16 (bits 7-9, 10-12 = 1),
-// both K-major, N >> 3 at bits 17-22 (N = 64), M >> 4 at bits 24-28 (M = 128)
-constexpr uint32_t kOzIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
+// instruction descriptors (kind::f16): D = F32 (bits 4-5 = 1), A = B = BF16 (bits 7-9, 10-12 = 1),
+// both K-major, N >> 3 at bits 17-22, M >> 4 at bits 24-28 (M = 128; N = 64 or 32)
+constexpr uint32_t kOzIdesc64 = (1u << 4) | (1u << 7) | (1u << 10) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
+constexpr uint32_t kOzIdesc32 = (1u << 4) | (1u << 7) | (1u << 10) | ((32u >> 3) << 17) | ((128u >> 4) << 24);
 
 __device__ __forceinline__ uint64_t oz_sdesc(uint32_t saddr) {
     uint64_t d = static_cast<uint64_t>((saddr & 0x3FFFFu) >> 4);
@@ -622,11 +627,11 @@ __device__ __forceinline__ double oz_pow2(int p) {       // 2^p, 0 below the nor
 __device__ __forceinline__ uint32_t oz_bf16(int d) {     // |d| <= 256: exact
     return __float_as_uint(static_cast<float>(d)) >> 16;
 }
-__device__ __forceinline__ bool oz_wait(uint32_t bar) {
+__device__ __forceinline__ bool oz_wait(uint32_t bar, uint32_t parity = 0) {
     uint32_t done = 0;
     for (int spin = 0; spin < kOzSpin && !done; ++spin) {
-        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n"
-                     " selp.u32 %0, 1, 0, p;\n}\n" : "=r"(done) : "r"(bar) : "memory");
+        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                     " selp.u32 %0, 1, 0, p;\n}\n" : "=r"(done) : "r"(bar), "r"(parity) : "memory");
         // back-to-back polls first: a copy or an MMA batch of one tile completes within
         // microseconds, and a sleep per poll adds its own latency to every tile
         if (!done && spin >= 4096) __nanosleep(32);
@@ -659,13 +664,100 @@ __device__ __forceinline__ void oz_store_digits(const double* v, int E, int q, i
 #pragma unroll
         for (int j = 0; j < kOzDigits; ++j) pk[j][t >> 1] = oz_bf16(d0[j]) | (oz_bf16(d1[j]) << 16);
     }
-    unsigned char* base = dig + static_cast<int64_t>(q >> 3) * 1024 + (q & 7) * 16;
+    unsigned char* base = dig + (cg >> 1) * (plane >> 1) + static_cast<int64_t>(q >> 3) * kOzSbo + (q & 7) * 16;
 #pragma unroll
     for (int j = 0; j < kOzDigits; ++j)
 #pragma unroll
         for (int h = 0; h < 2; ++h)
-            *reinterpret_cast<uint4*>(base + j * plane + (cg * 2 + h) * 128) =
+            *reinterpret_cast<uint4*>(base + j * plane + ((cg & 1) * 2 + h) * kOzLbo) =
                 make_uint4(pk[j][4 * h], pk[j][4 * h + 1], pk[j][4 * h + 2], pk[j][4 * h + 3]);
+}
+
+// Thread 0 of a digit-product block: start the bulk copies of K half h of the 7
+// planes of A (128 rows from row qa of adig) and B (32 rows from row qb of bdig)
+// into As / Bs, completing on the mbarrier at b0.
+__device__ __forceinline__ void oz_copy_half(int h, uint32_t b0, unsigned char* As, unsigned char* Bs,
+                                             const unsigned char* adig, int64_t aplane, int qa,
+                                             const unsigned char* bdig, int64_t bplane, int qb) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                 :: "r"(b0), "r"(static_cast<uint32_t>(kOzDigits * (kOzA + kOzBu))) : "memory");
+    for (int j = 0; j < kOzDigits; ++j) {
+        const unsigned char* ga = adig + j * aplane + h * (aplane >> 1) + static_cast<int64_t>(qa >> 3) * kOzSbo;
+        const unsigned char* gb = bdig + j * bplane + h * (bplane >> 1) + static_cast<int64_t>(qb >> 3) * kOzSbo;
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                     :: "r"(smem_addr(As + j * kOzA)), "l"(ga), "r"(static_cast<uint32_t>(kOzA)), "r"(b0)
+                     : "memory");
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                     :: "r"(smem_addr(Bs + j * kOzBu)), "l"(gb), "r"(static_cast<uint32_t>(kOzBu)), "r"(b0)
+                     : "memory");
+    }
+}
+
+// Thread 0, after oz_copy_half(0, ...): for each K half wait for its planes, issue
+// the 28 digit pairs x 2 K-steps of MMAs (M=128, N=32, K=16; level L into TMEM
+// columns 32L..32L+31), wait for them to finish with the buffer and start the next
+// half's copies. bar[0] counts the copies (phase h), bar[1] the MMA batches. Every
+// wait is bounded; on a time-out it waits once more for what is in flight and
+// returns false.
+__device__ __forceinline__ bool oz_products(uint64_t* bar, uint32_t tmem, unsigned char* As, unsigned char* Bs,
+                                            const unsigned char* adig, int64_t aplane, int qa,
+                                            const unsigned char* bdig, int64_t bplane, int qb) {
+    const uint32_t b0 = smem_addr(bar), b1 = smem_addr(bar + 1);
+    const uint32_t sa = smem_addr(As), sb = smem_addr(Bs);
+    for (int h = 0; h < 2; ++h) {
+        if (!oz_wait(b0, h)) {
+            oz_wait(b0, h);                            // copies still in flight: a second bounded wait
+            return false;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        for (int L = 0; L < kOzDigits; ++L) {
+            for (int da = 0; da <= L; ++da) {
+                const int db = L - da;
+#pragma unroll
+                for (int ks = 0; ks < 2; ++ks) {
+                    const uint32_t acc = (h > 0 || da > 0 || ks > 0) ? 1u : 0u;
+                    const uint64_t adesc = oz_sdesc(sa + da * static_cast<uint32_t>(kOzA) + ks * 2 * kOzLbo);
+                    const uint64_t bdesc = oz_sdesc(sb + db * static_cast<uint32_t>(kOzBu) + ks * 2 * kOzLbo);
+                    asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                                 " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+                                 :: "r"(tmem + static_cast<uint32_t>(32 * L)), "l"(adesc), "l"(bdesc),
+                                    "r"(kOzIdesc32), "r"(acc));
+                }
+            }
+        }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                     :: "r"(b1) : "memory");
+        if (!oz_wait(b1, h)) {
+            oz_wait(b1, h);                            // a second bounded wait before TMEM is freed
+            return false;
+        }
+        if (h == 0) oz_copy_half(1, b0, As, Bs, adig, aplane, qa, bdig, bplane, qb);
+    }
+    return true;
+}
+
+// Row accumulators of 8 TMEM columns (from column c) of the 7 levels for this
+// thread's lane, combined into the integers u with sum = u 2^(Ea+Eb-52):
+// hi 2^(E-30) + lo 2^(E-62) = 2^(E-52) (hi 2^22 + lo 2^-10), one integer below 2^62
+// (lo rounded to 2^(E-53)).
+__device__ __forceinline__ void oz_read8(uint32_t taddr, long long* u) {
+    uint32_t v[kOzDigits][8];
+#pragma unroll
+    for (int L = 0; L < kOzDigits; ++L)
+        asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                     : "=r"(v[L][0]), "=r"(v[L][1]), "=r"(v[L][2]), "=r"(v[L][3]), "=r"(v[L][4]),
+                       "=r"(v[L][5]), "=r"(v[L][6]), "=r"(v[L][7])
+                     : "r"(taddr + static_cast<uint32_t>(32 * L)));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        long long lv[kOzDigits];
+#pragma unroll
+        for (int L = 0; L < kOzDigits; ++L) lv[L] = __float2int_rn(__uint_as_float(v[L][q]));
+        const long long hi = lv[0] * 65536LL + lv[1] * 256LL + lv[2];   // |hi| < 2^39.2
+        const long long lo = lv[3] * 16777216LL + lv[4] * 65536LL + lv[5] * 256LL + lv[6];  // < 2^47.2
+        u[q] = hi * 4194304LL + ((lo + 512) >> 10);
+    }
 }
 
 // Digits of the step's trailing panel rows: one block per 64-row tile (the trsm
@@ -716,72 +808,66 @@ __global__ void __launch_bounds__(256) k_oz_digits(StepArgs a, const int* __rest
     if (cg == 0) dexp[q] = E;
 }
 
-// C(128 x 64) -= A B^T from the digit planes (one block of 256 threads per
-// 128-row x 64-column block of the trailing lower part; row block bi holds
-// column blocks 0..2bi+1). One thread stages the 14 planes with bulk copies and
-// issues the 112 MMAs (M=128, N=64, K=16; level L accumulates in TMEM columns
-// 64L..64L+63); every thread loads its C values meanwhile, then reads its row's
-// 7 accumulators for 32 columns and applies them. Every wait is bounded: on a
-// time-out the block records err[2], waits once more for what it issued, frees
-// its TMEM and leaves C untouched.
-__global__ void __launch_bounds__(256, 1) k_update_oz(StepArgs a, const int* __restrict__ items,
+// C(128 x 32) -= A B^T from the digit planes: two blocks per 128-row x 64-column
+// block of the trailing lower part (row block bi holds column blocks 0..2bi+1), each
+// taking 32 of its columns, so that two blocks fit an SM (70 KB of shared memory, 256
+// TMEM columns, at most 128 registers). Thread 0 streams the two K halves of the 14
+// planes through one buffer with bulk copies and issues 28 digit pairs x 2 K-steps of
+// MMAs (M=128, N=32, K=16) per half; level L accumulates in TMEM columns 32L..32L+31.
+// Every thread loads its 16 C values meanwhile, then reads its row's 7 accumulators
+// and applies them. The diagonal tile of the next step lies in both blocks of the
+// first 128 x 64 block: the one of the two that finishes second (a per-front counter,
+// no waiting) factors it. Every wait is bounded: on a time-out the block records
+// err[2], waits once more for what it issued, frees its TMEM and leaves C untouched.
+__global__ void __launch_bounds__(256, 2) k_update_oz(StepArgs a, const int* __restrict__ items,
                                                       const int* __restrict__ prefix, PlanDev pd, double* F,
                                                       double* __restrict__ Linv, const int64_t* __restrict__ inv_off,
                                                       const unsigned char* __restrict__ dig,
-                                                      const int* __restrict__ dexp, int64_t plane, int* err) {
+                                                      const int* __restrict__ dexp, int64_t plane, int* cnt,
+                                                      int* err) {
     extern __shared__ __align__(1024) unsigned char smraw[];
     unsigned char* As = smraw;
     unsigned char* Bs = smraw + kOzDigits * kOzA;
-    uint64_t* bar = reinterpret_cast<uint64_t*>(Bs + kOzDigits * kOzB);   // [0] planes loaded, [1] MMAs done
+    uint64_t* bar = reinterpret_cast<uint64_t*>(Bs + kOzDigits * kOzBu);   // [0] planes loaded, [1] MMAs done
     uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 2);
     int* fail = reinterpret_cast<int*>(bar + 3);
-    const int i = find_item(prefix + a.up3_off, a.nitems, blockIdx.x);
+    int* last = fail + 1;
+    const int unit = blockIdx.x >> 1, hc = blockIdx.x & 1;
+    const int i = find_item(prefix + a.up3_off, a.nitems, unit);
     const int s = items[a.item_off + i];
     if (!pd.lp_on[pd.sn_lp[s]]) return;
-    const int lb = blockIdx.x - prefix[a.up3_off + i];
-    int bi = block_row_of(lb);
+    const int lb = unit - prefix[a.up3_off + i];
+    const int bi = block_row_of(lb);
     const int bj = lb - bi * (bi + 1);
     const int N = pd.sn_nrows[s], K = pd.sn_ncols[s], LD = pd.sn_lda[s];
     const int k0 = a.k * T64;
     const int w = min(T64, K - k0);
     const int t0 = k0 + w;
-    const int r0 = t0 + bi * 128, c0 = t0 + bj * T64;
-    if (c0 >= N) return;                              // the whole block: column block past the front
-    const int nra = min(128, N - r0), ncb = min(T64, N - c0);
-    const int qa = prefix[a.dr_off + i] + bi * 128, qb = prefix[a.dr_off + i] + bj * T64;
+    const int r0 = t0 + bi * 128, c0 = t0 + bj * T64 + hc * 32;
+    if (c0 >= N) return;                              // the whole block: columns past the front
+    const int nra = min(128, N - r0), ncb = min(32, N - c0);
+    const int qa = prefix[a.dr_off + i] + bi * 128, qb = prefix[a.dr_off + i] + bj * T64 + hc * 32;
     double* Fs = F + pd.F_off[s];
     const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
-    // thread 0 starts the copies first; TMEM allocation and every thread's C loads
-    // then overlap them
+    // thread 0 starts the first half's copies; TMEM allocation and every thread's C
+    // loads then overlap them
     if (tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_addr(bar)));
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_addr(bar + 1)));
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         *fail = 0;
-        const uint32_t b0 = smem_addr(bar);
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
-                     :: "r"(b0), "r"(static_cast<uint32_t>(kOzDigits * (kOzA + kOzB))) : "memory");
-        for (int j = 0; j < kOzDigits; ++j) {
-            const unsigned char* ga = dig + j * plane + static_cast<int64_t>(qa >> 3) * 1024;
-            const unsigned char* gb = dig + j * plane + static_cast<int64_t>(qb >> 3) * 1024;
-            asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                         :: "r"(smem_addr(As + j * kOzA)), "l"(ga), "r"(static_cast<uint32_t>(kOzA)), "r"(b0)
-                         : "memory");
-            asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                         :: "r"(smem_addr(Bs + j * kOzB)), "l"(gb), "r"(static_cast<uint32_t>(kOzB)), "r"(b0)
-                         : "memory");
-        }
+        oz_copy_half(0, smem_addr(bar), As, Bs, dig, plane, qa, dig, plane, qb);
     }
     if (wid == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" :: "r"(smem_addr(tslot)));
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" :: "r"(smem_addr(tslot)));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
-    // this thread's row (TMEM lane) and 32 columns, and its C values
-    const int row = 32 * (wid & 3) + lane, ch = 32 * (wid >> 2);
+    // this thread's row (TMEM lane) and 16 columns, and its C values
+    const int row = 32 * (wid & 3) + lane, ch = 16 * (wid >> 2);
     const bool rok = row < nra;
-    double cv[32];
+    double cv[16];
 #pragma unroll
-    for (int j = 0; j < 32; ++j) {
+    for (int j = 0; j < 16; ++j) {
         const int col = ch + j;
         const bool in = rok && col < ncb && r0 + row >= c0 + col;
         cv[j] = in ? Fs[(r0 + row) + static_cast<int64_t>(c0 + col) * LD] : 0.0;
@@ -791,87 +877,52 @@ __global__ void __launch_bounds__(256, 1) k_update_oz(StepArgs a, const int* __r
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tslot;
-    if (tid == 0) {
-        const uint32_t b0 = smem_addr(bar);
-        bool ok = oz_wait(b0);
-        if (ok) {
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t sa = smem_addr(As), sb = smem_addr(Bs);
-            for (int L = 0; L < kOzDigits; ++L) {
-                uint32_t acc = 0;
-                for (int da = (L > kOzDigits - 1 ? L - kOzDigits + 1 : 0); da <= L && da < kOzDigits; ++da) {
-                    const int db = L - da;
-                    for (int ks = 0; ks < T64 / 16; ++ks) {
-                        const uint64_t adesc = oz_sdesc(sa + da * static_cast<uint32_t>(kOzA) + ks * 2 * kOzLbo);
-                        const uint64_t bdesc = oz_sdesc(sb + db * static_cast<uint32_t>(kOzB) + ks * 2 * kOzLbo);
-                        asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-                                     " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
-                                     :: "r"(tmem + static_cast<uint32_t>(64 * L)), "l"(adesc), "l"(bdesc),
-                                        "r"(kOzIdesc), "r"(acc));
-                        acc = 1;
-                    }
-                }
-            }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
-                         :: "r"(smem_addr(bar + 1)) : "memory");
-            ok = oz_wait(smem_addr(bar + 1));
-            if (!ok) oz_wait(smem_addr(bar + 1));     // a second bounded wait before TMEM is freed
-        } else {
-            oz_wait(b0);                               // copies still in flight: a second bounded wait
-        }
-        if (!ok) {
-            *fail = 1;
-            atomicExch(err + 2, 1);
-        }
+    if (tid == 0 && !oz_products(bar, tmem, As, Bs, dig, plane, qa, dig, plane, qb)) {
+        *fail = 1;
+        atomicExch(err + 2, 1);
     }
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const bool ok = *fail == 0;
     if (ok) {
 #pragma unroll
-        for (int c16 = 0; c16 < 2; ++c16) {
-            uint32_t v[kOzDigits][16];
+        for (int c8 = 0; c8 < 2; ++c8) {
+            long long u[8];
+            oz_read8(tmem + (static_cast<uint32_t>(32 * (wid & 3)) << 16) + static_cast<uint32_t>(ch + 8 * c8), u);
 #pragma unroll
-            for (int L = 0; L < kOzDigits; ++L) {
-                const uint32_t taddr = tmem + (static_cast<uint32_t>(32 * (wid & 3)) << 16) +
-                                       static_cast<uint32_t>(64 * L + ch + 16 * c16);
-                asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-                             : "=r"(v[L][0]), "=r"(v[L][1]), "=r"(v[L][2]), "=r"(v[L][3]), "=r"(v[L][4]),
-                               "=r"(v[L][5]), "=r"(v[L][6]), "=r"(v[L][7]), "=r"(v[L][8]), "=r"(v[L][9]),
-                               "=r"(v[L][10]), "=r"(v[L][11]), "=r"(v[L][12]), "=r"(v[L][13]), "=r"(v[L][14]),
-                               "=r"(v[L][15])
-                             : "r"(taddr));
-            }
-            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-            for (int q = 0; q < 16; ++q) {
-                const int j = 16 * c16 + q, col = ch + j;
-                if (!(rok && col < ncb && r0 + row >= c0 + col)) continue;
-                long long lv[kOzDigits];
-#pragma unroll
-                for (int L = 0; L < kOzDigits; ++L) lv[L] = __float2int_rn(__uint_as_float(v[L][q]));
-                const long long hi = lv[0] * 65536LL + lv[1] * 256LL + lv[2];   // |hi| < 2^39.2
-                const long long lo = lv[3] * 16777216LL + lv[4] * 65536LL + lv[5] * 256LL + lv[6];  // < 2^47.2
-                // hi 2^(E-30) + lo 2^(E-62) = 2^(E-52) (hi 2^22 + lo 2^-10): one integer below 2^62
-                // (lo rounded to 2^(E-53)), one conversion and one FP64 FMA on the slow FP64 pipe
-                const long long u = hi * 4194304LL + ((lo + 512) >> 10);
-                const int eb = dexp[qb + col];
-                Fs[(r0 + row) + static_cast<int64_t>(c0 + col) * LD] =
-                    fma(-static_cast<double>(u), oz_pow2(ea + eb - 52), cv[j]);
+            for (int q = 0; q < 8; ++q) {
+                const int j = 8 * c8 + q, col = ch + j;
+                // one conversion and one FP64 FMA on the slow FP64 pipe per entry
+                if (rok && col < ncb && r0 + row >= c0 + col)
+                    Fs[(r0 + row) + static_cast<int64_t>(c0 + col) * LD] =
+                        fma(-static_cast<double>(u[q]), oz_pow2(ea + dexp[qb + col] - 52), cv[j]);
             }
         }
     }
+    __threadfence();                                   // this block's C writes, before the counter below
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (wid == 0) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" :: "r"(tmem));
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" :: "r"(tmem));
     }
     if (!ok) return;
-    // the block holding the first trailing diagonal tile factors it (as in k_update)
+    // the next diagonal tile spans both blocks of the first 128 x 64 block: the second
+    // of the two to get here factors it (when the front ends within the first 32
+    // columns the first block is alone) and resets the counter for the next step
     if (lb == 0 && t0 < K) {
+        if (tid == 0) {
+            if (t0 + 32 >= N) {
+                *last = 1;
+            } else {
+                const int prev = atomicAdd(cnt + s, 1);
+                *last = prev == 1;
+                if (prev == 1) atomicExch(cnt + s, 0);
+                __threadfence();
+            }
+        }
         __syncthreads();
-        potrf_tile<double>(s, a.k + 1, pd, F, Linv, inv_off, err, smraw);
+        if (*last) potrf_tile<double>(s, a.k + 1, pd, F, Linv, inv_off, err, smraw);
     }
 }
 
@@ -909,7 +960,7 @@ __global__ void __launch_bounds__(256) k_oz_linv_digits(StepArgs a, const int* _
     if (cg == 0) dexp[q] = E;
 }
 
-__global__ void __launch_bounds__(256, 1) k_trsm_oz(StepArgs a, const int* __restrict__ items,
+__global__ void __launch_bounds__(256, 2) k_trsm_oz(StepArgs a, const int* __restrict__ items,
                                                     const int* __restrict__ prefix, PlanDev pd, double* F,
                                                     const unsigned char* __restrict__ dig,
                                                     const int* __restrict__ dexp, int64_t plane,
@@ -918,115 +969,58 @@ __global__ void __launch_bounds__(256, 1) k_trsm_oz(StepArgs a, const int* __res
     extern __shared__ __align__(1024) unsigned char smraw[];
     unsigned char* As = smraw;
     unsigned char* Bs = smraw + kOzDigits * kOzA;
-    uint64_t* bar = reinterpret_cast<uint64_t*>(Bs + kOzDigits * kOzB);   // [0] planes loaded, [1] MMAs done
+    uint64_t* bar = reinterpret_cast<uint64_t*>(Bs + kOzDigits * kOzBu);   // [0] planes loaded, [1] MMAs done
     uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 2);
     int* fail = reinterpret_cast<int*>(bar + 3);
-    const int i = find_item(prefix + a.dr_off, a.nitems, blockIdx.x * 128);
+    const int unit = blockIdx.x >> 1, hc = blockIdx.x & 1;   // 128 panel rows, 32 of the 64 columns
+    const int i = find_item(prefix + a.dr_off, a.nitems, unit * 128);
     const int s = items[a.item_off + i];
     if (!pd.lp_on[pd.sn_lp[s]]) return;
-    const int blk = blockIdx.x - prefix[a.dr_off + i] / 128;
+    const int blk = unit - prefix[a.dr_off + i] / 128;
     const int N = pd.sn_nrows[s], K = pd.sn_ncols[s], LD = pd.sn_lda[s];
     const int k0 = a.k * T64;
     const int w = min(T64, K - k0);
     const int r0 = k0 + w + blk * 128;
-    if (r0 >= N) return;                              // a padded block of the digit rows
+    if (r0 >= N || hc * 32 >= w) return;              // a padded block of the digit rows, or no columns
     const int nra = min(128, N - r0);
-    const int qa = prefix[a.dr_off + i] + blk * 128, qb = i * T64;
+    const int qa = prefix[a.dr_off + i] + blk * 128, qb = i * T64 + hc * 32;
     double* Fs = F + pd.F_off[s];
     const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
-    if (tid == 0) {
+    if (tid == 0) {                                    // the copies first, then TMEM allocation
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_addr(bar)));
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_addr(bar + 1)));
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         *fail = 0;
+        oz_copy_half(0, smem_addr(bar), As, Bs, dig, plane, qa, ldig, lplane, qb);
     }
     if (wid == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" :: "r"(smem_addr(tslot)));
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" :: "r"(smem_addr(tslot)));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tslot;
-    if (tid == 0) {
-        const uint32_t b0 = smem_addr(bar);
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
-                     :: "r"(b0), "r"(static_cast<uint32_t>(kOzDigits * (kOzA + kOzB))) : "memory");
-        for (int j = 0; j < kOzDigits; ++j) {
-            const unsigned char* ga = dig + j * plane + static_cast<int64_t>(qa >> 3) * 1024;
-            const unsigned char* gb = ldig + j * lplane + static_cast<int64_t>(qb >> 3) * 1024;
-            asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                         :: "r"(smem_addr(As + j * kOzA)), "l"(ga), "r"(static_cast<uint32_t>(kOzA)), "r"(b0)
-                         : "memory");
-            asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                         :: "r"(smem_addr(Bs + j * kOzB)), "l"(gb), "r"(static_cast<uint32_t>(kOzB)), "r"(b0)
-                         : "memory");
-        }
-        bool ok = oz_wait(b0);
-        if (ok) {
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t sa = smem_addr(As), sb = smem_addr(Bs);
-            for (int L = 0; L < kOzDigits; ++L) {
-                uint32_t acc = 0;
-                for (int da = 0; da <= L; ++da) {
-                    const int db = L - da;
-                    for (int ks = 0; ks < T64 / 16; ++ks) {
-                        const uint64_t adesc = oz_sdesc(sa + da * static_cast<uint32_t>(kOzA) + ks * 2 * kOzLbo);
-                        const uint64_t bdesc = oz_sdesc(sb + db * static_cast<uint32_t>(kOzB) + ks * 2 * kOzLbo);
-                        asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-                                     " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
-                                     :: "r"(tmem + static_cast<uint32_t>(64 * L)), "l"(adesc), "l"(bdesc),
-                                        "r"(kOzIdesc), "r"(acc));
-                        acc = 1;
-                    }
-                }
-            }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
-                         :: "r"(smem_addr(bar + 1)) : "memory");
-            ok = oz_wait(smem_addr(bar + 1));
-            if (!ok) oz_wait(smem_addr(bar + 1));     // a second bounded wait before TMEM is freed
-        } else {
-            oz_wait(b0);                               // copies still in flight: a second bounded wait
-        }
-        if (!ok) {
-            *fail = 1;
-            atomicExch(err + 2, 1);
-        }
+    if (tid == 0 && !oz_products(bar, tmem, As, Bs, dig, plane, qa, ldig, lplane, qb)) {
+        *fail = 1;
+        atomicExch(err + 2, 1);
     }
-    const int row = 32 * (wid & 3) + lane, ch = 32 * (wid >> 2);
+    const int row = 32 * (wid & 3) + lane, ch = 16 * (wid >> 2);
     const bool rok = row < nra;
     const int ea = rok ? dexp[qa + row] : 0;
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    const bool ok = *fail == 0;
-    if (ok) {
+    if (*fail == 0) {
 #pragma unroll
-        for (int c16 = 0; c16 < 2; ++c16) {
-            uint32_t v[kOzDigits][16];
+        for (int c8 = 0; c8 < 2; ++c8) {
+            long long u[8];
+            oz_read8(tmem + (static_cast<uint32_t>(32 * (wid & 3)) << 16) + static_cast<uint32_t>(ch + 8 * c8), u);
 #pragma unroll
-            for (int L = 0; L < kOzDigits; ++L) {
-                const uint32_t taddr = tmem + (static_cast<uint32_t>(32 * (wid & 3)) << 16) +
-                                       static_cast<uint32_t>(64 * L + ch + 16 * c16);
-                asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-                             : "=r"(v[L][0]), "=r"(v[L][1]), "=r"(v[L][2]), "=r"(v[L][3]), "=r"(v[L][4]),
-                               "=r"(v[L][5]), "=r"(v[L][6]), "=r"(v[L][7]), "=r"(v[L][8]), "=r"(v[L][9]),
-                               "=r"(v[L][10]), "=r"(v[L][11]), "=r"(v[L][12]), "=r"(v[L][13]), "=r"(v[L][14]),
-                               "=r"(v[L][15])
-                             : "r"(taddr));
-            }
-            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-            for (int q = 0; q < 16; ++q) {
-                const int col = ch + 16 * c16 + q;
-                if (!(rok && col < w)) continue;
-                long long lv[kOzDigits];
-#pragma unroll
-                for (int L = 0; L < kOzDigits; ++L) lv[L] = __float2int_rn(__uint_as_float(v[L][q]));
-                const long long hi = lv[0] * 65536LL + lv[1] * 256LL + lv[2];
-                const long long lo = lv[3] * 16777216LL + lv[4] * 65536LL + lv[5] * 256LL + lv[6];
-                const long long u = hi * 4194304LL + ((lo + 512) >> 10);
-                Fs[(r0 + row) + static_cast<int64_t>(k0 + col) * LD] =
-                    static_cast<double>(u) * oz_pow2(ea + lexp[qb + col] - 52);
+            for (int q = 0; q < 8; ++q) {
+                const int col = hc * 32 + ch + 8 * c8 + q;
+                if (rok && col < w)
+                    Fs[(r0 + row) + static_cast<int64_t>(k0 + col) * LD] =
+                        static_cast<double>(u[q]) * oz_pow2(ea + lexp[i * T64 + col] - 52);
             }
         }
     }
@@ -1034,7 +1028,7 @@ __global__ void __launch_bounds__(256, 1) k_trsm_oz(StepArgs a, const int* __res
     __syncthreads();
     if (wid == 0) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" :: "r"(tmem));
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" :: "r"(tmem));
     }
 }
 
@@ -1660,10 +1654,10 @@ static void set_smem_attrs() {
                                  static_cast<int>(potrf_smem(sizeof(T)))));
     if (std::is_same<T, double>::value)
         SK_CUDA(cudaFuncSetAttribute(k_update_oz, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     static_cast<int>(kOzSmem)));
+                                     static_cast<int>(kOzSmemU)));
     if (std::is_same<T, double>::value)
         SK_CUDA(cudaFuncSetAttribute(k_trsm_oz, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     static_cast<int>(kOzSmem)));
+                                     static_cast<int>(kOzSmemU)));
 }
 
 KktEngine::KktEngine(const ipm::FrontPlan& plan, const DeviceLP& lp, cudaStream_t stream)
@@ -1794,6 +1788,7 @@ KktEngine::KktEngine(const ipm::FrontPlan& plan, const DeviceLP& lp, cudaStream_
     reserve(arena_, tn_, static_cast<size_t>(std::max(1, p.N)));
     reserve(arena_, params_, 4);
     reserve(arena_, err_, 4);
+    reserve(arena_, oz_cnt_, std::max<size_t>(1, p.sn_ncols.size()));
     reserve(arena_, lp_fail_, std::max<size_t>(1, static_cast<size_t>(p.nlp)));
     for (auto& sb : sub_) {
         reserve(arena_, sb.d_items, std::max<size_t>(1, p.step_items.size()));
@@ -1806,7 +1801,7 @@ KktEngine::KktEngine(const ipm::FrontPlan& plan, const DeviceLP& lp, cudaStream_
     bnd(step_prefix_); bnd(round_items_); bnd(round_prefix_); bnd(level_sn_); bnd(slot_pos_); bnd(w_ptr_);
     bnd(slot_i_); bnd(slot_j_); bnd(w_col_); bnd(w_val_); bnd(inv_off_); bnd(blk_off_); bnd(fwd_tasks_);
     bnd(bwd_tasks_); bnd(g_dst_); bnd(g_zp_); bnd(g_ptr_); bnd(g_src_); bnd(sn_lp_); bnd(on32_); bnd(on64_); bnd(q_lp_); bnd(zc_sn_); bnd(zc_len_); bnd(zc_off_); bnd(flags_); bnd(counters_); bnd(solve_err_); bnd(D_); bnd(Mdiag_);
-    bnd(zp_); bnd(xp_); bnd(zsol_); bnd(fvec_); bnd(tn_); bnd(params_); bnd(err_); bnd(lp_fail_);
+    bnd(zp_); bnd(xp_); bnd(zsol_); bnd(fvec_); bnd(tn_); bnd(params_); bnd(err_); bnd(lp_fail_); bnd(oz_cnt_);
     for (auto& sb : sub_) { bnd(sb.d_items); bnd(sb.d_prefix); }
     upload(sn_first_, p.sn_first, st_); upload(sn_ncols_, p.sn_ncols, st_); upload(sn_nrows_, p.sn_nrows, st_);
     upload(sn_lda_, p.sn_lda, st_);
@@ -1864,6 +1859,8 @@ void KktEngine::launch_factor(T* F, T* Linv, Prof* prof, const SubSteps* sub) {
         k_zero_fronts<T><<<static_cast<int>(nzc_), 256, 0, st_>>>(zc_sn_.ptr, zc_len_.ptr, zc_off_.ptr, pdv, F);
     SK_CUDA(cudaMemsetAsync(err_.ptr, 0, 4 * sizeof(int), st_));
     SK_CUDA(cudaMemsetAsync(lp_fail_.ptr, 0, lp_fail_.count * sizeof(int), st_));
+    if (emulate64_ && std::is_same<T, double>::value)   // blocks of the first update tile that have finished
+        SK_CUDA(cudaMemsetAsync(oz_cnt_.ptr, 0, oz_cnt_.count * sizeof(int), st_));
     const double* theta = theta_bound_;
     run(0, [&] {
         if (p.dense_mode) {
@@ -1905,7 +1902,7 @@ void KktEngine::launch_factor(T* F, T* Linv, Prof* prof, const SubSteps* sub) {
                                 a, items, prefix, pdv, F, dig_.ptr, dexp_.ptr, plane);
                             k_oz_linv_digits<<<st.nitems, 256, 0, st_>>>(a, items, pdv, Linv, inv_off_.ptr,
                                                                          ldig_.ptr, lexp_.ptr, lplane);
-                            k_trsm_oz<<<static_cast<int>(st.digit_rows / 128), 256, kOzSmem, st_>>>(
+                            k_trsm_oz<<<static_cast<int>(st.digit_rows / 128) * 2, 256, kOzSmemU, st_>>>(
                                 a, items, prefix, pdv, F, dig_.ptr, dexp_.ptr, plane, ldig_.ptr,
                                 lexp_.ptr, lplane, err_.ptr);
                         }
@@ -1933,9 +1930,9 @@ void KktEngine::launch_factor(T* F, T* Linv, Prof* prof, const SubSteps* sub) {
                             const int64_t plane = plan_.max_digit_rows * 128;
                             k_oz_digits<<<static_cast<int>(st.trsm_tiles), 256, 0, st_>>>(
                                 a, items, prefix, pdv, F, dig_.ptr, dexp_.ptr, plane);
-                            k_update_oz<<<static_cast<int>(st.upd3_blocks), 256, kOzSmem, st_>>>(
+                            k_update_oz<<<static_cast<int>(st.upd3_blocks) * 2, 256, kOzSmemU, st_>>>(
                                 a, items, prefix, pdv, F, Linv, inv_off_.ptr, dig_.ptr,
-                                dexp_.ptr, plane, err_.ptr);
+                                dexp_.ptr, plane, oz_cnt_.ptr, err_.ptr);
                         }
                     }
                     if (!tc)

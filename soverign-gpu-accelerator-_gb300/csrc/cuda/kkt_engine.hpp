@@ -152,6 +152,7 @@ private:
     // numeric work
     Slot<double> D_, Mdiag_, zp_, xp_, zsol_, fvec_, tn_, params_;
     Slot<int> err_;
+    Slot<int> oz_cnt_;                          // per front: blocks of the first update tile done (fused potrf)
     bool fp32_ = false;
     int failed_sn_ = -1;
     std::vector<int> failed_lps_;
