@@ -1738,11 +1738,7 @@ KktEngine::KktEngine(const ipm::FrontPlan& plan, const DeviceLP& lp, cudaStream_
     }
     gather_off_[p.nlevels] = static_cast<int>(g_dst.size());
     // LP of each front (from the batch row of its first column) and the all-on LP mask
-    std::vector<int> sn_lp(static_cast<size_t>(p.ns), 0);
-    for (int s = 0; s < p.ns; ++s) {
-        const Index r = p.perm[p.sn_first[s]];
-        sn_lp[s] = static_cast<int>(std::upper_bound(p.row_off.begin(), p.row_off.end(), r) - p.row_off.begin()) - 1;
-    }
+    const std::vector<int> sn_lp = ipm::supernode_lps(p);
     sn_lp_h_ = sn_lp;
     on32_h_.assign(static_cast<size_t>(std::max(1, p.nlp)), 1);
     on64_h_ = on32_h_;
@@ -1877,8 +1873,8 @@ void KktEngine::launch_factor(T* F, T* Linv, Prof* prof, const SubSteps* sub) {
                 Mdiag_.ptr, D_.ptr, params_.ptr, q_lp_.ptr, pdv.lp_on, F);
         }
     });
-    const std::vector<ipm::PlanStep>& steps = sub ? sub->steps : p.steps;
-    const std::vector<int>& level_ptr = sub ? sub->level_ptr : p.step_level_ptr;
+    const std::vector<ipm::PlanStep>& steps = sub ? sub->rs.steps : p.steps;
+    const std::vector<int>& level_ptr = sub ? sub->rs.level_ptr : p.step_level_ptr;
     const int* items = sub ? sub->d_items.ptr : step_items_.ptr;
     const int* prefix = sub ? sub->d_prefix.ptr : step_prefix_.ptr;
     for (int l = 0; l < p.nlevels; ++l) {
@@ -1941,7 +1937,7 @@ void KktEngine::launch_factor(T* F, T* Linv, Prof* prof, const SubSteps* sub) {
                 });
                 if (prof) {
                     for (int it = 0; it < st.nitems; ++it) {
-                        const int s2 = (sub ? sub->items : p.step_items)[st.item_off + it];
+                        const int s2 = (sub ? sub->rs.items : p.step_items)[st.item_off + it];
                         const double w = std::min<int64_t>(T64, p.sn_ncols[s2] - static_cast<int64_t>(st.k) * T64);
                         const double t = p.sn_nrows[s2] - static_cast<double>(st.k) * T64 - w;
                         prof->upd_flops += 2.0 * w * t * (t + 1.0) / 2.0;
@@ -2050,53 +2046,14 @@ const KktEngine::SubSteps* KktEngine::pick_steps(bool fp32) {
         if (mask[k]) on_work += lp_work_[k];
     if (on_work >= 0.75 * total_work_) return nullptr;
     SubSteps& sb = sub_[fp32 ? 0 : 1];
-    if (sb.mask == mask && !sb.level_ptr.empty()) return &sb;
-    const auto& p = plan_;
+    if (sb.mask == mask && !sb.rs.level_ptr.empty()) return &sb;
     sb.mask = mask;
-    sb.steps.clear();
-    sb.items.clear();
-    sb.prefix.clear();
-    sb.level_ptr.assign(static_cast<size_t>(p.nlevels) + 1, 0);
-    std::vector<int> keep;
-    for (int l = 0; l < p.nlevels; ++l) {
-        for (int q = p.step_level_ptr[l]; q < p.step_level_ptr[l + 1]; ++q) {
-            const ipm::PlanStep& st = p.steps[q];
-            keep.clear();
-            for (int i = 0; i < st.nitems; ++i) {
-                const int lp = sn_lp_h_[p.step_items[st.item_off + i]];
-                if (lp < static_cast<int>(mask.size()) && mask[lp]) keep.push_back(i);
-            }
-            if (keep.empty()) continue;
-            ipm::PlanStep c = st;
-            c.item_off = static_cast<int>(sb.items.size());
-            c.nitems = static_cast<int>(keep.size());
-            for (int i : keep) sb.items.push_back(p.step_items[st.item_off + i]);
-            // the kept items' counts, summed again from 0
-            auto remap = [&](int off, int64_t& total) {
-                const int at = static_cast<int>(sb.prefix.size());
-                int64_t acc = 0;
-                sb.prefix.push_back(0);
-                for (int i : keep) {
-                    acc += p.step_prefix[off + i + 1] - p.step_prefix[off + i];
-                    sb.prefix.push_back(static_cast<int>(acc));
-                }
-                total = acc;
-                return at;
-            };
-            c.trsm_prefix_off = remap(st.trsm_prefix_off, c.trsm_tiles);
-            c.upd_prefix_off = remap(st.upd_prefix_off, c.upd_tiles);
-            c.upd2_prefix_off = remap(st.upd2_prefix_off, c.upd2_blocks);
-            c.upd3_prefix_off = remap(st.upd3_prefix_off, c.upd3_blocks);
-            c.digit_row_off = remap(st.digit_row_off, c.digit_rows);
-            sb.steps.push_back(c);
-        }
-        sb.level_ptr[l + 1] = static_cast<int>(sb.steps.size());
-    }
-    if (!sb.items.empty())
-        SK_CUDA(cudaMemcpyAsync(sb.d_items.ptr, sb.items.data(), sizeof(int) * sb.items.size(),
+    ipm::restrict_steps(plan_, sn_lp_h_, mask, sb.rs);
+    if (!sb.rs.items.empty())
+        SK_CUDA(cudaMemcpyAsync(sb.d_items.ptr, sb.rs.items.data(), sizeof(int) * sb.rs.items.size(),
                                 cudaMemcpyHostToDevice, st_));
-    if (!sb.prefix.empty())
-        SK_CUDA(cudaMemcpyAsync(sb.d_prefix.ptr, sb.prefix.data(), sizeof(int) * sb.prefix.size(),
+    if (!sb.rs.prefix.empty())
+        SK_CUDA(cudaMemcpyAsync(sb.d_prefix.ptr, sb.rs.prefix.data(), sizeof(int) * sb.rs.prefix.size(),
                                 cudaMemcpyHostToDevice, st_));
     return &sb;
 }

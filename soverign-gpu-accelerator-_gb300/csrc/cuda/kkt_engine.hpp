@@ -95,16 +95,14 @@ private:
     void run_factor_levels(bool fp32);
     void run_solve_levels();
     struct Prof;
-    // The plan's tile steps restricted to the fronts of the LPs of one mask: the
-    // items of each step whose LP is on and their prefix arrays, rebuilt when the
-    // mask changes, so that a factorisation of a few LPs of a large batch launches
-    // only their blocks (each launch of the full plan has one block per tile of
-    // every front, and those of LPs that are off still take an SM slot each).
+    // The plan's tile steps restricted to the fronts of the LPs of one mask
+    // (ipm::restrict_steps), rebuilt when the mask changes, so that a factorisation
+    // of a few LPs of a large batch launches only their blocks (each launch of the
+    // full plan has one block per tile of every front, and those of LPs that are
+    // off still take an SM slot each).
     struct SubSteps {
         std::vector<int> mask;                  // the mask the lists were built for
-        std::vector<ipm::PlanStep> steps;
-        std::vector<int> level_ptr;             // nlevels + 1 into steps
-        std::vector<int> items, prefix;
+        ipm::RestrictedSteps rs;
         Slot<int> d_items, d_prefix;
     };
     SubSteps sub_[2];                           // FP32 passes, FP64 passes

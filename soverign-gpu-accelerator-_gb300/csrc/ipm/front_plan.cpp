@@ -686,5 +686,56 @@ void build_front_plan(const std::vector<LpView>& lps, const core::CSRMatrix& A, 
     p.w_ptr.swap(cnt);
 }
 
+std::vector<int> supernode_lps(const FrontPlan& p) {
+    std::vector<int> sn_lp(static_cast<size_t>(p.ns), 0);
+    for (int s = 0; s < p.ns; ++s) {
+        const Index r = p.perm[p.sn_first[s]];
+        sn_lp[s] = static_cast<int>(std::upper_bound(p.row_off.begin(), p.row_off.end(), r) - p.row_off.begin()) - 1;
+    }
+    return sn_lp;
+}
+
+void restrict_steps(const FrontPlan& p, const std::vector<int>& sn_lp, const std::vector<int>& on,
+                    RestrictedSteps& out) {
+    out.steps.clear();
+    out.items.clear();
+    out.prefix.clear();
+    out.level_ptr.assign(static_cast<size_t>(p.nlevels) + 1, 0);
+    std::vector<int> keep;
+    for (int l = 0; l < p.nlevels; ++l) {
+        for (int q = p.step_level_ptr[l]; q < p.step_level_ptr[l + 1]; ++q) {
+            const PlanStep& st = p.steps[q];
+            keep.clear();
+            for (int i = 0; i < st.nitems; ++i) {
+                const int lp = sn_lp[p.step_items[st.item_off + i]];
+                if (lp >= 0 && lp < static_cast<int>(on.size()) && on[lp]) keep.push_back(i);
+            }
+            if (keep.empty()) continue;
+            PlanStep c = st;
+            c.item_off = static_cast<int>(out.items.size());
+            c.nitems = static_cast<int>(keep.size());
+            for (int i : keep) out.items.push_back(p.step_items[st.item_off + i]);
+            auto remap = [&](int off, int64_t& total) {
+                const int at = static_cast<int>(out.prefix.size());
+                int64_t acc = 0;
+                out.prefix.push_back(0);
+                for (int i : keep) {
+                    acc += p.step_prefix[off + i + 1] - p.step_prefix[off + i];
+                    out.prefix.push_back(static_cast<int>(acc));
+                }
+                total = acc;
+                return at;
+            };
+            c.trsm_prefix_off = remap(st.trsm_prefix_off, c.trsm_tiles);
+            c.upd_prefix_off = remap(st.upd_prefix_off, c.upd_tiles);
+            c.upd2_prefix_off = remap(st.upd2_prefix_off, c.upd2_blocks);
+            c.upd3_prefix_off = remap(st.upd3_prefix_off, c.upd3_blocks);
+            c.digit_row_off = remap(st.digit_row_off, c.digit_rows);
+            out.steps.push_back(c);
+        }
+        out.level_ptr[l + 1] = static_cast<int>(out.steps.size());
+    }
+}
+
 }  // namespace ipm
 }  // namespace sankhya

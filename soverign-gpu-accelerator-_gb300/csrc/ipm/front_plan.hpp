@@ -122,5 +122,22 @@ void build_front_plan(const std::vector<LpView>& lps, const core::CSRMatrix& A_c
 // True when A A^T of this LP should be handled as one dense front.
 bool prefer_dense_front(const LpView& lp);
 
+// LP of each supernode (fronts never span LPs): the LP that owns its first row.
+std::vector<int> supernode_lps(const FrontPlan& plan);
+
+// The plan's tile steps restricted to the fronts of the LPs with on[lp] != 0 (a
+// factorisation of some LPs of a batch launches their blocks only). Per step: the
+// items whose LP is on, in the plan's order, and for each of the five per-item
+// counts (trsm tiles, update tiles, 128x128 blocks, 128x64 blocks, digit rows) the
+// kept items' counts summed again from 0 into `prefix`, the step's offsets pointing
+// there and its totals recomputed; steps left without items are dropped. level_ptr
+// (nlevels + 1) indexes `steps` per level.
+struct RestrictedSteps {
+    std::vector<PlanStep> steps;
+    std::vector<int> level_ptr, items, prefix;
+};
+void restrict_steps(const FrontPlan& plan, const std::vector<int>& sn_lp, const std::vector<int>& on,
+                    RestrictedSteps& out);
+
 }  // namespace ipm
 }  // namespace sankhya
