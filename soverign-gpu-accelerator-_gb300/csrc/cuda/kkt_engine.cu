@@ -931,8 +931,8 @@ __global__ void __launch_bounds__(256, 2) k_update_oz(StepArgs a, const int* __r
 // values, Linv = the inverse of the factored diagonal tile): k_oz_digits writes the
 // digits of B before the solve, k_oz_linv_digits those of the 64 rows of Linv of
 // every item of the step (one block per item, rows i * 64 .. in a buffer of its own),
-// and k_trsm_oz forms X = u 2^(Ea+Eb-52) per 128-row block with the MMAs of
-// k_update_oz (N = 64 = the Linv rows) and no C operand.
+// and k_trsm_oz forms X = u 2^(Ea+Eb-52) with the MMAs of k_update_oz and no C
+// operand: two blocks per 128 panel rows, each taking 32 of the 64 Linv rows (N = 32).
 __global__ void __launch_bounds__(256) k_oz_linv_digits(StepArgs a, const int* __restrict__ items, PlanDev pd,
                                                         const double* __restrict__ Linv,
                                                         const int64_t* __restrict__ inv_off,
