@@ -421,12 +421,20 @@ def heldout_comparison(sk, net, count, batch):
 def update_roofline(prof, kernel, peak, src, workload):
     u = prof["update"]
     ach = prof["update_flops"] / (u["ms"] / 1000.0) / 1e12 if u["ms"] > 0 else 0.0
-    return {"kernel": "%s (%s)" % (kernel, workload), "bound": "tensor", "achieved": ach, "peak": peak,
-            "unit": "TFLOP/s", "frac": ach / peak,
-            "peak_source": "%s bf16 dense tensor peak (MEASURED_PEAKS.json bf16_tflops)" % src, "traffic": None,
-            "launches": u["launches"], "ms_total": u["ms"], "algorithmic_flops": prof["update_flops"],
-            "note": "FP64 flops of the trailing updates (sum over fronts of 2 w t(t+1)/2 per tile step) over the "
-                    "update class's event-timed duration in an instrumented replay of one factorisation"}
+    out = {"kernel": "%s (%s)" % (kernel, workload), "bound": "tensor", "achieved": ach, "peak": peak,
+           "unit": "TFLOP/s", "frac": ach / peak,
+           "peak_source": "%s bf16 dense tensor peak (MEASURED_PEAKS.json bf16_tflops)" % src, "traffic": None,
+           "launches": u["launches"], "ms_total": u["ms"], "algorithmic_flops": prof["update_flops"],
+           "note": "FP64 flops of the trailing updates (sum over fronts of 2 w t(t+1)/2 per tile step) over the "
+                   "update class's event-timed duration in an instrumented replay of one factorisation"}
+    mma = prof.get("mma_flops")
+    if mma and u["ms"] > 0:
+        # the work the tensor cores run for those flops: TF32 x3 three products, the emulated FP64
+        # update 28 BF16 digit-pair products, over 128 x 64 blocks with K padded to 64
+        out["executed_tflops"] = mma / (u["ms"] / 1000.0) / 1e12
+        out["executed_frac"] = out["executed_tflops"] / peak
+        out["executed_flops"] = mma
+    return out
 
 
 def solve_roofline(prof, nnz_factor, elem, hbm, src, workload, kernel):

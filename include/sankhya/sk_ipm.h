@@ -166,9 +166,13 @@ void sk_solver_destroy(sk_solver* h);
  * bytes the update launches must move at least (each input tile read once, each
  * output tile read and written once); with cap >= 17, out[16] = algorithmic bytes
  * of the assembly launches (A or the Khatri-Rao map read once, Theta read once,
- * each normal-matrix entry written once, the diagonal and D written once).
- * fp32: 0 = FP64 fronts, 1 = FP32 fronts with tensor-core (tcgen05) updates, 2 =
- * FP32 fronts with SIMT updates. Returns the number of values written (16 or 17).
+ * each normal-matrix entry written once, the diagonal and D written once); with
+ * cap >= 18, out[17] = flops the tensor cores execute in the update launches (per
+ * 128 x 64 block of the lower part with K padded to 64: three TF32 products for FP32
+ * fronts, 28 BF16 digit-pair products for FP64 fronts on the tensor cores; 0 for
+ * SIMT updates). fp32: 0 = FP64 fronts, 1 = FP32 fronts with tensor-core (tcgen05)
+ * updates, 2 = FP32 fronts with SIMT updates. Returns the number of values written
+ * (16, 17 or 18).
  * No reference counterpart. */
 int sk_solver_profile(sk_solver* h, int fp32, double* out, int cap);
 

@@ -403,9 +403,9 @@ int sk_solver_profile(sk_solver* h, int fp32, double* out, int cap) {
     api::clear_error();
     if (!h || !out || cap < 16) return -SK_ERR_INVALID;
     try {
-        double all[17];
+        double all[18];
         h->ipm->profile(fp32 != 0, fp32 == 1, all);
-        const int nv = cap >= 17 ? 17 : 16;
+        const int nv = cap >= 18 ? 18 : (cap >= 17 ? 17 : 16);
         for (int q = 0; q < nv; ++q) out[q] = all[q];
         return nv;
     } catch (...) {

@@ -666,7 +666,7 @@ DeviceIPM::DeviceIPM(const std::vector<ipm::LpView>& lps, const std::vector<cons
     setup_ms_ = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }
 
-void DeviceIPM::profile(bool fp32, bool tensor, double* out17) {
+void DeviceIPM::profile(bool fp32, bool tensor, double* out18) {
     Impl& I = *im_;
     std::vector<double> ones(I.nlp, 1.0);
     I.put_scalars(0, ones);
@@ -674,7 +674,7 @@ void DeviceIPM::profile(bool fp32, bool tensor, double* out17) {
     k_fill<<<nblk(I.M), 256, 0, I.st>>>(I.M, I.r.ptr, 1.0);
     kkt_->set_active(std::vector<char>(I.nlp, 1));   // every front, whatever the last run left on
     kkt_->set_tensor_update(tensor);
-    kkt_->profile(I.theta.ptr, fp32 ? 1e-7 : 1e-9, fp32, I.r.ptr, I.corr.ptr, out17);
+    kkt_->profile(I.theta.ptr, fp32 ? 1e-7 : 1e-9, fp32, I.r.ptr, I.corr.ptr, out18);
 }
 
 DeviceIPM::~DeviceIPM() {

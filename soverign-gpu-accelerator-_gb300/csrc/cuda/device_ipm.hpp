@@ -50,7 +50,7 @@ public:
     const double* capture_y() const;
     void run();
     // Kernel-class breakdown at the current iterate (see sk_solver_profile).
-    void profile(bool fp32, bool tensor, double* out17);
+    void profile(bool fp32, bool tensor, double* out18);
     void result(int lp, double* x, double* y, double* s, sk_info* info) const;
     int num_lps() const { return nlp_; }
     const ipm::FrontPlan& plan() const { return kkt_->plan(); }

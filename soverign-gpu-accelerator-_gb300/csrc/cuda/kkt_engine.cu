@@ -1629,6 +1629,7 @@ struct KktEngine::Prof {
     cudaStream_t st;
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev;
     double upd_flops = 0.0, upd_bytes = 0.0;
+    double mma_flops = 0.0;   // flops the tensor cores execute in the update launches
     template <class F>
     void timed(int cls, F&& launch) {
         cudaEvent_t a, b;
@@ -1943,6 +1944,11 @@ void KktEngine::launch_factor(T* F, T* Linv, Prof* prof, const SubSteps* sub) {
                         prof->upd_flops += 2.0 * w * t * (t + 1.0) / 2.0;
                         prof->upd_bytes += sizeof(T) * (t * w + 2.0 * t * (t + 1.0) / 2.0);
                     }
+                    // per 128 x 64 block of the lower part, K padded to 64: TF32 x3 runs
+                    // three products, the emulated FP64 update 28 BF16 digit-pair products
+                    const double blk = 2.0 * 128 * 64 * 64 * static_cast<double>(st.upd3_blocks);
+                    if (std::is_same<T, float>::value && tensor_) prof->mma_flops += 3.0 * blk;
+                    if (std::is_same<T, double>::value && emulate64_) prof->mma_flops += 28.0 * blk;
                 }
             }
         }
@@ -2255,6 +2261,7 @@ void KktEngine::profile(const double* d_theta, double delta, bool fp32, const do
     out[14] = pr.upd_flops;
     out[15] = pr.upd_bytes;
     out[16] = assembly_bytes(fp32 ? sizeof(float) : sizeof(double));
+    out[17] = pr.mma_flops;
 }
 
 double KktEngine::assembly_bytes(size_t elem) const {

@@ -71,7 +71,8 @@ public:
 
     // Diagnostics: one factorisation + one solve (of d_rhs) without graphs, with
     // CUDA events around every launch; fills out[17] as sk_solver_profile documents.
-    void profile(const double* d_theta, double delta, bool fp32, const double* d_rhs, double* d_out, double* out);
+    void profile(const double* d_theta, double delta, bool fp32, const double* d_rhs, double* d_out,
+                 double* out);   // out: 18 values (sk_solver_profile)
 
     bool last_fp32() const { return fp32_; }
     int failed_supernode() const { return failed_sn_; }

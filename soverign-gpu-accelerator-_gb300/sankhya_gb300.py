@@ -419,8 +419,8 @@ class Solver:
 
     def profile(self, fp32=True, tensor=True):
         """Kernel-class breakdown; fp32 fronts use tensor-core updates unless tensor=False."""
-        out = np.zeros(17)
-        n = lib().sk_solver_profile(self.h, (1 if tensor else 2) if fp32 else 0, out, 17)
+        out = np.zeros(18)
+        n = lib().sk_solver_profile(self.h, (1 if tensor else 2) if fp32 else 0, out, 18)
         if n < 0:
             raise RuntimeError("sk_solver_profile failed (%d): %s" % (n, last_error()))
         names = ["assembly", "potrf", "trsm", "update", "extend_add", "fwd_solve", "bwd_solve"]
@@ -428,6 +428,7 @@ class Solver:
         d["update_flops"] = out[14]
         d["update_min_bytes"] = out[15]
         d["assembly_bytes"] = out[16] if n >= 17 else None
+        d["mma_flops"] = out[17] if n >= 18 else None
         return d
 
     def close(self):
